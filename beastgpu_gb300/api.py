@@ -1,0 +1,240 @@
+"""Host-side mirror of BEASTGPU's `assemble_gpu` interface over the C ABI.
+
+    Z = assemble_gpu(op, X, Y, config, GpuWriteBackTrueInstance(); quadstrat=...)
+
+follows assemble_gpu(operator, test_functions, trial_functions, config, writeBackStrategy;
+storage_policy, threading, quadstrat) (assamble_gpu.jl:8,25): it returns the dense complex
+Galerkin matrix with test functions as rows and trial functions as columns.  `assemble`
+mirrors BEAST.assemble(op, X, Y; quadstrat).  Both write-back strategies of the reference give
+the same matrix here: the gather write is always done on the GPU (no FP64 atomics), and the
+matrix is copied to the host (column-major, Julia's layout) unless `out="device"`.
+
+Everything runs through libbeastgb.so; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from .operators import Operator, QuadStrat, defaultquadstrat
+from .spaces import Space
+
+# ---- write-back strategies (CustomDataStructs/GpuWriteBack.jl) -----------------------------
+
+
+class GpuWriteBack:
+    pass
+
+
+class GpuWriteBackTrue(GpuWriteBack):
+    """Matrix assembled in device memory, then copied to the host (reference default)."""
+
+
+class GpuWriteBackFalse(GpuWriteBack):
+    """Reference: per-pair blocks copied to the host and scattered there.  Here the scatter is
+    a deterministic gather on the GPU for both strategies, so the result is identical."""
+
+
+def GpuWriteBackTrueInstance():
+    return GpuWriteBackTrue()
+
+
+def GpuWriteBackFalseInstance():
+    return GpuWriteBackFalse()
+
+
+@dataclass
+class GPUConfiguration:
+    """The fields of the reference's GPUConfiguration (utils/configuration.jl:11-26) that mean
+    something on one GB300, plus the precision mode and tile choice.
+
+    precision: "fp64" (plain all-FP64 kernels, the drop-in) or "mixed" (FP32 far pairs with
+    double-float phase base, FP64 singular and near pairs).
+    total_GPU_budget: HBM bytes the call may use for the output staging (0 = 90% of free);
+    host outputs larger than half of it are produced in row blocks.
+    """
+    writeBackStrategy: GpuWriteBack = None
+    precision: str = "fp64"
+    device: int = 0
+    total_GPU_budget: int = 0
+    tile_config: int = -1
+    makeCompexWithGPU: bool = True
+
+    def __post_init__(self):
+        if self.writeBackStrategy is None:
+            self.writeBackStrategy = GpuWriteBackTrueInstance()
+        if self.precision not in ("fp64", "mixed"):
+            raise ValueError("precision must be 'fp64' or 'mixed'")
+
+
+_handles = {}
+_hlock = threading.Lock()
+
+
+class Handle:
+    """Owns one bgb_handle (device scratch, streams)."""
+
+    def __init__(self, device: int = 0, hbm_budget: int = 0, tile_config: int = -1):
+        lib = _lib.load()
+        self.ptr = C.c_void_p()
+        cfg = _lib.Config(device, int(hbm_budget), 0, int(tile_config), 0)
+        _lib.check(lib.bgb_create(C.byref(self.ptr), C.byref(cfg)))
+        self.device = device
+
+    def close(self):
+        if self.ptr:
+            _lib.load().bgb_destroy(self.ptr)
+            self.ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def get_handle(device: int = 0, hbm_budget: int = 0, tile_config: int = -1) -> Handle:
+    key = (device, int(hbm_budget), int(tile_config))
+    with _hlock:
+        h = _handles.get(key)
+        if h is None:
+            h = Handle(device, hbm_budget, tile_config)
+            _handles[key] = h
+        return h
+
+
+class _Keep:
+    def __init__(self):
+        self.refs = []
+
+    def ptr(self, a, dtype):
+        a = np.ascontiguousarray(a, dtype=dtype)
+        self.refs.append(a)
+        return a.ctypes.data
+
+
+def c_space(space: Space, keep: _Keep) -> _lib.Space:
+    m = space.mesh
+    return _lib.Space(space.refspace, m.nv, m.nt, space.nfun, keep.ptr(m.vertices, np.float64),
+                      keep.ptr(m.triangles, np.int32), keep.ptr(space.fn_index, np.int32),
+                      keep.ptr(space.fn_coef, np.float64))
+
+
+def c_operator(op: Operator) -> _lib.Operator:
+    a, b, g = complex(op.alpha), complex(op.beta), complex(op.gamma)
+    return _lib.Operator(op.kind, (C.c_double * 2)(a.real, a.imag), (C.c_double * 2)(b.real, b.imag),
+                         (C.c_double * 2)(g.real, g.imag))
+
+
+def c_quadstrat(qs: QuadStrat) -> _lib.QuadStrat:
+    return _lib.QuadStrat(qs.far_test, qs.far_trial, qs.near_test, qs.near_trial, qs.ss_cf, qs.ss_ce, qs.ss_cv)
+
+
+def _precision(p):
+    if isinstance(p, int):
+        return p
+    return {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED}[p]
+
+
+def assemble_gpu(operator: Operator, test_functions: Space, trial_functions: Space, config: GPUConfiguration = None,
+                 writeBackStrategy: GpuWriteBack = None, *, quadstrat: QuadStrat = None, out: str = "host",
+                 dtype=None, rows=None, out_buffer=None, stream=None, return_stats: bool = False):
+    """Dense Galerkin matrix Z[m, n] = <f_m, op g_n> (test rows, trial columns).
+
+    out="host": numpy array in Fortran (column-major) order, complex128 for precision "fp64"
+    and complex64 for "mixed" unless `dtype` says otherwise.  out="device": a torch CUDA
+    tensor view of shape (rows, cols) with column-major strides.  rows=(row0, nrows) assembles
+    a row window.  out_buffer: a preallocated host (numpy or pinned torch) or device (torch)
+    buffer of the right shape/dtype to write into.
+    """
+    config = config or GPUConfiguration()
+    quadstrat = quadstrat or defaultquadstrat(operator, test_functions, trial_functions)
+    prec = _precision(config.precision)
+    if dtype is None:
+        dtype = np.complex128 if prec == _lib.PREC_FP64 else np.complex64
+    dtype = np.dtype(dtype)
+    if dtype not in (np.complex128, np.complex64):
+        raise ValueError("dtype must be complex128 or complex64")
+    c64 = dtype == np.complex128
+    row0, nrows = (0, test_functions.nfun) if rows is None else (int(rows[0]), int(rows[1]))
+    ncols = trial_functions.nfun
+    h = get_handle(config.device, config.total_GPU_budget, config.tile_config)
+    keep = _Keep()
+    cop, ct, cb, cq = c_operator(operator), c_space(test_functions, keep), c_space(trial_functions, keep), \
+        c_quadstrat(quadstrat)
+    stats = _lib.Stats()
+    lib = _lib.load()
+    if out == "host":
+        if out_buffer is None:
+            Z = np.empty((nrows, ncols), dtype=dtype, order="F")
+            ptr = Z.ctypes.data
+        else:
+            Z = out_buffer
+            ptr = Z.data_ptr() if hasattr(Z, "data_ptr") else Z.ctypes.data
+        kind = _lib.OUT_HOST_C64 if c64 else _lib.OUT_HOST_C32
+        _lib.check(lib.bgb_assemble(h.ptr, C.byref(cop), C.byref(ct), C.byref(cb), C.byref(cq), prec, C.c_void_p(ptr),
+                                    kind, max(1, nrows), row0, nrows, None, C.byref(stats)))
+    elif out == "device":
+        import torch
+        tdt = torch.complex128 if c64 else torch.complex64
+        if out_buffer is None:
+            Zt = torch.empty((ncols, max(1, nrows)), dtype=tdt, device=f"cuda:{config.device}")
+        else:
+            Zt = out_buffer
+        st = stream if stream is not None else torch.cuda.current_stream(config.device).cuda_stream
+        kind = _lib.OUT_DEVICE_C64 if c64 else _lib.OUT_DEVICE_C32
+        _lib.check(lib.bgb_assemble(h.ptr, C.byref(cop), C.byref(ct), C.byref(cb), C.byref(cq), prec,
+                                    C.c_void_p(Zt.data_ptr()), kind, max(1, nrows), row0, nrows, C.c_void_p(st),
+                                    C.byref(stats)))
+        Z = Zt.T
+    else:
+        raise ValueError("out must be 'host' or 'device'")
+    return (Z, stats.as_dict()) if return_stats else Z
+
+
+def assemble(operator: Operator, test_functions: Space, trial_functions: Space, *, quadstrat: QuadStrat = None,
+             precision: str = "fp64", **kw):
+    """BEAST.assemble(op, X, Y; quadstrat) on the GPU (host complex matrix)."""
+    return assemble_gpu(operator, test_functions, trial_functions, GPUConfiguration(precision=precision),
+                        quadstrat=quadstrat, **kw)
+
+
+def classify(test_functions: Space, trial_functions: Space, k2: float, block=None, device: int = 0):
+    """Pair classes (0 far, 1 CV, 2 CE, 3 CF, 4 near) of a block of triangle pairs on the GPU."""
+    t0, t1, s0, s1 = block or (0, test_functions.mesh.nt, 0, trial_functions.mesh.nt)
+    h = get_handle(device)
+    keep = _Keep()
+    out = np.empty((t1 - t0, s1 - s0), dtype=np.int8)
+    _lib.check(_lib.load().bgb_classify_block(h.ptr, C.byref(c_space(test_functions, keep)),
+                                              C.byref(c_space(trial_functions, keep)), float(k2), t0, t1, s0, s1,
+                                              out.ctypes.data))
+    return out
+
+
+def local_matrices(operator: Operator, test_functions: Space, trial_functions: Space, tau, sigma, *,
+                   quadstrat: QuadStrat = None, precision: str = "fp64", force_class: int = -1, device: int = 0):
+    """3x3 local matrices L[p, i, j] of explicit triangle pairs and their classes."""
+    quadstrat = quadstrat or defaultquadstrat()
+    tau = np.ascontiguousarray(tau, dtype=np.int32)
+    sigma = np.ascontiguousarray(sigma, dtype=np.int32)
+    h = get_handle(device)
+    keep = _Keep()
+    out = np.empty((tau.size, 3, 3, 2), dtype=np.float64)
+    cls = np.empty(tau.size, dtype=np.int8)
+    _lib.check(_lib.load().bgb_local_matrices(
+        h.ptr, C.byref(c_operator(operator)), C.byref(c_space(test_functions, keep)),
+        C.byref(c_space(trial_functions, keep)), C.byref(c_quadstrat(quadstrat)), _precision(precision), tau.size,
+        tau.ctypes.data, sigma.ctypes.data, int(force_class), out.ctypes.data, cls.ctypes.data))
+    return out[..., 0] + 1j * out[..., 1], cls
+
+
+def measure_issue_peaks(device: int = 0):
+    """(FP32 TFLOP/s, FP64 TFLOP/s, MUFU Tops/s) measured on the device."""
+    h = get_handle(device)
+    a, b, c = C.c_double(), C.c_double(), C.c_double()
+    _lib.check(_lib.load().bgb_measure_issue_peaks(h.ptr, C.byref(a), C.byref(b), C.byref(c)))
+    return a.value, b.value, c.value

@@ -1,0 +1,87 @@
+// Far-pair dispatch (precision x operator x rule instance) and record preparation.
+#include "bgb_far_impl.cuh"
+
+namespace bgb {
+namespace farimpl {
+BGB_FAR_EXTERN(PMixed, 0)
+BGB_FAR_EXTERN(PMixed, 1)
+BGB_FAR_EXTERN(PMixed, 2)
+BGB_FAR_EXTERN(PFp64, 0)
+BGB_FAR_EXTERN(PFp64, 1)
+BGB_FAR_EXTERN(PFp64, 2)
+
+template <class P, int QT, int QB>
+static int dispatch_op(const FarConst& K, const TilePlan& p, cudaStream_t st) {
+  switch (K.op_kind) {
+    case BGB_OP_HELMHOLTZ3D_SL: return launch_tiles_t<P, BGB_OP_HELMHOLTZ3D_SL, QT, QB>(K, p, st);
+    case BGB_OP_MAXWELL3D_SL: return launch_tiles_t<P, BGB_OP_MAXWELL3D_SL, QT, QB>(K, p, st);
+    case BGB_OP_MAXWELL3D_DL: return launch_tiles_t<P, BGB_OP_MAXWELL3D_DL, QT, QB>(K, p, st);
+  }
+  set_error("unknown operator kind %d", K.op_kind);
+  return BGB_ERR_INVALID;
+}
+
+template <class P, int QT, int QB>
+static int dispatch_diag(const FarConst& K, const void* rt, const void* rb, const int* tau, const int* sigma,
+                         int64_t n, double2* out, cudaStream_t st) {
+  switch (K.op_kind) {
+    case BGB_OP_HELMHOLTZ3D_SL: return launch_diag_t<P, BGB_OP_HELMHOLTZ3D_SL, QT, QB>(K, rt, rb, tau, sigma, n, out, st);
+    case BGB_OP_MAXWELL3D_SL: return launch_diag_t<P, BGB_OP_MAXWELL3D_SL, QT, QB>(K, rt, rb, tau, sigma, n, out, st);
+    case BGB_OP_MAXWELL3D_DL: return launch_diag_t<P, BGB_OP_MAXWELL3D_DL, QT, QB>(K, rt, rb, tau, sigma, n, out, st);
+  }
+  set_error("unknown operator kind %d", K.op_kind);
+  return BGB_ERR_INVALID;
+}
+}  // namespace farimpl
+
+using namespace farimpl;
+
+int far_generic_q(int qt, int qb) { return !(qt == 3 && qb == 4); }
+
+int rec_stride(int precision, int q, int generic) {
+  const int Q = generic ? BGB_MAXQ : q;
+  return precision == BGB_PREC_MIXED ? 17 + 4 * Q : 13 + 4 * Q;
+}
+
+size_t far_smem_bytes(int precision, int qt, int qb, const TilePlan& p) {
+  const bool gen = far_generic_q(qt, qb);
+  if (precision == BGB_PREC_MIXED)
+    return gen ? smem_t<PMixed, 0, BGB_MAXQ, BGB_MAXQ>(p) : smem_t<PMixed, 0, 3, 4>(p);
+  return gen ? smem_t<PFp64, 0, BGB_MAXQ, BGB_MAXQ>(p) : smem_t<PFp64, 0, 3, 4>(p);
+}
+
+int launch_far_tiles(int precision, const FarConst& k, const TilePlan& p, cudaStream_t st) {
+  const bool gen = far_generic_q(k.qt, k.qb);
+  if (precision == BGB_PREC_MIXED)
+    return gen ? dispatch_op<PMixed, BGB_MAXQ, BGB_MAXQ>(k, p, st) : dispatch_op<PMixed, 3, 4>(k, p, st);
+  return gen ? dispatch_op<PFp64, BGB_MAXQ, BGB_MAXQ>(k, p, st) : dispatch_op<PFp64, 3, 4>(k, p, st);
+}
+
+int launch_far_pairs_diag(int precision, const FarConst& k, const void* rt, const void* rb, const int* tau,
+                          const int* sigma, int64_t n, double2* out, cudaStream_t st) {
+  const bool gen = far_generic_q(k.qt, k.qb);
+  if (precision == BGB_PREC_MIXED)
+    return gen ? dispatch_diag<PMixed, BGB_MAXQ, BGB_MAXQ>(k, rt, rb, tau, sigma, n, out, st)
+               : dispatch_diag<PMixed, 3, 4>(k, rt, rb, tau, sigma, n, out, st);
+  return gen ? dispatch_diag<PFp64, BGB_MAXQ, BGB_MAXQ>(k, rt, rb, tau, sigma, n, out, st)
+             : dispatch_diag<PFp64, 3, 4>(k, rt, rb, tau, sigma, n, out, st);
+}
+
+void launch_prepare_rec(int precision, int side, int q, const Geo64* g, int nt, const RuleTable& rules, int rule,
+                        double wscale, void* out, cudaStream_t st) {
+  (void)side;
+  if (nt <= 0) return;
+  const int blocks = (nt + 127) / 128;
+  const bool gen = (q == BGB_MAXQ);
+  if (precision == BGB_PREC_MIXED) {
+    if (gen) k_prepare_rec32<BGB_MAXQ><<<blocks, 128, 0, st>>>(g, nt, rules, rule, wscale, (float*)out);
+    else if (q == 3) k_prepare_rec32<3><<<blocks, 128, 0, st>>>(g, nt, rules, rule, wscale, (float*)out);
+    else k_prepare_rec32<4><<<blocks, 128, 0, st>>>(g, nt, rules, rule, wscale, (float*)out);
+  } else {
+    if (gen) k_prepare_rec64<BGB_MAXQ><<<blocks, 128, 0, st>>>(g, nt, rules, rule, wscale, (double*)out);
+    else if (q == 3) k_prepare_rec64<3><<<blocks, 128, 0, st>>>(g, nt, rules, rule, wscale, (double*)out);
+    else k_prepare_rec64<4><<<blocks, 128, 0, st>>>(g, nt, rules, rule, wscale, (double*)out);
+  }
+}
+
+}  // namespace bgb

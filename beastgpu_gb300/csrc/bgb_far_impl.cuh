@@ -1,0 +1,753 @@
+// Far-pair tile kernels (plain FP64 and mixed FP32) with the deterministic gather write.
+//
+// A CTA owns one output tile: a block of test functions (rows) x a block of trial
+// functions (columns), both taken from a Morton-ordered sweep so their supports are compact.
+// It stages the triangles supporting those functions ("halo" included) in shared memory,
+// sweeps the trial triangles in chunks, computes the 3x3 local matrix of every (test
+// triangle, trial triangle) pair of the chunk into shared memory, and then lets each thread
+// add the chunk's contributions to the output entries it owns.  Every entry Z[m, n]
+// therefore accumulates its contributions in one fixed order -- trial triangle ascending,
+// then test triangle ascending -- no matter how the tiles are shaped: results are
+// bit-identical across tile configurations and runs, with no atomics.  Each output entry is
+// written exactly once.  Non-far pairs (singular or near, found by the classifier) are
+// taken from the FP64 singular-pair buffer instead of the far rule.
+//
+// Roofline: compute-bound on FP32 issue (mixed) or FP64 issue (plain), plus MUFU
+// (rsqrt, rcp, sin, cos).  Per point pair the mixed kernel spends ~23 FP32 ops + 4 MUFU on
+// the kernel value and 13 (Helmholtz / EFIE) or ~26 (MFIE) on accumulation.
+//
+// Mixed precision (FP32) keeps the phase k R accurate without FP64: per pair, the centroid
+// distance D = c_tau - c_sigma is formed in double-float, R0 is any FP32 number close to |D|,
+// and phi0 = k R0 mod 2 pi is reduced exactly (Dekker product + Cody-Waite); per point pair
+// only delta = R - R0 = q / (R + R0) with q = |D_hi + s|^2 - R0^2 computed cancellation-free
+// in FP32 enters the phase (psi = phi0 + k delta), so the absolute phase error stays ~1e-7
+// rad regardless of k R.  Shape functions use coordinates relative to each triangle's
+// centroid, so the EFIE/MFIE bilinear forms carry no cancellation either.
+// Far-pair kernel templates; instantiated per precision and operator in bgb_far_*_op*.cu.
+#pragma once
+#include "bgb_kernels.cuh"
+
+#include <algorithm>
+
+namespace bgb {
+namespace farimpl {
+
+constexpr double kTwoPi = 6.283185307179586476925286766559;
+constexpr float kPiA = 6.28125f;
+constexpr float kPiB = (float)(kTwoPi - 6.28125);
+constexpr float kPiC = (float)(kTwoPi - 6.28125 - (double)(float)(kTwoPi - 6.28125));
+constexpr float kInv2Pi = (float)(1.0 / kTwoPi);
+constexpr int kThreads = 256;
+
+template <int Q>
+struct Off32 {
+  static constexpr int CH = 0, CL = 3, RAD = 6, INV2A = 7, X = 8, W = 8 + 3 * Q, VO = 8 + 4 * Q, SIZE = 17 + 4 * Q;
+};
+template <int Q>
+struct Off64 {
+  static constexpr int C = 0, X = 3, W = 3 + 3 * Q, VO = 3 + 4 * Q, INV2A = 12 + 4 * Q, SIZE = 13 + 4 * Q;
+};
+
+struct PMixed {
+  using R = float;
+  using C = float2;
+  template <int Q>
+  static constexpr int rec() { return Off32<Q>::SIZE; }
+  static __device__ __forceinline__ C mk(double a, double b) { return make_float2((float)a, (float)b); }
+};
+struct PFp64 {
+  using R = double;
+  using C = double2;
+  template <int Q>
+  static constexpr int rec() { return Off64<Q>::SIZE; }
+  static __device__ __forceinline__ C mk(double a, double b) { return make_double2(a, b); }
+};
+
+// ----------------------------------------------------------------------------------------
+// Mixed FP32 far pair
+// ----------------------------------------------------------------------------------------
+template <int OP, int QT, int QB>
+__device__ __forceinline__ void far_pair_mixed(const FarConst& K, const float* __restrict__ a,
+                                               const float* __restrict__ b, float2 L[9]) {
+  using OA = Off32<QT>;
+  using OB = Off32<QB>;
+  float Dh[3], Dl[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    float s, e;
+    two_sum(a[OA::CH + c], -b[OB::CH + c], s, e);
+    e = __fadd_rn(e, __fsub_rn(a[OA::CL + c], b[OB::CL + c]));
+    fast_two_sum(s, e, Dh[c], Dl[c]);
+  }
+  const float n2 = fmaf(Dh[0], Dh[0], fmaf(Dh[1], Dh[1], Dh[2] * Dh[2]));
+  const float R0 = n2 * rsqrtf(n2);
+  // c0 = |D_hi|^2 - R0^2, exact to double-float accuracy
+  float p0, e0, p1, e1, p2, e2, s1, f1, s2, f2, r2h, r2l;
+  two_prod(Dh[0], Dh[0], p0, e0);
+  two_prod(Dh[1], Dh[1], p1, e1);
+  two_prod(Dh[2], Dh[2], p2, e2);
+  two_sum(p0, p1, s1, f1);
+  two_sum(s1, p2, s2, f2);
+  const float lo = __fadd_rn(__fadd_rn(__fadd_rn(f1, f2), __fadd_rn(e0, e1)), e2);
+  two_prod(R0, R0, r2h, r2l);
+  const float c0 = __fadd_rn(__fsub_rn(s2, r2h), __fsub_rn(lo, r2l));
+  // phi0 = k R0 mod 2 pi
+  float ph, pl;
+  two_prod(K.k_hi, R0, ph, pl);
+  pl = fmaf(K.k_lo, R0, pl);
+  const float nq = rintf(ph * kInv2Pi);
+  float phi0 = fmaf(-nq, kPiA, ph);
+  phi0 = fmaf(-nq, kPiB, phi0);
+  phi0 = fmaf(-nq, kPiC, phi0);
+  phi0 = __fadd_rn(phi0, pl);
+  const float R0sq = R0 * R0;
+  const float D2x = 2.f * Dh[0], D2y = 2.f * Dh[1], D2z = 2.f * Dh[2];
+  const float kh = K.k_hi;
+  const float amp0 = K.lossy ? __expf(-K.gre * R0) : 1.f;
+  const int qt = QT < BGB_MAXQ ? QT : K.qt;
+  const int qb = QB < BGB_MAXQ ? QB : K.qb;
+
+  // accumulators
+  float2 S = make_float2(0.f, 0.f), P0 = make_float2(0.f, 0.f);
+  float2 Px[3], Py[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) Px[c] = Py[c] = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) L[k] = make_float2(0.f, 0.f);
+
+#pragma unroll
+  for (int I = 0; I < QT; ++I) {
+    if (I >= qt) break;
+    const float Xx = a[OA::X + 3 * I], Xy = a[OA::X + 3 * I + 1], Xz = a[OA::X + 3 * I + 2];
+    const float ax = Dl[0] + Xx, ay = Dl[1] + Xy, az = Dl[2] + Xz;
+    const float wI = a[OA::W + I];
+    float2 TI = make_float2(0.f, 0.f);
+    float2 UI[3], EI[3], BI[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) UI[c] = EI[c] = BI[c] = make_float2(0.f, 0.f);
+    float2 M[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) M[c] = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int J = 0; J < QB; ++J) {
+      if (J >= qb) break;
+      const float Yx = b[OB::X + 3 * J], Yy = b[OB::X + 3 * J + 1], Yz = b[OB::X + 3 * J + 2];
+      const float sx = ax - Yx, sy = ay - Yy, sz = az - Yz;
+      const float q = fmaf(sx, D2x + sx, fmaf(sy, D2y + sy, fmaf(sz, D2z + sz, c0)));
+      const float R2 = R0sq + q;
+      const float rs = rsqrtf(R2);
+      const float Rr = R2 * rs;
+      const float delta = __fdividef(q, Rr + R0);
+      float psi = fmaf(kh, delta, phi0);
+      const float nn = rintf(psi * kInv2Pi);
+      psi = fmaf(-nn, kPiA, psi);
+      psi = fmaf(-nn, kPiB, psi);
+      float sn, cs;
+      __sincosf(psi, &sn, &cs);
+      float amp = wI * b[OB::W + J] * rs;
+      if (K.lossy) amp *= amp0 * __expf(-K.gre * delta);
+      const float gr = amp * cs, gi = -amp * sn;
+      if (OP == BGB_OP_HELMHOLTZ3D_SL) {
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const float g = K.shpB[J][j];
+          M[j].x = fmaf(gr, g, M[j].x);
+          M[j].y = fmaf(gi, g, M[j].y);
+        }
+      } else if (OP == BGB_OP_MAXWELL3D_SL) {
+        TI.x += gr;
+        TI.y += gi;
+        UI[0].x = fmaf(gr, Yx, UI[0].x); UI[0].y = fmaf(gi, Yx, UI[0].y);
+        UI[1].x = fmaf(gr, Yy, UI[1].x); UI[1].y = fmaf(gi, Yy, UI[1].y);
+        UI[2].x = fmaf(gr, Yz, UI[2].x); UI[2].y = fmaf(gi, Yz, UI[2].y);
+      } else {
+        // H = -(gamma + 1/R) G / R ; d = x - y
+        const float g2r = gr * rs, g2i = gi * rs;
+        const float re = K.gre + rs;
+        const float Hx = -(re * g2r - kh * g2i), Hy = -(re * g2i + kh * g2r);
+        const float dx = Dh[0] + sx, dy = Dh[1] + sy, dz = Dh[2] + sz;
+        EI[0].x = fmaf(Hx, dx, EI[0].x); EI[0].y = fmaf(Hy, dx, EI[0].y);
+        EI[1].x = fmaf(Hx, dy, EI[1].x); EI[1].y = fmaf(Hy, dy, EI[1].y);
+        EI[2].x = fmaf(Hx, dz, EI[2].x); EI[2].y = fmaf(Hy, dz, EI[2].y);
+        const float c0x = dy * Yz - dz * Yy, c0y = dz * Yx - dx * Yz, c0z = dx * Yy - dy * Yx;
+        BI[0].x = fmaf(Hx, c0x, BI[0].x); BI[0].y = fmaf(Hy, c0x, BI[0].y);
+        BI[1].x = fmaf(Hx, c0y, BI[1].x); BI[1].y = fmaf(Hy, c0y, BI[1].y);
+        BI[2].x = fmaf(Hx, c0z, BI[2].x); BI[2].y = fmaf(Hy, c0z, BI[2].y);
+      }
+    }
+    if (OP == BGB_OP_HELMHOLTZ3D_SL) {
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const float f = K.shpT[I][i];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          L[i * 3 + j].x = fmaf(f, M[j].x, L[i * 3 + j].x);
+          L[i * 3 + j].y = fmaf(f, M[j].y, L[i * 3 + j].y);
+        }
+      }
+    } else if (OP == BGB_OP_MAXWELL3D_SL) {
+      S.x = fmaf(Xx, UI[0].x, fmaf(Xy, UI[1].x, fmaf(Xz, UI[2].x, S.x)));
+      S.y = fmaf(Xx, UI[0].y, fmaf(Xy, UI[1].y, fmaf(Xz, UI[2].y, S.y)));
+      Px[0].x = fmaf(Xx, TI.x, Px[0].x); Px[0].y = fmaf(Xx, TI.y, Px[0].y);
+      Px[1].x = fmaf(Xy, TI.x, Px[1].x); Px[1].y = fmaf(Xy, TI.y, Px[1].y);
+      Px[2].x = fmaf(Xz, TI.x, Px[2].x); Px[2].y = fmaf(Xz, TI.y, Px[2].y);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) { Py[c].x += UI[c].x; Py[c].y += UI[c].y; }
+      P0.x += TI.x;
+      P0.y += TI.y;
+    } else {
+      // C += X x E_I (stored in Px), A1 += X . B_I (stored in S), B += B_I (Py), E += E_I (stored via L[0..2])
+      Px[0].x += Xy * EI[2].x - Xz * EI[1].x; Px[0].y += Xy * EI[2].y - Xz * EI[1].y;
+      Px[1].x += Xz * EI[0].x - Xx * EI[2].x; Px[1].y += Xz * EI[0].y - Xx * EI[2].y;
+      Px[2].x += Xx * EI[1].x - Xy * EI[0].x; Px[2].y += Xx * EI[1].y - Xy * EI[0].y;
+      S.x = fmaf(Xx, BI[0].x, fmaf(Xy, BI[1].x, fmaf(Xz, BI[2].x, S.x)));
+      S.y = fmaf(Xx, BI[0].y, fmaf(Xy, BI[1].y, fmaf(Xz, BI[2].y, S.y)));
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        Py[c].x += BI[c].x; Py[c].y += BI[c].y;
+        L[c].x += EI[c].x; L[c].y += EI[c].y;
+      }
+    }
+  }
+
+  const float2 alpha = make_float2((float)K.alpha[0], (float)K.alpha[1]);
+  if (OP == BGB_OP_HELMHOLTZ3D_SL) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) L[k] = cmulf(alpha, L[k]);
+    return;
+  }
+  const float inv4AA = a[OA::INV2A] * b[OB::INV2A];
+  const float2 ca = make_float2(alpha.x * inv4AA, alpha.y * inv4AA);
+  if (OP == BGB_OP_MAXWELL3D_SL) {
+    const float invAA = 4.f * inv4AA;
+    const float2 cb = make_float2((float)K.beta[0] * invAA, (float)K.beta[1] * invAA);
+    const float2 tb = cmulf(cb, P0);
+    float2 av[3], bv[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const float vx = a[OA::VO + 3 * i], vy = a[OA::VO + 3 * i + 1], vz = a[OA::VO + 3 * i + 2];
+      av[i].x = vx * Py[0].x + vy * Py[1].x + vz * Py[2].x;
+      av[i].y = vx * Py[0].y + vy * Py[1].y + vz * Py[2].y;
+      const float wx = b[OB::VO + 3 * i], wy = b[OB::VO + 3 * i + 1], wz = b[OB::VO + 3 * i + 2];
+      bv[i].x = wx * Px[0].x + wy * Px[1].x + wz * Px[2].x;
+      bv[i].y = wx * Px[0].y + wy * Px[1].y + wz * Px[2].y;
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const float vw = a[OA::VO + 3 * i] * b[OB::VO + 3 * j] + a[OA::VO + 3 * i + 1] * b[OB::VO + 3 * j + 1] +
+                         a[OA::VO + 3 * i + 2] * b[OB::VO + 3 * j + 2];
+        float2 t;
+        t.x = S.x - av[i].x - bv[j].x + vw * P0.x;
+        t.y = S.y - av[i].y - bv[j].y + vw * P0.y;
+        const float2 r = cmulf(ca, t);
+        L[i * 3 + j] = make_float2(r.x + tb.x, r.y + tb.y);
+      }
+    return;
+  }
+  // MFIE: L = alpha/(4AA) (A1 - W_j . C - V_i . B + V_i . (E x W_j))
+  const float2 E0 = L[0], E1 = L[1], E2 = L[2];
+  float2 vb[3], wc[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const float vx = a[OA::VO + 3 * i], vy = a[OA::VO + 3 * i + 1], vz = a[OA::VO + 3 * i + 2];
+    vb[i].x = vx * Py[0].x + vy * Py[1].x + vz * Py[2].x;
+    vb[i].y = vx * Py[0].y + vy * Py[1].y + vz * Py[2].y;
+    const float wx = b[OB::VO + 3 * i], wy = b[OB::VO + 3 * i + 1], wz = b[OB::VO + 3 * i + 2];
+    wc[i].x = wx * Px[0].x + wy * Px[1].x + wz * Px[2].x;
+    wc[i].y = wx * Px[0].y + wy * Px[1].y + wz * Px[2].y;
+  }
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    const float wx = b[OB::VO + 3 * j], wy = b[OB::VO + 3 * j + 1], wz = b[OB::VO + 3 * j + 2];
+    // E x W_j
+    const float2 x0 = make_float2(E1.x * wz - E2.x * wy, E1.y * wz - E2.y * wy);
+    const float2 x1 = make_float2(E2.x * wx - E0.x * wz, E2.y * wx - E0.y * wz);
+    const float2 x2 = make_float2(E0.x * wy - E1.x * wx, E0.y * wy - E1.y * wx);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const float vx = a[OA::VO + 3 * i], vy = a[OA::VO + 3 * i + 1], vz = a[OA::VO + 3 * i + 2];
+      float2 t;
+      t.x = S.x - wc[j].x - vb[i].x + (vx * x0.x + vy * x1.x + vz * x2.x);
+      t.y = S.y - wc[j].y - vb[i].y + (vx * x0.y + vy * x1.y + vz * x2.y);
+      L[i * 3 + j] = cmulf(ca, t);
+    }
+  }
+}
+
+// ----------------------------------------------------------------------------------------
+// Plain FP64 far pair (same accumulation structure, FP64 throughout, CUDA sincos / exp)
+// ----------------------------------------------------------------------------------------
+template <int OP, int QT, int QB>
+__device__ __forceinline__ void far_pair_fp64(const FarConst& K, const double* __restrict__ a,
+                                              const double* __restrict__ b, double2 L[9]) {
+  using OA = Off64<QT>;
+  using OB = Off64<QB>;
+  const double Dx = a[OA::C] - b[OB::C], Dy = a[OA::C + 1] - b[OB::C + 1], Dz = a[OA::C + 2] - b[OB::C + 2];
+  const double gre = K.gamma[0], gim = K.gamma[1];
+  const int qt = QT < BGB_MAXQ ? QT : K.qt;
+  const int qb = QB < BGB_MAXQ ? QB : K.qb;
+  double2 S = make_double2(0, 0), P0 = make_double2(0, 0);
+  double2 Px[3], Py[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) Px[c] = Py[c] = make_double2(0, 0);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) L[k] = make_double2(0, 0);
+#pragma unroll
+  for (int I = 0; I < QT; ++I) {
+    if (I >= qt) break;
+    const double Xx = a[OA::X + 3 * I], Xy = a[OA::X + 3 * I + 1], Xz = a[OA::X + 3 * I + 2];
+    const double ax = Dx + Xx, ay = Dy + Xy, az = Dz + Xz;
+    const double wI = a[OA::W + I];
+    double2 TI = make_double2(0, 0);
+    double2 UI[3], EI[3], BI[3], M[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) UI[c] = EI[c] = BI[c] = M[c] = make_double2(0, 0);
+#pragma unroll
+    for (int J = 0; J < QB; ++J) {
+      if (J >= qb) break;
+      const double Yx = b[OB::X + 3 * J], Yy = b[OB::X + 3 * J + 1], Yz = b[OB::X + 3 * J + 2];
+      const double dx = ax - Yx, dy = ay - Yy, dz = az - Yz;
+      const double R2 = dx * dx + dy * dy + dz * dz;
+      const double R = sqrt(R2);
+      const double rinv = 1.0 / R;
+      double sn = 0.0, cs = 1.0;
+      if (gim != 0.0) sincos(gim * R, &sn, &cs);
+      double amp = wI * b[OB::W + J] * rinv;
+      if (gre != 0.0) amp *= exp(-gre * R);
+      const double gr = amp * cs, gi = -amp * sn;
+      if (OP == BGB_OP_HELMHOLTZ3D_SL) {
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const double g = K.shpB64[J][j];
+          M[j].x = fma(gr, g, M[j].x);
+          M[j].y = fma(gi, g, M[j].y);
+        }
+      } else if (OP == BGB_OP_MAXWELL3D_SL) {
+        TI.x += gr;
+        TI.y += gi;
+        UI[0].x = fma(gr, Yx, UI[0].x); UI[0].y = fma(gi, Yx, UI[0].y);
+        UI[1].x = fma(gr, Yy, UI[1].x); UI[1].y = fma(gi, Yy, UI[1].y);
+        UI[2].x = fma(gr, Yz, UI[2].x); UI[2].y = fma(gi, Yz, UI[2].y);
+      } else {
+        const double g2r = gr * rinv, g2i = gi * rinv;
+        const double re = gre + rinv;
+        const double Hx = -(re * g2r - gim * g2i), Hy = -(re * g2i + gim * g2r);
+        EI[0].x = fma(Hx, dx, EI[0].x); EI[0].y = fma(Hy, dx, EI[0].y);
+        EI[1].x = fma(Hx, dy, EI[1].x); EI[1].y = fma(Hy, dy, EI[1].y);
+        EI[2].x = fma(Hx, dz, EI[2].x); EI[2].y = fma(Hy, dz, EI[2].y);
+        const double c0x = dy * Yz - dz * Yy, c0y = dz * Yx - dx * Yz, c0z = dx * Yy - dy * Yx;
+        BI[0].x = fma(Hx, c0x, BI[0].x); BI[0].y = fma(Hy, c0x, BI[0].y);
+        BI[1].x = fma(Hx, c0y, BI[1].x); BI[1].y = fma(Hy, c0y, BI[1].y);
+        BI[2].x = fma(Hx, c0z, BI[2].x); BI[2].y = fma(Hy, c0z, BI[2].y);
+      }
+    }
+    if (OP == BGB_OP_HELMHOLTZ3D_SL) {
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const double f = K.shpT64[I][i];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          L[i * 3 + j].x = fma(f, M[j].x, L[i * 3 + j].x);
+          L[i * 3 + j].y = fma(f, M[j].y, L[i * 3 + j].y);
+        }
+      }
+    } else if (OP == BGB_OP_MAXWELL3D_SL) {
+      S.x = fma(Xx, UI[0].x, fma(Xy, UI[1].x, fma(Xz, UI[2].x, S.x)));
+      S.y = fma(Xx, UI[0].y, fma(Xy, UI[1].y, fma(Xz, UI[2].y, S.y)));
+      Px[0].x = fma(Xx, TI.x, Px[0].x); Px[0].y = fma(Xx, TI.y, Px[0].y);
+      Px[1].x = fma(Xy, TI.x, Px[1].x); Px[1].y = fma(Xy, TI.y, Px[1].y);
+      Px[2].x = fma(Xz, TI.x, Px[2].x); Px[2].y = fma(Xz, TI.y, Px[2].y);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) { Py[c].x += UI[c].x; Py[c].y += UI[c].y; }
+      P0.x += TI.x;
+      P0.y += TI.y;
+    } else {
+      Px[0].x += Xy * EI[2].x - Xz * EI[1].x; Px[0].y += Xy * EI[2].y - Xz * EI[1].y;
+      Px[1].x += Xz * EI[0].x - Xx * EI[2].x; Px[1].y += Xz * EI[0].y - Xx * EI[2].y;
+      Px[2].x += Xx * EI[1].x - Xy * EI[0].x; Px[2].y += Xx * EI[1].y - Xy * EI[0].y;
+      S.x = fma(Xx, BI[0].x, fma(Xy, BI[1].x, fma(Xz, BI[2].x, S.x)));
+      S.y = fma(Xx, BI[0].y, fma(Xy, BI[1].y, fma(Xz, BI[2].y, S.y)));
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        Py[c].x += BI[c].x; Py[c].y += BI[c].y;
+        L[c].x += EI[c].x; L[c].y += EI[c].y;
+      }
+    }
+  }
+  const double2 alpha = make_double2(K.alpha[0], K.alpha[1]);
+  if (OP == BGB_OP_HELMHOLTZ3D_SL) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) L[k] = cmul(alpha, L[k]);
+    return;
+  }
+  const double inv4AA = a[OA::INV2A] * b[OB::INV2A];
+  const double2 ca = make_double2(alpha.x * inv4AA, alpha.y * inv4AA);
+  if (OP == BGB_OP_MAXWELL3D_SL) {
+    const double invAA = 4.0 * inv4AA;
+    const double2 cb = make_double2(K.beta[0] * invAA, K.beta[1] * invAA);
+    const double2 tb = cmul(cb, P0);
+    double2 av[3], bv[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const double vx = a[OA::VO + 3 * i], vy = a[OA::VO + 3 * i + 1], vz = a[OA::VO + 3 * i + 2];
+      av[i].x = vx * Py[0].x + vy * Py[1].x + vz * Py[2].x;
+      av[i].y = vx * Py[0].y + vy * Py[1].y + vz * Py[2].y;
+      const double wx = b[OB::VO + 3 * i], wy = b[OB::VO + 3 * i + 1], wz = b[OB::VO + 3 * i + 2];
+      bv[i].x = wx * Px[0].x + wy * Px[1].x + wz * Px[2].x;
+      bv[i].y = wx * Px[0].y + wy * Px[1].y + wz * Px[2].y;
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const double vw = a[OA::VO + 3 * i] * b[OB::VO + 3 * j] + a[OA::VO + 3 * i + 1] * b[OB::VO + 3 * j + 1] +
+                          a[OA::VO + 3 * i + 2] * b[OB::VO + 3 * j + 2];
+        double2 t;
+        t.x = S.x - av[i].x - bv[j].x + vw * P0.x;
+        t.y = S.y - av[i].y - bv[j].y + vw * P0.y;
+        const double2 r = cmul(ca, t);
+        L[i * 3 + j] = make_double2(r.x + tb.x, r.y + tb.y);
+      }
+    return;
+  }
+  const double2 E0 = L[0], E1 = L[1], E2 = L[2];
+  double2 vb[3], wc[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const double vx = a[OA::VO + 3 * i], vy = a[OA::VO + 3 * i + 1], vz = a[OA::VO + 3 * i + 2];
+    vb[i].x = vx * Py[0].x + vy * Py[1].x + vz * Py[2].x;
+    vb[i].y = vx * Py[0].y + vy * Py[1].y + vz * Py[2].y;
+    const double wx = b[OB::VO + 3 * i], wy = b[OB::VO + 3 * i + 1], wz = b[OB::VO + 3 * i + 2];
+    wc[i].x = wx * Px[0].x + wy * Px[1].x + wz * Px[2].x;
+    wc[i].y = wx * Px[0].y + wy * Px[1].y + wz * Px[2].y;
+  }
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    const double wx = b[OB::VO + 3 * j], wy = b[OB::VO + 3 * j + 1], wz = b[OB::VO + 3 * j + 2];
+    const double2 x0 = make_double2(E1.x * wz - E2.x * wy, E1.y * wz - E2.y * wy);
+    const double2 x1 = make_double2(E2.x * wx - E0.x * wz, E2.y * wx - E0.y * wz);
+    const double2 x2 = make_double2(E0.x * wy - E1.x * wx, E0.y * wy - E1.y * wx);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const double vx = a[OA::VO + 3 * i], vy = a[OA::VO + 3 * i + 1], vz = a[OA::VO + 3 * i + 2];
+      double2 t;
+      t.x = S.x - wc[j].x - vb[i].x + (vx * x0.x + vy * x1.x + vz * x2.x);
+      t.y = S.y - wc[j].y - vb[i].y + (vx * x0.y + vy * x1.y + vz * x2.y);
+      L[i * 3 + j] = cmul(ca, t);
+    }
+  }
+}
+
+template <class P, int OP, int QT, int QB>
+__device__ __forceinline__ void far_pair(const FarConst& K, const typename P::R* a, const typename P::R* b,
+                                         typename P::C L[9]) {
+  if constexpr (sizeof(typename P::R) == 4)
+    far_pair_mixed<OP, QT, QB>(K, a, b, L);
+  else
+    far_pair_fp64<OP, QT, QB>(K, a, b, L);
+}
+
+__device__ __forceinline__ int64_t find_sigma(const int64_t* __restrict__ off, const int* __restrict__ sig, int tau,
+                                              int sigma) {
+  int64_t lo = off[tau], hi = off[tau + 1];
+  while (lo < hi) {
+    int64_t mid = (lo + hi) >> 1;
+    int v = sig[mid];
+    if (v == sigma) return mid;
+    if (v < sigma) lo = mid + 1;
+    else hi = mid;
+  }
+  return -1;
+}
+
+// ----------------------------------------------------------------------------------------
+// Tile kernel
+// ----------------------------------------------------------------------------------------
+template <class P>
+struct Smem {
+  float4* bndT;
+  float4* bndB;
+  int* triT;
+  int* triB;
+  typename P::R* recT;
+  typename P::R* recB;
+  int* fcnt;
+  int* fcode;
+  typename P::R* fcoef;
+  typename P::C* Lbuf;
+  typename P::C* Zs;
+};
+
+__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+template <class P>
+__host__ __device__ inline size_t carve(unsigned char* base, int tmax, int nmax, int rt, int rb, int FM, int FN,
+                                        int MAXS, int SC, Smem<P>* s) {
+  using R = typename P::R;
+  using C = typename P::C;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    size_t o = off;
+    off = align16(off + bytes);
+    return base ? base + o : nullptr;
+  };
+  unsigned char* p;
+  p = take(sizeof(float4) * tmax); if (s) s->bndT = (float4*)p;
+  p = take(sizeof(float4) * nmax); if (s) s->bndB = (float4*)p;
+  p = take(sizeof(int) * tmax); if (s) s->triT = (int*)p;
+  p = take(sizeof(int) * nmax); if (s) s->triB = (int*)p;
+  p = take(sizeof(R) * (size_t)tmax * rt); if (s) s->recT = (R*)p;
+  p = take(sizeof(R) * (size_t)nmax * rb); if (s) s->recB = (R*)p;
+  p = take(sizeof(int) * FM); if (s) s->fcnt = (int*)p;
+  p = take(sizeof(int) * (size_t)FM * MAXS); if (s) s->fcode = (int*)p;
+  p = take(sizeof(R) * (size_t)FM * MAXS); if (s) s->fcoef = (R*)p;
+  p = take(sizeof(C) * 9 * (size_t)tmax * SC); if (s) s->Lbuf = (C*)p;
+  p = take(sizeof(C) * (size_t)FM * FN); if (s) s->Zs = (C*)p;
+  return off;
+}
+
+template <class P, int OP, int QT, int QB>
+__global__ void __launch_bounds__(kThreads) k_far_tiles(const __grid_constant__ FarConst K,
+                                                        const __grid_constant__ TilePlan p) {
+  using R = typename P::R;
+  using C = typename P::C;
+  constexpr int RT = P::template rec<QT>();
+  constexpr int RB = P::template rec<QB>();
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int tid = threadIdx.x;
+  const int bm = blockIdx.x, bn = blockIdx.y;
+  if (p.abort_flag && *p.abort_flag) return;
+  Smem<P> s;
+  carve<P>(smem, p.tmax, p.nmax, RT, RB, p.FM, p.FN, p.MAXS, p.SC, &s);
+
+  const int t0 = p.tb_off[bm], tm = p.tb_off[bm + 1] - t0;
+  const int b0 = p.bb_off[bn], nbk = p.bb_off[bn + 1] - b0;
+  const int f0 = p.tb_fn_off[bm], fm = p.tb_fn_off[bm + 1] - f0;
+  const int g0 = p.bb_fn_off[bn], fn = p.bb_fn_off[bn + 1] - g0;
+  const R* __restrict__ gRT = (const R*)p.rec_t;
+  const R* __restrict__ gRB = (const R*)p.rec_b;
+
+  for (int i = tid; i < tm; i += kThreads) {
+    const int t = p.tb_tris[t0 + i];
+    s.triT[i] = t;
+    s.bndT[i] = p.bnd_t[t];
+  }
+  for (int i = tid; i < nbk; i += kThreads) {
+    const int t = p.bb_tris[b0 + i];
+    s.triB[i] = t;
+    s.bndB[i] = p.bnd_b[t];
+  }
+  for (int i = tid; i < tm * RT; i += kThreads) {
+    const int r = i / RT, c = i - r * RT;
+    s.recT[i] = gRT[(int64_t)p.tb_tris[t0 + r] * RT + c];
+  }
+  for (int i = tid; i < nbk * RB; i += kThreads) {
+    const int r = i / RB, c = i - r * RB;
+    s.recB[i] = gRB[(int64_t)p.bb_tris[b0 + r] * RB + c];
+  }
+  for (int m = tid; m < fm; m += kThreads) {
+    const int a0 = p.fs_off[f0 + m], a1 = p.fs_off[f0 + m + 1];
+    const int cnt = min(a1 - a0, p.MAXS);
+    s.fcnt[m] = cnt;
+    for (int k = 0; k < cnt; ++k) {
+      s.fcode[m * p.MAXS + k] = p.fs_code[a0 + k];
+      s.fcoef[m * p.MAXS + k] = (R)p.fs_coef[a0 + k];
+    }
+  }
+  for (int i = tid; i < fm * fn; i += kThreads) s.Zs[i] = P::mk(0.0, 0.0);
+  __syncthreads();
+
+  const int LS = p.tmax * p.SC;
+  const int c0 = p.bb_chunk_off[bn], c1 = p.bb_chunk_off[bn + 1];
+  for (int c = c0; c < c1; ++c) {
+    const int sbase = (c - c0) * p.SC;
+    const int scn = min(p.SC, nbk - sbase);
+    const int np = tm * scn;
+    for (int q = tid; q < np; q += kThreads) {
+      const int ti = q / scn, si = q - ti * scn;
+      const int sb = sbase + si;
+      C L[9];
+      bool done = false;
+      if (sphere_candidate(s.bndT[ti], s.bndB[sb])) {
+        const int64_t e = find_sigma(p.sing_off, p.sing_sigma, s.triT[ti], s.triB[sb]);
+        if (e >= 0) {
+#pragma unroll
+          for (int k = 0; k < 9; ++k) {
+            const double2 v = p.sing_L[e * 9 + k];
+            L[k] = P::mk(v.x, v.y);
+          }
+          done = true;
+        }
+      }
+      if (!done) far_pair<P, OP, QT, QB>(K, s.recT + ti * RT, s.recB + sb * RB, L);
+      const int li = ti * p.SC + si;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) s.Lbuf[k * LS + li] = L[k];
+    }
+    __syncthreads();
+    const int gg0 = p.ch_grp_off[c], ng = p.ch_grp_off[c + 1] - gg0;
+    for (int it = tid; it < ng * fm; it += kThreads) {
+      const int g = it / fm, m = it - g * fm;
+      const int gi = gg0 + g;
+      const int n = p.grp_fn[gi];
+      C acc = s.Zs[n * fm + m];
+      const int sb0 = p.grp_sup_off[gi], sb1 = p.grp_sup_off[gi + 1];
+      const int cnt = s.fcnt[m];
+      for (int bsup = sb0; bsup < sb1; ++bsup) {
+        const int code = p.gs_code[bsup];
+        const int sl = (code >> 2) - sbase, j = code & 3;
+        const R cb = (R)p.gs_coef[bsup];
+        for (int a = 0; a < cnt; ++a) {
+          const int fc = s.fcode[m * p.MAXS + a];
+          const int ta = fc >> 2, i = fc & 3;
+          const R w = s.fcoef[m * p.MAXS + a] * cb;
+          const C l = s.Lbuf[(i * 3 + j) * LS + ta * p.SC + sl];
+          acc.x = fma(w, l.x, acc.x);
+          acc.y = fma(w, l.y, acc.y);
+        }
+      }
+      s.Zs[n * fm + m] = acc;
+    }
+    __syncthreads();
+  }
+  for (int i = tid; i < fm * fn; i += kThreads) {
+    const int n = i / fm, m = i - n * fm;
+    const int64_t idx = p.rows[f0 + m] + p.cols[g0 + n] * p.ld;
+    const C v = s.Zs[i];
+    if (p.out_c64) ((double2*)p.out)[idx] = make_double2(v.x, v.y);
+    else ((float2*)p.out)[idx] = make_float2((float)v.x, (float)v.y);
+  }
+}
+
+// ----------------------------------------------------------------------------------------
+// Records
+// ----------------------------------------------------------------------------------------
+template <int Q>
+__global__ void k_prepare_rec32(const Geo64* __restrict__ g, int nt, const __grid_constant__ RuleTable rules, int rule,
+                                double wscale, float* __restrict__ out) {
+  using O = Off32<Q>;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nt) return;
+  const Geo64& T = g[t];
+  float* r = out + (int64_t)t * O::SIZE;
+  double c[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) c[k] = (T.v[0][k] + T.v[1][k] + T.v[2][k]) / 3.0;
+  for (int k = 0; k < 3; ++k) {
+    const float hi = (float)c[k];
+    r[O::CH + k] = hi;
+    r[O::CL + k] = (float)(c[k] - (double)hi);
+  }
+  r[O::RAD] = 0.f;
+  r[O::INV2A] = (float)(1.0 / (2.0 * T.area));
+  const int q = rules.npoints[rule];
+  for (int I = 0; I < Q; ++I) {
+    double u = 0, v = 0, w = 0;
+    if (I < q) {
+      u = rules.uvw[rules.offset[rule] + I][0];
+      v = rules.uvw[rules.offset[rule] + I][1];
+      w = rules.uvw[rules.offset[rule] + I][2];
+    }
+    for (int k = 0; k < 3; ++k) {
+      const double x = (T.v[2][k] + T.t[0][k] * u) + T.t[1][k] * v;
+      r[O::X + 3 * I + k] = (float)(x - c[k]);
+    }
+    r[O::W + I] = (float)((w / 2.0) * (2.0 * T.area) * wscale);
+  }
+  for (int i = 0; i < 3; ++i)
+    for (int k = 0; k < 3; ++k) r[O::VO + 3 * i + k] = (float)(T.v[i][k] - c[k]);
+}
+
+template <int Q>
+__global__ void k_prepare_rec64(const Geo64* __restrict__ g, int nt, const __grid_constant__ RuleTable rules, int rule,
+                                double wscale, double* __restrict__ out) {
+  using O = Off64<Q>;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nt) return;
+  const Geo64& T = g[t];
+  double* r = out + (int64_t)t * O::SIZE;
+  double c[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) c[k] = (T.v[0][k] + T.v[1][k] + T.v[2][k]) / 3.0;
+  for (int k = 0; k < 3; ++k) r[O::C + k] = c[k];
+  const int q = rules.npoints[rule];
+  for (int I = 0; I < Q; ++I) {
+    double u = 0, v = 0, w = 0;
+    if (I < q) {
+      u = rules.uvw[rules.offset[rule] + I][0];
+      v = rules.uvw[rules.offset[rule] + I][1];
+      w = rules.uvw[rules.offset[rule] + I][2];
+    }
+    for (int k = 0; k < 3; ++k) {
+      const double x = (T.v[2][k] + T.t[0][k] * u) + T.t[1][k] * v;
+      r[O::X + 3 * I + k] = x - c[k];
+    }
+    r[O::W + I] = (w / 2.0) * (2.0 * T.area) * wscale;
+  }
+  for (int i = 0; i < 3; ++i)
+    for (int k = 0; k < 3; ++k) r[O::VO + 3 * i + k] = T.v[i][k] - c[k];
+  r[O::INV2A] = 1.0 / (2.0 * T.area);
+}
+
+// Diagnostic kernel: far rule of explicit pairs, one thread per pair, records from HBM.
+template <class P, int OP, int QT, int QB>
+__global__ void k_far_pairs_diag(const __grid_constant__ FarConst K, const typename P::R* __restrict__ rt,
+                                 const typename P::R* __restrict__ rb, const int* __restrict__ tau,
+                                 const int* __restrict__ sigma, int64_t n, double2* __restrict__ out) {
+  constexpr int RT = P::template rec<QT>();
+  constexpr int RB = P::template rec<QB>();
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    typename P::C L[9];
+    far_pair<P, OP, QT, QB>(K, rt + (int64_t)tau[e] * RT, rb + (int64_t)sigma[e] * RB, L);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) out[e * 9 + k] = make_double2(L[k].x, L[k].y);
+  }
+}
+
+template <class P, int OP, int QT, int QB>
+int launch_tiles_t(const FarConst& K, const TilePlan& p, cudaStream_t st) {
+  constexpr int RT = P::template rec<QT>();
+  constexpr int RB = P::template rec<QB>();
+  const size_t bytes = carve<P>(nullptr, p.tmax, p.nmax, RT, RB, p.FM, p.FN, p.MAXS, p.SC, nullptr);
+  auto kern = k_far_tiles<P, OP, QT, QB>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(far tiles)");
+  if (p.n_tblocks <= 0 || p.n_bblocks <= 0) return 0;
+  dim3 grid(p.n_tblocks, p.n_bblocks);
+  kern<<<grid, kThreads, bytes, st>>>(K, p);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "k_far_tiles launch");
+  return 0;
+}
+
+template <class P, int OP, int QT, int QB>
+size_t smem_t(const TilePlan& p) {
+  return carve<P>(nullptr, p.tmax, p.nmax, P::template rec<QT>(), P::template rec<QB>(), p.FM, p.FN, p.MAXS, p.SC,
+                  nullptr);
+}
+
+template <class P, int OP, int QT, int QB>
+int launch_diag_t(const FarConst& K, const void* rt, const void* rb, const int* tau, const int* sigma, int64_t n,
+                  double2* out, cudaStream_t st) {
+  if (n <= 0) return 0;
+  const int blocks = (int)std::min<int64_t>((n + 127) / 128, 65535);
+  using R = typename P::R;
+  k_far_pairs_diag<P, OP, QT, QB><<<blocks, 128, 0, st>>>(K, (const R*)rt, (const R*)rb, tau, sigma, n, out);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? 0 : cuda_fail(e, "k_far_pairs_diag launch");
+}
+
+// Instances live in bgb_far_{mixed,fp64}_op{0,1,2}.cu.
+#define BGB_FAR_EXTERN(P, OP)                                                                                   \
+  extern template int launch_tiles_t<P, OP, 3, 4>(const FarConst&, const TilePlan&, cudaStream_t);             \
+  extern template int launch_tiles_t<P, OP, BGB_MAXQ, BGB_MAXQ>(const FarConst&, const TilePlan&, cudaStream_t); \
+  extern template int launch_diag_t<P, OP, 3, 4>(const FarConst&, const void*, const void*, const int*,        \
+                                                 const int*, int64_t, double2*, cudaStream_t);                \
+  extern template int launch_diag_t<P, OP, BGB_MAXQ, BGB_MAXQ>(const FarConst&, const void*, const void*,      \
+                                                               const int*, const int*, int64_t, double2*,     \
+                                                               cudaStream_t);
+
+}  // namespace farimpl
+}  // namespace bgb

@@ -1,0 +1,92 @@
+// Kernel launch interfaces shared by the translation units of libbeastgb.
+#pragma once
+
+#include "bgb_common.cuh"
+
+namespace bgb {
+
+// ---- bgb_singular.cu -------------------------------------------------------------------
+void launch_prepare_geo64(const double* verts, const int32_t* tris, int nt, Geo64* out, cudaStream_t st);
+void launch_prepare_bounds(const Geo64* g, int nt, double k2, int trial_side, float4* out, cudaStream_t st);
+void launch_classify(bool fill, const float4* tb, const float4* bb, const Geo64* tg, const Geo64* bg, int nt, int nb,
+                     double k2, int* count, const int64_t* offset, int* out_tau, int* out_sigma, int8_t* out_cls,
+                     int* err, int num_sms, cudaStream_t st);
+void launch_scan(const int* counts, int n, int64_t* offsets, cudaStream_t st);
+void launch_classify_dense(const Geo64* tg, const Geo64* bg, int t0, int t1, int s0, int s1, double k2, int8_t* out,
+                           int* err, cudaStream_t st);
+void launch_singular(const OpParams& op, const QuadSel& qs, const RuleTable& rules, int rsA, int rsB, const Geo64* tg,
+                     const Geo64* bg, const int* et, const int* es, const int8_t* ec, int64_t n, double2* out,
+                     const volatile int* abort_flag, int num_sms, cudaStream_t st);
+void launch_local_diag64(const OpParams& op, const QuadSel& qs, const RuleTable& rules, int rsA, int rsB,
+                         const Geo64* tg, const Geo64* bg, const int* tau, const int* sigma, int64_t n, int force,
+                         double2* out, int8_t* cls, int* err, int num_sms, cudaStream_t st);
+
+// ---- bgb_far.cu ------------------------------------------------------------------------
+// Constants of the far-pair kernels (passed by value).
+struct FarConst {
+  int op_kind;
+  int qt, qb;                  // rule points (runtime, <= template maxima)
+  int lossy;                   // gamma has a real part
+  double alpha[2], beta[2], gamma[2];
+  float k_hi, k_lo, gre;       // gamma_im as double-float, gamma_re
+  float shpT[BGB_MAXQ][3], shpB[BGB_MAXQ][3];     // Lagrange hats at rule points
+  double shpT64[BGB_MAXQ][3], shpB64[BGB_MAXQ][3];
+};
+
+// Device-side plan of one tiled assembly (all arrays device pointers).
+struct TilePlan {
+  // records
+  const void* rec_t;           // test records (float or double, stride rec_stride_t)
+  const void* rec_b;
+  const float4* bnd_t;         // bounding spheres (classification radii)
+  const float4* bnd_b;
+  // test blocks
+  int n_tblocks;
+  const int* tb_off;           // [n_tblocks + 1] into tb_tris
+  const int* tb_tris;          // global test triangle ids, sorted ascending per block
+  const int* tb_fn_off;        // [n_tblocks + 1] into internal test function list
+  const int* fs_off;           // [n_tfun + 1] support entries of internal test function m
+  const int* fs_code;          // slot << 2 | local
+  const double* fs_coef;
+  const int64_t* rows;         // output row (relative to the window) of internal test function m
+  // trial blocks
+  int n_bblocks;
+  const int* bb_off;           // [n_bblocks + 1] into bb_tris
+  const int* bb_tris;          // global trial triangle ids, sorted ascending per block
+  const int* bb_fn_off;        // [n_bblocks + 1] into internal trial function list
+  const int* bb_chunk_off;     // [n_bblocks + 1] into chunk list
+  const int* ch_grp_off;       // [n_chunks + 1] into group list
+  const int* grp_fn;           // local trial function (within block)
+  const int* grp_sup_off;      // [n_groups + 1] into group support entries
+  const int* gs_code;          // slot (within block's triangle list) << 2 | local
+  const double* gs_coef;
+  const int64_t* cols;         // output column of internal trial function n
+  // singular / near overrides (CSR over global test triangles, sorted by trial triangle)
+  const int64_t* sing_off;
+  const int* sing_sigma;
+  const double2* sing_L;
+  // shapes
+  int FM, FN, SC, MAXS;        // block sizes, chunk, max supports per test function
+  int tmax, nmax;              // max triangles per test / trial block
+  // output
+  void* out;
+  int out_c64;                 // 1: complex double, 0: complex float
+  int64_t ld;
+  const volatile int* abort_flag;
+};
+
+size_t far_smem_bytes(int precision, int qt, int qb, const TilePlan& p);
+int launch_far_tiles(int precision, const FarConst& k, const TilePlan& p, cudaStream_t st);
+void launch_prepare_rec(int precision, int side, int q, const Geo64* g, int nt, const RuleTable& rules, int rule,
+                        double wscale, void* out, cudaStream_t st);
+int far_generic_q(int qt, int qb);  // 1 when the (qt, qb) pair uses the generic instance
+int rec_stride(int precision, int q, int generic);
+
+// Diagnostic: far-pair local matrices of explicit pairs with the tile kernels' pair code.
+int launch_far_pairs_diag(int precision, const FarConst& k, const void* rec_t, const void* rec_b, const int* tau,
+                          const int* sigma, int64_t n, double2* out, cudaStream_t st);
+
+// ---- bgb_peaks.cu ----------------------------------------------------------------------
+int measure_issue_peaks(int num_sms, double* fp32, double* fp64, double* mufu);
+
+}  // namespace bgb

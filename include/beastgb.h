@@ -1,0 +1,183 @@
+/*
+ * beastgb.h -- C ABI of libbeastgb, a GB300 (sm_103a) BEM Galerkin matrix-assembly engine.
+ *
+ * The library is the drop-in for the assembly path of BEASTGPU / BEAST:
+ *   assemble_gpu(op, X, Y, config, writeBackStrategy; quadstrat)  (assamble_gpu.jl:8,25)
+ *   BEAST.assemble(op, X, Y; quadstrat)                            (data/BEAST__multi.jl:15)
+ * A Julia `ccall` shim marshals BEAST's assembly data into the structs below (the same
+ * packing load_parameters.jl:25-54 does for the reference's kernels) and calls
+ * bgb_assemble.  All pointers are plain host pointers unless a field says "device".
+ *
+ * Errors: every entry point returns 0 on success or a negative bgb_status; the message of
+ * the last failure on the calling thread is bgb_last_error().  Nothing aborts the process
+ * and no kernel traps: device-side waits are bounded and report BGB_ERR_TIMEOUT.
+ *
+ * Threading: one handle per host thread (or per CUDA stream); calls on different handles
+ * may run concurrently.  A handle owns its device scratch and pinned staging buffers.
+ */
+#ifndef BEASTGB_H
+#define BEASTGB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BGB_ABI_VERSION 1
+
+typedef enum {
+  BGB_OK = 0,
+  BGB_ERR_INVALID = -1,       /* bad argument, inconsistent tables, degenerate geometry */
+  BGB_ERR_OOM = -2,           /* device or pinned host allocation failed */
+  BGB_ERR_CUDA = -3,          /* CUDA runtime error */
+  BGB_ERR_TIMEOUT = -4,       /* a bounded device wait gave up */
+  BGB_ERR_ABORTED = -5,       /* bgb_abort() was called while the call ran */
+  BGB_ERR_CAPACITY = -6,      /* a fixed capacity was exceeded */
+  BGB_ERR_NOT_SUPPORTED = -7  /* operator / space / rule combination not implemented */
+} bgb_status;
+
+/* Operators (BEAST: Helmholtz3D.singlelayer, Maxwell3D.singlelayer, Maxwell3D.doublelayer). */
+typedef enum {
+  BGB_OP_HELMHOLTZ3D_SL = 0, /* alpha int int G f g */
+  BGB_OP_MAXWELL3D_SL = 1,   /* int int G [alpha f.g + beta div f div g] */
+  BGB_OP_MAXWELL3D_DL = 2    /* alpha int int f(x) . (grad_x G(x,y) x g(y)) */
+} bgb_op_kind;
+
+/* Local shape-function families (BEAST reference spaces). */
+typedef enum {
+  BGB_REFSPACE_LAGRANGE_C0D1 = 0, /* barycentric hats (u, v, 1-u-v) */
+  BGB_REFSPACE_RT = 1             /* Raviart-Thomas / RWG: (x - v_i) / (2A), div 1/A */
+} bgb_refspace;
+
+typedef enum { BGB_PREC_FP64 = 0, BGB_PREC_MIXED = 1 } bgb_precision;
+
+typedef enum {
+  BGB_OUT_HOST_C64 = 0,   /* host complex double, (re, im) pairs */
+  BGB_OUT_HOST_C32 = 1,   /* host complex float */
+  BGB_OUT_DEVICE_C64 = 2, /* device complex double */
+  BGB_OUT_DEVICE_C32 = 3  /* device complex float */
+} bgb_out_kind;
+
+/* Pair classes (quadrule_determine.jl:76). */
+typedef enum { BGB_CLASS_FAR = 0, BGB_CLASS_CV = 1, BGB_CLASS_CE = 2, BGB_CLASS_CF = 3, BGB_CLASS_NEAR = 4 } bgb_pair_class;
+
+/* Operator: G(R) = exp(-gamma R) / (4 pi R), gamma = i k.  Complex numbers are (re, im). */
+typedef struct {
+  int32_t kind;    /* bgb_op_kind */
+  double alpha[2];
+  double beta[2];  /* Maxwell single layer only */
+  double gamma[2];
+} bgb_operator;
+
+/* Function space as per-triangle assembly tables (BEAST assemblydata, one function per
+ * local shape as in load_parameters.jl:50-54).  Triangles are in chart order (v1, v2, v3);
+ * local shape i belongs to vertex i (Lagrange) or to the edge opposite vertex i (RT). */
+typedef struct {
+  int32_t refspace;          /* bgb_refspace */
+  int32_t nv, nt, nfun;
+  const double* vertices;    /* [nv][3] */
+  const int32_t* triangles;  /* [nt][3], 0-based vertex indices */
+  const int32_t* fn_index;   /* [nt][3], global function of local shape i, -1 if none */
+  const double* fn_coef;     /* [nt][3] */
+} bgb_space;
+
+/* Quadrature strategy (BEAST DoubleNumWiltonSauterQStrat fields used by the path).
+ * Triangle rules: 1, 3, 4, 6, 7, 12 or 13 points (symmetric Dunavant rules).
+ * Sauter-Schwab: Gauss-Legendre points per dimension, 1..16. */
+typedef struct {
+  int32_t far_test, far_trial;   /* reference: 3 and 4 (GPU_scheduler.jl:94-95) */
+  int32_t near_test, near_trial;
+  int32_t ss_cf, ss_ce, ss_cv;   /* reference: 4 (SauterSchwab.jl:331,433) */
+} bgb_quadstrat;
+
+/* Handle configuration (GPUConfiguration, utils/configuration.jl:11-26, reduced to what a
+ * GB300 needs).  Zero-initialised fields take defaults. */
+typedef struct {
+  int32_t device;              /* CUDA device ordinal */
+  int64_t hbm_budget_bytes;    /* 0 = 90% of free device memory; bounds row blocks */
+  int64_t pinned_ring_bytes;   /* 0 = 2 x 512 MiB staging ring for host output */
+  int32_t tile_config;         /* -1 = first tile shape that fits shared memory, else a tile id (bgb_tile_info) */
+  int32_t flags;               /* reserved, 0 */
+} bgb_config;
+
+typedef struct {
+  int64_t pairs_total;          /* nt_test * nt_trial over the assembled rows */
+  int64_t pairs_class[5];       /* far, CV, CE, CF, near */
+  int64_t pairs_computed;       /* triangle pairs evaluated by the far kernel (incl. halo) */
+  double ms_classify, ms_singular, ms_far, ms_copy, ms_total;
+  int32_t row_blocks;
+  int32_t tile_config;
+} bgb_stats;
+
+typedef struct bgb_handle bgb_handle;
+
+/* Create / destroy a handle on cfg->device (cfg may be NULL).
+ * Replaces: the GPUConfiguration() constructor plus CUDA backend set-up
+ * (utils/configuration.jl:29-50, assamble_gpu.jl:25-65). */
+int bgb_create(bgb_handle** out, const bgb_config* cfg);
+int bgb_destroy(bgb_handle* h);
+
+/* Assemble rows [row0, row0 + nrows) of Z (test functions) against all trial functions.
+ * nrows < 0 means all rows.  Output is column-major (Julia layout): element (m, n) at
+ * out[(m - row0) + n * ld], ld >= nrows.  Device outputs are written on `stream`
+ * (a cudaStream_t, NULL = the handle's stream); host outputs are complete on return.
+ * Replaces: assemble_gpu(op, X, Y, config, GpuWriteBackTrueInstance(); quadstrat)
+ * (assamble_gpu.jl:25-137) and BEAST.assemble for the same operator (data/BEAST__multi.jl:15). */
+int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test,
+                 const bgb_space* trial, const bgb_quadstrat* qs, int32_t precision,
+                 void* out, int32_t out_kind, int64_t ld, int64_t row0, int64_t nrows,
+                 void* stream, bgb_stats* stats);
+
+/* One problem of a batch. */
+typedef struct {
+  bgb_operator op;
+  bgb_space test, trial;
+  bgb_quadstrat qs;
+  void* out;        /* device or host per out_kind of the batch call */
+  int64_t ld;
+} bgb_problem;
+
+/* Assemble n independent problems (uneven sizes and wavenumbers) with one persistent launch
+ * per kernel stage over a shared work queue.  No reference counterpart: the reference
+ * assembles one operator per call (assamble_gpu.jl:25). */
+int bgb_assemble_batch(bgb_handle* h, int32_t n, const bgb_problem* problems, int32_t precision,
+                       int32_t out_kind, void* stream, bgb_stats* stats);
+
+/* Pair classes of a block of triangle pairs on the device, out[(t - t0) * (s1 - s0) + (s - s0)]
+ * (host int8 buffer).  Replaces: determine_quadrule_types / quadrule_determine_type
+ * (quadrule_determine.jl:5-47,54-77). */
+int bgb_classify_block(bgb_handle* h, const bgb_space* test, const bgb_space* trial, double k2,
+                       int32_t t0, int32_t t1, int32_t s0, int32_t s1, int8_t* out);
+
+/* Local 3x3 complex matrices of a list of triangle pairs (out: double[npairs][9][2], host),
+ * with the rule chosen by classification or forced (force_class >= 0).  Singular and near
+ * pairs always use the FP64 kernels; far pairs use the far kernel's pair code of `precision`.
+ * Replaces the per-pair integrals of sauterschwab_parameterized_gpu_outside_loop_kernel!
+ * (SauterSchwab.jl:212-262) and doubleQuadRuleMainCaseKernel! (doubleQuadRuleMainCase.jl:60-105)
+ * before their scatter. */
+int bgb_local_matrices(bgb_handle* h, const bgb_operator* op, const bgb_space* test,
+                       const bgb_space* trial, const bgb_quadstrat* qs, int32_t precision, int64_t npairs,
+                       const int32_t* tau, const int32_t* sigma, int32_t force_class,
+                       double* out, int8_t* cls_out);
+
+/* Ask a running call on this handle to stop at its next check point (BGB_ERR_ABORTED). */
+int bgb_abort(bgb_handle* h);
+
+/* Tile shapes compiled into the far-pair kernel: fills up to `cap` ids, returns the count. */
+int bgb_tile_info(int32_t* ids, int32_t cap);
+
+/* FP32 / FP64 FMA issue peaks and MUFU throughput measured on the handle's device
+ * (TFLOP/s, TFLOP/s, Tops/s), for roofline denominators. */
+int bgb_measure_issue_peaks(bgb_handle* h, double* fp32_tflops, double* fp64_tflops, double* mufu_tops);
+
+/* Message of the last failure on the calling thread ("" if none). */
+const char* bgb_last_error(void);
+
+int bgb_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif
