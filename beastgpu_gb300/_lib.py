@@ -48,13 +48,14 @@ class Stats(C.Structure):
     _fields_ = [("pairs_total", C.c_int64), ("pairs_class", C.c_int64 * 5), ("pairs_computed", C.c_int64),
                 ("ms_classify", C.c_double), ("ms_singular", C.c_double), ("ms_far", C.c_double),
                 ("ms_copy", C.c_double), ("ms_total", C.c_double), ("row_blocks", C.c_int32),
-                ("tile_config", C.c_int32)]
+                ("tile_config", C.c_int32), ("kernel_launches", C.c_int32), ("reserved", C.c_int32)]
 
     def as_dict(self):
         return {"pairs_total": self.pairs_total, "pairs_class": list(self.pairs_class),
                 "pairs_computed": self.pairs_computed, "ms_classify": self.ms_classify,
                 "ms_singular": self.ms_singular, "ms_far": self.ms_far, "ms_copy": self.ms_copy,
-                "ms_total": self.ms_total, "row_blocks": self.row_blocks, "tile_config": self.tile_config}
+                "ms_total": self.ms_total, "row_blocks": self.row_blocks, "tile_config": self.tile_config,
+                "kernel_launches": self.kernel_launches}
 
 
 class Problem(C.Structure):

@@ -767,17 +767,21 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
 
   RuleTable R = make_rules();
   cudaEventRecord(h->ev[0], h->stream);
+  int launches = 0;
   if ((rc = upload_space(h, test, h->verts_t, h->tris_t, h->geo_t))) return rc;
+  launches += test->nt > 0;
   const bool same = same_space(test, trial);
   const Geo64* gt = h->geo_t.as<Geo64>();
   const Geo64* gb = gt;
   if (!same) {
     if ((rc = upload_space(h, trial, h->verts_b, h->tris_b, h->geo_b))) return rc;
     gb = h->geo_b.as<Geo64>();
+    launches += trial->nt > 0;
   }
   // 1. classification
   int64_t nsing = 0;
   if ((rc = classify_all(h, test, trial, gt, gb, opp.k2, &nsing))) return rc;
+  launches += 6;  // 2 bounds, 2 classify passes, scan (+1 singular below)
   cudaEventRecord(h->ev[1], h->stream);
   // 2. singular / near pairs (FP64)
   if ((rc = h->sing_L.ensure(sizeof(double2) * 9 * std::max<int64_t>(1, nsing)))) return rc;
@@ -795,6 +799,7 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
     return rc;
   launch_prepare_rec(precision, 0, gen ? BGB_MAXQ : K.qt, gt, test->nt, R, qsel.far_t, 1.0, h->rec_t.p, h->stream);
   launch_prepare_rec(precision, 1, gen ? BGB_MAXQ : K.qb, gb, trial->nt, R, qsel.far_b, BGB_INV_4PI_D, h->rec_b.p, h->stream);
+  launches += 2;
 
   // 4. host plan
   const bool pinned_cfg = h->cfg.tile_config >= 0;
@@ -919,6 +924,7 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
     T.ld = dld;
     cudaEventRecord(h->ev[3], h->stream);
     if ((rc = launch_far_tiles(precision, K, T, h->stream))) return rc;
+    ++launches;
     cudaEventRecord(h->ev[4], h->stream);
     if (host_out) {
       char* hdst = (char*)out + (size_t)(r0 - row0) * esz;
@@ -952,6 +958,7 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
     for (int c = 0; c < 5; ++c) st.pairs_class[c] = cnt[c];
   }
   st.ms_total = std::chrono::duration<double, std::milli>(clk::now() - t_start).count();
+  st.kernel_launches = launches;
   if (stats) *stats = st;
   return 0;
 }
@@ -974,6 +981,7 @@ int bgb_assemble_batch(bgb_handle* h, int32_t n, const bgb_problem* problems, in
     acc.ms_copy += s1.ms_copy;
     acc.ms_total += s1.ms_total;
     acc.row_blocks += s1.row_blocks;
+    acc.kernel_launches += s1.kernel_launches;
   }
   if (stats) *stats = acc;
   return 0;

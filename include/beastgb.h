@@ -108,6 +108,8 @@ typedef struct {
   double ms_classify, ms_singular, ms_far, ms_copy, ms_total;
   int32_t row_blocks;
   int32_t tile_config;
+  int32_t kernel_launches;      /* kernels this call launched */
+  int32_t reserved;
 } bgb_stats;
 
 typedef struct bgb_handle bgb_handle;
