@@ -85,7 +85,7 @@ struct bgb_handle {
   // buffers
   bgb::DevBuf verts_t, tris_t, verts_b, tris_b, geo_t, geo_b, bnd_t, bnd_b, rec_t, rec_b;
   bgb::DevBuf cls_count, cls_off, ent_tau, ent_sigma, ent_cls, sing_L, err;
-  bgb::DevBuf plan_i, plan_l, plan_d;
+  bgb::DevBuf plan_i, plan_l, plan_d, plan_f;
   bgb::DevBuf stage[2];
   bgb::DevBuf diag_a, diag_b, diag_c, diag_d;
   cudaEvent_t ev[8] = {};
@@ -243,6 +243,10 @@ static FarConst make_farconst(const OpParams& op, const RuleTable& R, const Quad
     k.beta[c] = op.beta[c];
     k.gamma[c] = op.gamma[c];
   }
+  for (int c = 0; c < 2; ++c) {
+    k.alpha32[c] = (float)op.alpha[c];
+    k.beta32[c] = (float)op.beta[c];
+  }
   k.k_hi = (float)op.gamma[1];
   k.k_lo = (float)(op.gamma[1] - (double)k.k_hi);
   k.gre = (float)op.gamma[0];
@@ -358,7 +362,7 @@ struct HostPlan {
   std::vector<int> bb_off, bb_tris, bb_fn_off, bb_chunk_off, ch_grp_off, grp_fn, grp_sup_off, gs_code;
   std::vector<double> gs_coef;
   std::vector<int64_t> cols;
-  int tmax = 0, nmax = 0, MAXS = 1;
+  int tmax = 0, nmax = 0, MAXS = 1, gmax = 1, gsmax = 1;
   int64_t pairs = 0;  // triangle pairs computed by the tiles (incl. halo)
 };
 
@@ -444,6 +448,10 @@ static void plan_trial_side(const Supports& S, const std::vector<int>& order, in
       P.ch_grp_off.push_back((int)P.grp_fn.size());
     }
     for (size_t i = b0; i < b1; ++i) P.cols.push_back(order[i]);
+    const int g_lo = P.ch_grp_off[P.ch_grp_off.size() - 1 - nchunks];
+    const int g_hi = P.ch_grp_off.back();
+    P.gmax = std::max(P.gmax, g_hi - g_lo);
+    P.gsmax = std::max(P.gsmax, P.grp_sup_off[g_hi] - P.grp_sup_off[g_lo]);
     P.bb_tris.insert(P.bb_tris.end(), tris.begin(), tris.end());
     P.bb_off.push_back((int)P.bb_tris.size());
     P.bb_fn_off.push_back((int)b1);
@@ -463,10 +471,14 @@ static const TileCfg kTileCfgs[] = {
     {32, 32, 8},    // 5
     {32, 32, 4},    // 6: FP64, Lagrange
     {16, 16, 4},    // 7
-    {48, 48, 8},    // 8
+    {48, 48, 8},    // 8: mixed, RWG
+    {48, 48, 4},    // 9
+    {40, 40, 8},    // 10
+    {48, 48, 16},   // 11
+    {56, 56, 8},    // 12
 };
 // Preference order when the caller does not pin a tile: the first whose shared memory fits.
-static const int kPrefMixed[] = {0, 1, 8, 5, 6, 7};
+static const int kPrefMixed[] = {8, 1, 5, 6, 7};
 static const int kPrefFp64[] = {4, 8, 5, 6, 7};
 static const int kNumTileCfgs = sizeof(kTileCfgs) / sizeof(kTileCfgs[0]);
 
@@ -607,7 +619,7 @@ int bgb_destroy(bgb_handle* h) {
   if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
   DevBuf* bufs[] = {&h->verts_t, &h->tris_t, &h->verts_b, &h->tris_b, &h->geo_t, &h->geo_b, &h->bnd_t, &h->bnd_b,
                     &h->rec_t, &h->rec_b, &h->cls_count, &h->cls_off, &h->ent_tau, &h->ent_sigma, &h->ent_cls,
-                    &h->sing_L, &h->err, &h->plan_i, &h->plan_l, &h->plan_d, &h->stage[0], &h->stage[1],
+                    &h->sing_L, &h->err, &h->plan_i, &h->plan_l, &h->plan_d, &h->plan_f, &h->stage[0], &h->stage[1],
                     &h->diag_a, &h->diag_b, &h->diag_c, &h->diag_d};
   for (DevBuf* b : bufs) b->release();
   for (int i = 0; i < 8; ++i)
@@ -844,6 +856,7 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
       plan_trial_side(Sb, ord_b, tc.FN, tc.SC, P);
       TilePlan probe{};
       probe.FM = tc.FM; probe.FN = tc.FN; probe.SC = tc.SC; probe.MAXS = P.MAXS;
+      probe.gmax = P.gmax; probe.gsmax = P.gsmax;
       probe.tmax = std::max(1, P.tmax); probe.nmax = std::max(1, P.nmax);
       smem = far_smem_bytes(precision, K.qt, K.qb, probe);
       if (smem <= (size_t)smem_max) { cfg_id = prefs[pi_]; break; }
@@ -869,12 +882,20 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
            o_grp_sup = put_i(P.grp_sup_off), o_gs_code = put_i(P.gs_code);
     size_t o_rows = put_l(P.rows), o_cols = put_l(P.cols);
     size_t o_fs_coef = put_d(P.fs_coef), o_gs_coef = put_d(P.gs_coef);
+    std::vector<float> F32;
+    F32.reserve(P.fs_coef.size() + P.gs_coef.size());
+    for (double v : P.fs_coef) F32.push_back((float)v);
+    const size_t o_gs32 = F32.size();
+    for (double v : P.gs_coef) F32.push_back((float)v);
     if ((rc = h->plan_i.ensure(sizeof(int) * std::max<size_t>(1, I.size()))) ||
         (rc = h->plan_l.ensure(sizeof(int64_t) * std::max<size_t>(1, Lg.size()))) ||
-        (rc = h->plan_d.ensure(sizeof(double) * std::max<size_t>(1, D.size()))))
+        (rc = h->plan_d.ensure(sizeof(double) * std::max<size_t>(1, D.size()))) ||
+        (rc = h->plan_f.ensure(sizeof(float) * std::max<size_t>(1, F32.size()))))
       return rc;
     BGB_CUDA(cudaStreamSynchronize(h->stream));  // previous block's plan arrays no longer in use
-    if ((rc = upload(h, h->plan_i, I, 0)) || (rc = upload(h, h->plan_l, Lg, 0)) || (rc = upload(h, h->plan_d, D, 0))) return rc;
+    if ((rc = upload(h, h->plan_i, I, 0)) || (rc = upload(h, h->plan_l, Lg, 0)) || (rc = upload(h, h->plan_d, D, 0)) ||
+        (rc = upload(h, h->plan_f, F32, 0)))
+      return rc;
     const int* pi = h->plan_i.as<int>();
     const int64_t* pl = h->plan_l.as<int64_t>();
     const double* pd = h->plan_d.as<double>();
@@ -901,6 +922,10 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
     T.grp_sup_off = pi + o_grp_sup;
     T.gs_code = pi + o_gs_code;
     T.gs_coef = pd + o_gs_coef;
+    T.fs_coef32 = h->plan_f.as<float>();
+    T.gs_coef32 = h->plan_f.as<float>() + o_gs32;
+    T.gmax = P.gmax;
+    T.gsmax = P.gsmax;
     T.cols = pl + o_cols;
     T.sing_off = h->cls_off.as<int64_t>();
     T.sing_sigma = h->ent_sigma.as<int>();

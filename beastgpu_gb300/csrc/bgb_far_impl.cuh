@@ -210,7 +210,7 @@ __device__ __forceinline__ void far_pair_mixed(const FarConst& K, const float* _
     }
   }
 
-  const float2 alpha = make_float2((float)K.alpha[0], (float)K.alpha[1]);
+  const float2 alpha = make_float2(K.alpha32[0], K.alpha32[1]);
   if (OP == BGB_OP_HELMHOLTZ3D_SL) {
 #pragma unroll
     for (int k = 0; k < 9; ++k) L[k] = cmulf(alpha, L[k]);
@@ -220,7 +220,7 @@ __device__ __forceinline__ void far_pair_mixed(const FarConst& K, const float* _
   const float2 ca = make_float2(alpha.x * inv4AA, alpha.y * inv4AA);
   if (OP == BGB_OP_MAXWELL3D_SL) {
     const float invAA = 4.f * inv4AA;
-    const float2 cb = make_float2((float)K.beta[0] * invAA, (float)K.beta[1] * invAA);
+    const float2 cb = make_float2(K.beta32[0] * invAA, K.beta32[1] * invAA);
     const float2 tb = cmulf(cb, P0);
     float2 av[3], bv[3];
 #pragma unroll
@@ -478,13 +478,18 @@ struct Smem {
   typename P::R* fcoef;
   typename P::C* Lbuf;
   typename P::C* Zs;
+  int* grpFn;      // per group of the trial block: local function
+  int* grpOff;     // per group: first support (block-relative), plus one end marker per chunk
+  int* chGrp;      // per chunk: first group (block-relative)
+  int* gsCode;
+  typename P::R* gsCoef;
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
 template <class P>
 __host__ __device__ inline size_t carve(unsigned char* base, int tmax, int nmax, int rt, int rb, int FM, int FN,
-                                        int MAXS, int SC, Smem<P>* s) {
+                                        int MAXS, int SC, int gmax, int gsmax, Smem<P>* s) {
   using R = typename P::R;
   using C = typename P::C;
   size_t off = 0;
@@ -505,6 +510,12 @@ __host__ __device__ inline size_t carve(unsigned char* base, int tmax, int nmax,
   p = take(sizeof(R) * (size_t)FM * MAXS); if (s) s->fcoef = (R*)p;
   p = take(sizeof(C) * 9 * (size_t)tmax * SC); if (s) s->Lbuf = (C*)p;
   p = take(sizeof(C) * (size_t)FM * FN); if (s) s->Zs = (C*)p;
+  const int nch = (nmax + SC - 1) / SC;
+  p = take(sizeof(int) * (size_t)gmax); if (s) s->grpFn = (int*)p;
+  p = take(sizeof(int) * (size_t)(gmax + 1)); if (s) s->grpOff = (int*)p;
+  p = take(sizeof(int) * (size_t)(nch + 1)); if (s) s->chGrp = (int*)p;
+  p = take(sizeof(int) * (size_t)gsmax); if (s) s->gsCode = (int*)p;
+  p = take(sizeof(R) * (size_t)gsmax); if (s) s->gsCoef = (R*)p;
   return off;
 }
 
@@ -520,7 +531,7 @@ __global__ void __launch_bounds__(kThreads) k_far_tiles(const __grid_constant__ 
   const int bm = blockIdx.x, bn = blockIdx.y;
   if (p.abort_flag && *p.abort_flag) return;
   Smem<P> s;
-  carve<P>(smem, p.tmax, p.nmax, RT, RB, p.FM, p.FN, p.MAXS, p.SC, &s);
+  carve<P>(smem, p.tmax, p.nmax, RT, RB, p.FM, p.FN, p.MAXS, p.SC, p.gmax, p.gsmax, &s);
 
   const int t0 = p.tb_off[bm], tm = p.tb_off[bm + 1] - t0;
   const int b0 = p.bb_off[bn], nbk = p.bb_off[bn + 1] - b0;
@@ -547,20 +558,34 @@ __global__ void __launch_bounds__(kThreads) k_far_tiles(const __grid_constant__ 
     const int r = i / RB, c = i - r * RB;
     s.recB[i] = gRB[(int64_t)p.bb_tris[b0 + r] * RB + c];
   }
+  const bool f32 = sizeof(R) == 4;
   for (int m = tid; m < fm; m += kThreads) {
     const int a0 = p.fs_off[f0 + m], a1 = p.fs_off[f0 + m + 1];
     const int cnt = min(a1 - a0, p.MAXS);
     s.fcnt[m] = cnt;
     for (int k = 0; k < cnt; ++k) {
       s.fcode[m * p.MAXS + k] = p.fs_code[a0 + k];
-      s.fcoef[m * p.MAXS + k] = (R)p.fs_coef[a0 + k];
+      s.fcoef[m * p.MAXS + k] = f32 ? (R)p.fs_coef32[a0 + k] : (R)p.fs_coef[a0 + k];
     }
+  }
+  // the trial block's gather groups (all chunks), block-relative
+  const int c0 = p.bb_chunk_off[bn], c1 = p.bb_chunk_off[bn + 1];
+  const int gb0 = p.ch_grp_off[c0], gb1 = p.ch_grp_off[c1];
+  const int sb0 = p.grp_sup_off[gb0], sb1 = p.grp_sup_off[gb1];
+  for (int i = tid; i < gb1 - gb0; i += kThreads) {
+    s.grpFn[i] = p.grp_fn[gb0 + i];
+    s.grpOff[i] = p.grp_sup_off[gb0 + i] - sb0;
+  }
+  if (tid == 0) s.grpOff[gb1 - gb0] = sb1 - sb0;
+  for (int i = tid; i <= c1 - c0; i += kThreads) s.chGrp[i] = p.ch_grp_off[c0 + i] - gb0;
+  for (int i = tid; i < sb1 - sb0; i += kThreads) {
+    s.gsCode[i] = p.gs_code[sb0 + i];
+    s.gsCoef[i] = f32 ? (R)p.gs_coef32[sb0 + i] : (R)p.gs_coef[sb0 + i];
   }
   for (int i = tid; i < fm * fn; i += kThreads) s.Zs[i] = P::mk(0.0, 0.0);
   __syncthreads();
 
   const int LS = p.tmax * p.SC;
-  const int c0 = p.bb_chunk_off[bn], c1 = p.bb_chunk_off[bn + 1];
   for (int c = c0; c < c1; ++c) {
     const int sbase = (c - c0) * p.SC;
     const int scn = min(p.SC, nbk - sbase);
@@ -587,18 +612,18 @@ __global__ void __launch_bounds__(kThreads) k_far_tiles(const __grid_constant__ 
       for (int k = 0; k < 9; ++k) s.Lbuf[k * LS + li] = L[k];
     }
     __syncthreads();
-    const int gg0 = p.ch_grp_off[c], ng = p.ch_grp_off[c + 1] - gg0;
+    const int gg0 = s.chGrp[c - c0], ng = s.chGrp[c - c0 + 1] - gg0;
     for (int it = tid; it < ng * fm; it += kThreads) {
       const int g = it / fm, m = it - g * fm;
       const int gi = gg0 + g;
-      const int n = p.grp_fn[gi];
+      const int n = s.grpFn[gi];
       C acc = s.Zs[n * fm + m];
-      const int sb0 = p.grp_sup_off[gi], sb1 = p.grp_sup_off[gi + 1];
+      const int q0 = s.grpOff[gi], q1 = s.grpOff[gi + 1];
       const int cnt = s.fcnt[m];
-      for (int bsup = sb0; bsup < sb1; ++bsup) {
-        const int code = p.gs_code[bsup];
+      for (int bsup = q0; bsup < q1; ++bsup) {
+        const int code = s.gsCode[bsup];
         const int sl = (code >> 2) - sbase, j = code & 3;
-        const R cb = (R)p.gs_coef[bsup];
+        const R cb = s.gsCoef[bsup];
         for (int a = 0; a < cnt; ++a) {
           const int fc = s.fcode[m * p.MAXS + a];
           const int ta = fc >> 2, i = fc & 3;
@@ -710,7 +735,7 @@ template <class P, int OP, int QT, int QB>
 int launch_tiles_t(const FarConst& K, const TilePlan& p, cudaStream_t st) {
   constexpr int RT = P::template rec<QT>();
   constexpr int RB = P::template rec<QB>();
-  const size_t bytes = carve<P>(nullptr, p.tmax, p.nmax, RT, RB, p.FM, p.FN, p.MAXS, p.SC, nullptr);
+  const size_t bytes = carve<P>(nullptr, p.tmax, p.nmax, RT, RB, p.FM, p.FN, p.MAXS, p.SC, p.gmax, p.gsmax, nullptr);
   auto kern = k_far_tiles<P, OP, QT, QB>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(far tiles)");
@@ -725,7 +750,7 @@ int launch_tiles_t(const FarConst& K, const TilePlan& p, cudaStream_t st) {
 template <class P, int OP, int QT, int QB>
 size_t smem_t(const TilePlan& p) {
   return carve<P>(nullptr, p.tmax, p.nmax, P::template rec<QT>(), P::template rec<QB>(), p.FM, p.FN, p.MAXS, p.SC,
-                  nullptr);
+                  p.gmax, p.gsmax, nullptr);
 }
 
 template <class P, int OP, int QT, int QB>

@@ -28,6 +28,7 @@ struct FarConst {
   int qt, qb;                  // rule points (runtime, <= template maxima)
   int lossy;                   // gamma has a real part
   double alpha[2], beta[2], gamma[2];
+  float alpha32[2], beta32[2];
   float k_hi, k_lo, gre;       // gamma_im as double-float, gamma_re
   float shpT[BGB_MAXQ][3], shpB[BGB_MAXQ][3];     // Lagrange hats at rule points
   double shpT64[BGB_MAXQ][3], shpB64[BGB_MAXQ][3];
@@ -60,6 +61,9 @@ struct TilePlan {
   const int* grp_sup_off;      // [n_groups + 1] into group support entries
   const int* gs_code;          // slot (within block's triangle list) << 2 | local
   const double* gs_coef;
+  const float* gs_coef32;      // float copy for the mixed kernel
+  const float* fs_coef32;
+  int gmax, gsmax;             // max groups / group supports per trial block
   const int64_t* cols;         // output column of internal trial function n
   // singular / near overrides (CSR over global test triangles, sorted by trial triangle)
   const int64_t* sing_off;

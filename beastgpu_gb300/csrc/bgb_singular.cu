@@ -6,9 +6,10 @@
 //                     test rejects far pairs, the exact FP64 predicate (BEAST quadrule,
 //                     doubleQuadRuleMainCase.jl:324-339) decides the rest; non-far pairs are
 //                     compacted in trial order (ballot/popc), so the list is deterministic.
-//  k_singular         one warp per non-far pair: Sauter-Schwab CF/CE/CV (SauterSchwab.jl:212-297)
-//                     or the near-pair double quadrature, FP64, warp-shuffle reduction, one
-//                     3x3 complex local matrix per pair (no atomics).
+//  k_singular<OP>     one warp per non-far pair: Sauter-Schwab CF/CE/CV (SauterSchwab.jl:212-297)
+//                     or the near-pair double quadrature, FP64.  Each point adds a few
+//                     operator moments (8-10 complex), reduced by warp shuffles; the 3x3
+//                     complex local matrix is formed once per pair (no atomics).
 //  k_classify_dense   diagnostic: exact class of every pair of a block.
 #include "bgb_kernels.cuh"
 
@@ -232,112 +233,290 @@ __device__ inline void make_chart(const int P[3], Chart& C) {
   }
 }
 
-__device__ inline void ss_point(const OpParams& op, const Geo64& A, const Geo64& B, int rsA, int rsB,
-                                const Chart& cA, const Chart& cB, double u1, double u2, double v1, double v2,
-                                double mul, double2 L[3][3]) {
-  double bx1 = cA.cv[2][0] + cA.ct[0][0] * u1 + cA.ct[1][0] * u2;
-  double bx2 = cA.cv[2][1] + cA.ct[0][1] * u1 + cA.ct[1][1] * u2;
-  double by1 = cB.cv[2][0] + cB.ct[0][0] * v1 + cB.ct[1][0] * v2;
-  double by2 = cB.cv[2][1] + cB.ct[0][1] * v1 + cB.ct[1][1] * v2;
-  Shp64 X, Y;
-  shapes64(A, rsA, bx1, bx2, X);
-  shapes64(B, rsB, by1, by2, Y);
-  double wgt = ((4.0 * A.area) * B.area) * mul;  // Jacobians 2A * 2A times the SS weight
-  accumulate64(op, X, Y, wgt, L);
-}
+// ----------------------------------------------------------------------------------------
+// Integrand moments.  Each evaluation point adds a handful of operator-specific moments
+// (instead of 9 shape-function products); the 3x3 local matrix is formed once per pair.
+//   Helmholtz SL: m[a][b] = sum G p_a q_b,  p = (1, bx1, bx2), q = (1, by1, by2) (chart
+//                 coordinates), f = (bx1, bx2, 1-bx1-bx2).
+//   Maxwell SL:   S = sum G X.Y, Px = sum G X, Py = sum G Y, P0 = sum G  (X, Y relative to the
+//                 centroids), f_i.g_j = (X - V_i).(Y - W_j) / (4 A_tau A_sigma).
+//   Maxwell DL:   A1 = sum H X.(d x Y), B = sum H d x Y, C = sum H X x d, E = sum H d with
+//                 grad_x G = H d, d = x - y.
+// ----------------------------------------------------------------------------------------
+template <int OP>
+struct NAcc { static constexpr int N = OP == BGB_OP_HELMHOLTZ3D_SL ? 9 : (OP == BGB_OP_MAXWELL3D_SL ? 8 : 10); };
 
-// All regions of one 4-D Gauss-Legendre point (SauterSchwab.jl:265-297).
-__device__ inline void ss_gl_point(const OpParams& op, int cls, const Geo64& A, const Geo64& B, int rsA, int rsB,
-                                   const Chart& cA, const Chart& cB, double h1, double h2, double h3, double xi,
-                                   double wt, double2 L[3][3]) {
-  double xi3 = xi * xi * xi;
-  if (cls == BGB_CLASS_CV) {
-    double xh1 = xi * h1, xh2 = xi * h2;
-    double mul = wt * xi3 * h2;
-    ss_point(op, A, B, rsA, rsB, cA, cB, 1 - xi, xh1, 1 - xh2, xh2 * h3, mul, L);
-    ss_point(op, A, B, rsA, rsB, cA, cB, 1 - xh2, xh2 * h3, 1 - xi, xh1, mul, L);
-  } else if (cls == BGB_CLASS_CE) {
-    double xh1 = xi * h1, h12 = h1 * h2, h23 = h2 * h3, h123 = h12 * h3;
-    double mul = wt * xi3 * (h1 * h1) * h2;
-    ss_point(op, A, B, rsA, rsB, cA, cB, 1 - xi, xh1, 1 - xi * (1 - h123), xh1 * h2 * (1 - h3), mul, L);
-    ss_point(op, A, B, rsA, rsB, cA, cB, 1 - xi * (1 - h12), xh1 * (1 - h2), 1 - xi, xh1 * h23, mul, L);
-    ss_point(op, A, B, rsA, rsB, cA, cB, 1 - xi * (1 - h123), xh1 * h2 * (1 - h3), 1 - xi, xh1, mul, L);
-    ss_point(op, A, B, rsA, rsB, cA, cB, 1 - xi * (1 - h123), xh1 * (1 - h23), 1 - xi, xh1 * h2, mul, L);
-    double mul5 = wt * xi3 * (h1 * h1);
-    ss_point(op, A, B, rsA, rsB, cA, cB, 1 - xi, xh1 * h3, 1 - xi * (1 - h12), xh1 * (1 - h2), mul5, L);
-  } else {
-    double mul = wt * xi3 * (h1 * h1) * h2;
-    double a = (xi - xi * h1) + xi * h1 * h2;
-    double b = 1 - (xi - xi * h1 * h2 * h3);
-    double c = xi - xi * h1;
-    double d = xi * h1 * ((1 - h2) + h2 * h3);
-    double e = 1 - (xi - xi * h1 * h2);
-    double f = xi * h1 * (1 - h2);
-    double g = xi * h1 * (1 - h2 * h3);
-    ss_point(op, A, B, rsA, rsB, cA, cB, 1 - xi, a, b, c, mul, L);
-    ss_point(op, A, B, rsA, rsB, cA, cB, b, c, 1 - xi, a, mul, L);
-    ss_point(op, A, B, rsA, rsB, cA, cB, 1 - xi, d, e, f, mul, L);
-    ss_point(op, A, B, rsA, rsB, cA, cB, e, f, 1 - xi, d, mul, L);
-    ss_point(op, A, B, rsA, rsB, cA, cB, b, g, 1 - xi, f, mul, L);
-    ss_point(op, A, B, rsA, rsB, cA, cB, 1 - xi, f, b, g, mul, L);
+struct PairGeo {
+  double xa[3][3];   // x = xa[0] + xa[1] u1 + xa[2] u2   (test point from SS chart params)
+  double xb[3][3];
+  double ba[3][2];   // (bx1, bx2) = ba[0] + ba[1] u1 + ba[2] u2
+  double bb[3][2];
+  double cA[3], cB[3];
+};
+
+__device__ inline void make_pair_geo(const Geo64& A, const Geo64& B, const Chart& cA, const Chart& cB, PairGeo& P) {
+  // chart (u1, u2) -> barycentric (b1, b2) -> cartesian, composed into one affine map per side
+  const Geo64* T[2] = {&A, &B};
+  const Chart* C[2] = {&cA, &cB};
+  for (int side = 0; side < 2; ++side) {
+    double(*ba)[2] = side ? P.bb : P.ba;
+    double(*xa)[3] = side ? P.xb : P.xa;
+    const Chart& ch = *C[side];
+    const Geo64& G = *T[side];
+    ba[0][0] = ch.cv[2][0]; ba[0][1] = ch.cv[2][1];
+    ba[1][0] = ch.ct[0][0]; ba[1][1] = ch.ct[0][1];
+    ba[2][0] = ch.ct[1][0]; ba[2][1] = ch.ct[1][1];
+    for (int c = 0; c < 3; ++c) {
+      xa[0][c] = G.v[2][c] + G.t[0][c] * ba[0][0] + G.t[1][c] * ba[0][1];
+      xa[1][c] = G.t[0][c] * ba[1][0] + G.t[1][c] * ba[1][1];
+      xa[2][c] = G.t[0][c] * ba[2][0] + G.t[1][c] * ba[2][1];
+    }
+  }
+  for (int c = 0; c < 3; ++c) {
+    P.cA[c] = (A.v[0][c] + A.v[1][c] + A.v[2][c]) / 3.0;
+    P.cB[c] = (B.v[0][c] + B.v[1][c] + B.v[2][c]) / 3.0;
   }
 }
 
-__device__ inline void warp_reduce_L(double2 L[3][3]) {
+// Add one point pair with weight w (quadrature weights and Jacobians included).
+template <int OP>
+__device__ __forceinline__ void add_point(const OpParams& op, const double x[3], const double y[3], double bx1,
+                                          double bx2, double by1, double by2, const double cA[3],
+                                          const double cB[3], double w, double2* acc) {
+  const double d0 = x[0] - y[0], d1 = x[1] - y[1], d2 = x[2] - y[2];
+  const double R2 = d0 * d0 + d1 * d1 + d2 * d2;
+  const double rinv = rsqrt(R2);
+  const double R = R2 * rinv;
+  double sn = 0.0, cs = 1.0;
+  if (op.gamma[1] != 0.0) sincos(op.gamma[1] * R, &sn, &cs);
+  double amp = w * BGB_INV_4PI_D * rinv;
+  if (op.gamma[0] != 0.0) amp *= exp(-op.gamma[0] * R);
+  const double gr = amp * cs, gi = -amp * sn;
+  if (OP == BGB_OP_HELMHOLTZ3D_SL) {
+    const double p[3] = {1.0, bx1, bx2}, q[3] = {1.0, by1, by2};
 #pragma unroll
-  for (int i = 0; i < 3; ++i)
+    for (int a = 0; a < 3; ++a)
 #pragma unroll
-    for (int j = 0; j < 3; ++j)
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        L[i][j].x += __shfl_xor_sync(0xffffffffu, L[i][j].x, off);
-        L[i][j].y += __shfl_xor_sync(0xffffffffu, L[i][j].y, off);
+      for (int b = 0; b < 3; ++b) {
+        const double pq = p[a] * q[b];
+        acc[a * 3 + b].x = fma(gr, pq, acc[a * 3 + b].x);
+        acc[a * 3 + b].y = fma(gi, pq, acc[a * 3 + b].y);
       }
+  } else if (OP == BGB_OP_MAXWELL3D_SL) {
+    const double X0 = x[0] - cA[0], X1 = x[1] - cA[1], X2 = x[2] - cA[2];
+    const double Y0 = y[0] - cB[0], Y1 = y[1] - cB[1], Y2 = y[2] - cB[2];
+    const double xy = X0 * Y0 + X1 * Y1 + X2 * Y2;
+    acc[0].x = fma(gr, xy, acc[0].x); acc[0].y = fma(gi, xy, acc[0].y);
+    acc[1].x = fma(gr, X0, acc[1].x); acc[1].y = fma(gi, X0, acc[1].y);
+    acc[2].x = fma(gr, X1, acc[2].x); acc[2].y = fma(gi, X1, acc[2].y);
+    acc[3].x = fma(gr, X2, acc[3].x); acc[3].y = fma(gi, X2, acc[3].y);
+    acc[4].x = fma(gr, Y0, acc[4].x); acc[4].y = fma(gi, Y0, acc[4].y);
+    acc[5].x = fma(gr, Y1, acc[5].x); acc[5].y = fma(gi, Y1, acc[5].y);
+    acc[6].x = fma(gr, Y2, acc[6].x); acc[6].y = fma(gi, Y2, acc[6].y);
+    acc[7].x += gr; acc[7].y += gi;
+  } else {
+    // H = -(gamma + 1/R) G / R
+    const double g2r = gr * rinv, g2i = gi * rinv;
+    const double re = op.gamma[0] + rinv;
+    const double Hx = -(re * g2r - op.gamma[1] * g2i), Hy = -(re * g2i + op.gamma[1] * g2r);
+    const double X0 = x[0] - cA[0], X1 = x[1] - cA[1], X2 = x[2] - cA[2];
+    const double Y0 = y[0] - cB[0], Y1 = y[1] - cB[1], Y2 = y[2] - cB[2];
+    const double e0 = d1 * Y2 - d2 * Y1, e1 = d2 * Y0 - d0 * Y2, e2 = d0 * Y1 - d1 * Y0;  // d x Y
+    const double f0 = X1 * d2 - X2 * d1, f1 = X2 * d0 - X0 * d2, f2 = X0 * d1 - X1 * d0;  // X x d
+    const double a1 = X0 * e0 + X1 * e1 + X2 * e2;
+    const double v[10] = {a1, e0, e1, e2, f0, f1, f2, d0, d1, d2};
+#pragma unroll
+    for (int k = 0; k < 10; ++k) {
+      acc[k].x = fma(Hx, v[k], acc[k].x);
+      acc[k].y = fma(Hy, v[k], acc[k].y);
+    }
+  }
+}
+
+// Local matrix L[i][j] from the moments.
+template <int OP>
+__device__ inline void finalize(const OpParams& op, const Geo64& A, const Geo64& B, const double cA[3],
+                                const double cB[3], const double2* acc, double2 L[3][3]) {
+  const double2 alpha = make_double2(op.alpha[0], op.alpha[1]);
+  if (OP == BGB_OP_HELMHOLTZ3D_SL) {
+    // f = T p with T = [[0,1,0],[0,0,1],[1,-1,-1]]
+    const double T[3][3] = {{0, 1, 0}, {0, 0, 1}, {1, -1, -1}};
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        double2 s = make_double2(0, 0);
+        for (int a = 0; a < 3; ++a)
+          for (int b = 0; b < 3; ++b) {
+            const double t = T[i][a] * T[j][b];
+            s.x += t * acc[a * 3 + b].x;
+            s.y += t * acc[a * 3 + b].y;
+          }
+        L[i][j] = cmul(alpha, s);
+      }
+    return;
+  }
+  const double inv4AA = 1.0 / (4.0 * A.area * B.area);
+  double V[3][3], W[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int c = 0; c < 3; ++c) {
+      V[i][c] = A.v[i][c] - cA[c];
+      W[i][c] = B.v[i][c] - cB[c];
+    }
+  const double2 ca = cscale(alpha, inv4AA);
+  if (OP == BGB_OP_MAXWELL3D_SL) {
+    const double2 S = acc[0], P0 = acc[7];
+    const double2 tb = cmul(cscale(make_double2(op.beta[0], op.beta[1]), 4.0 * inv4AA), P0);
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        double2 t = S;
+        for (int c = 0; c < 3; ++c) {
+          t.x -= V[i][c] * acc[4 + c].x + W[j][c] * acc[1 + c].x;
+          t.y -= V[i][c] * acc[4 + c].y + W[j][c] * acc[1 + c].y;
+        }
+        const double vw = V[i][0] * W[j][0] + V[i][1] * W[j][1] + V[i][2] * W[j][2];
+        t.x += vw * P0.x;
+        t.y += vw * P0.y;
+        L[i][j] = cadd(cmul(ca, t), tb);
+      }
+    return;
+  }
+  // MFIE: alpha/(4AA) (A1 - W_j.C - V_i.B + V_i.(E x W_j)); B = acc[1..3], C = acc[4..6], E = acc[7..9]
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double2 t = acc[0];
+      const double* w = W[j];
+      const double* v = V[i];
+      for (int c = 0; c < 3; ++c) {
+        t.x -= w[c] * acc[4 + c].x + v[c] * acc[1 + c].x;
+        t.y -= w[c] * acc[4 + c].y + v[c] * acc[1 + c].y;
+      }
+      const double2 x0 = make_double2(acc[8].x * w[2] - acc[9].x * w[1], acc[8].y * w[2] - acc[9].y * w[1]);
+      const double2 x1 = make_double2(acc[9].x * w[0] - acc[7].x * w[2], acc[9].y * w[0] - acc[7].y * w[2]);
+      const double2 x2 = make_double2(acc[7].x * w[1] - acc[8].x * w[0], acc[7].y * w[1] - acc[8].y * w[0]);
+      t.x += v[0] * x0.x + v[1] * x1.x + v[2] * x2.x;
+      t.y += v[0] * x0.y + v[1] * x1.y + v[2] * x2.y;
+      L[i][j] = cmul(ca, t);
+    }
+}
+
+// Region maps of the Sauter-Schwab rules (SauterSchwab.jl:265-297): test/trial chart
+// parameters (u1, u2), (v1, v2) and the weight of region r at the 4-D point (h1, h2, h3, xi).
+__device__ __forceinline__ void ss_region(int cls, int r, double h1, double h2, double h3, double xi, double wt,
+                                          double& u1, double& u2, double& v1, double& v2, double& mul) {
+  const double xi3 = xi * xi * xi;
+  if (cls == BGB_CLASS_CV) {
+    const double xh1 = xi * h1, xh2 = xi * h2;
+    mul = wt * xi3 * h2;
+    double a1 = 1 - xi, a2 = xh1, b1 = 1 - xh2, b2 = xh2 * h3;
+    if (r == 0) { u1 = a1; u2 = a2; v1 = b1; v2 = b2; }
+    else { u1 = b1; u2 = b2; v1 = a1; v2 = a2; }
+  } else if (cls == BGB_CLASS_CE) {
+    const double xh1 = xi * h1, h12 = h1 * h2, h23 = h2 * h3, h123 = h12 * h3;
+    mul = wt * xi3 * (h1 * h1) * h2;
+    switch (r) {
+      case 0: u1 = 1 - xi; u2 = xh1; v1 = 1 - xi * (1 - h123); v2 = xh1 * h2 * (1 - h3); break;
+      case 1: u1 = 1 - xi * (1 - h12); u2 = xh1 * (1 - h2); v1 = 1 - xi; v2 = xh1 * h23; break;
+      case 2: u1 = 1 - xi * (1 - h123); u2 = xh1 * h2 * (1 - h3); v1 = 1 - xi; v2 = xh1; break;
+      case 3: u1 = 1 - xi * (1 - h123); u2 = xh1 * (1 - h23); v1 = 1 - xi; v2 = xh1 * h2; break;
+      default:
+        mul = wt * xi3 * (h1 * h1);
+        u1 = 1 - xi; u2 = xh1 * h3; v1 = 1 - xi * (1 - h12); v2 = xh1 * (1 - h2);
+    }
+  } else {
+    mul = wt * xi3 * (h1 * h1) * h2;
+    const double a = (xi - xi * h1) + xi * h1 * h2, b = 1 - (xi - xi * h1 * h2 * h3), c = xi - xi * h1;
+    const double d = xi * h1 * ((1 - h2) + h2 * h3), e = 1 - (xi - xi * h1 * h2), f = xi * h1 * (1 - h2);
+    const double g = xi * h1 * (1 - h2 * h3);
+    switch (r) {
+      case 0: u1 = 1 - xi; u2 = a; v1 = b; v2 = c; break;
+      case 1: u1 = b; u2 = c; v1 = 1 - xi; v2 = a; break;
+      case 2: u1 = 1 - xi; u2 = d; v1 = e; v2 = f; break;
+      case 3: u1 = e; u2 = f; v1 = 1 - xi; v2 = d; break;
+      case 4: u1 = b; u2 = g; v1 = 1 - xi; v2 = f; break;
+      default: u1 = 1 - xi; u2 = f; v1 = b; v2 = g;
+    }
+  }
 }
 
 // Integral of one non-far pair by a warp; every lane returns the full (reduced) matrix.
+template <int OP>
 __device__ void pair_integral64(const OpParams& op, const QuadSel& qs, const RuleTable& rules, int cls,
-                                const Geo64& A, const Geo64& B, int rsA, int rsB, double2 L[3][3]) {
+                                const Geo64& A, const Geo64& B, double2 L[3][3]) {
+  constexpr int NA = NAcc<OP>::N;
   const int lane = threadIdx.x & 31;
+  double2 acc[NA];
 #pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j) L[i][j] = make_double2(0.0, 0.0);
+  for (int k = 0; k < NA; ++k) acc[k] = make_double2(0.0, 0.0);
+  double cA[3], cB[3];
+  for (int c = 0; c < 3; ++c) {
+    cA[c] = (A.v[0][c] + A.v[1][c] + A.v[2][c]) / 3.0;
+    cB[c] = (B.v[0][c] + B.v[1][c] + B.v[2][c]) / 3.0;
+  }
   if (cls == BGB_CLASS_NEAR || cls == BGB_CLASS_FAR) {
-    int rt = cls == BGB_CLASS_NEAR ? qs.near_t : qs.far_t;
-    int rb = cls == BGB_CLASS_NEAR ? qs.near_b : qs.far_b;
-    int qt = rules.npoints[rt], qb = rules.npoints[rb];
+    const int rt = cls == BGB_CLASS_NEAR ? qs.near_t : qs.far_t;
+    const int rb = cls == BGB_CLASS_NEAR ? qs.near_b : qs.far_b;
+    const int qt = rules.npoints[rt], qb = rules.npoints[rb];
     for (int idx = lane; idx < qt * qb; idx += 32) {
-      int I = idx / qb, J = idx % qb;
+      const int I = idx / qb, J = idx - I * qb;
       const double* p = rules.uvw[rules.offset[rt] + I];
       const double* q = rules.uvw[rules.offset[rb] + J];
-      Shp64 X, Y;
-      shapes64(A, rsA, p[0], p[1], X);
-      shapes64(B, rsB, q[0], q[1], Y);
-      double wx = (p[2] / 2.0) * (A.area * 2.0), wy = (q[2] / 2.0) * (B.area * 2.0);
-      accumulate64(op, X, Y, wx * wy, L);
+      double x[3], y[3];
+      for (int c = 0; c < 3; ++c) {
+        x[c] = __dadd_rn(__dadd_rn(A.v[2][c], __dmul_rn(A.t[0][c], p[0])), __dmul_rn(A.t[1][c], p[1]));
+        y[c] = __dadd_rn(__dadd_rn(B.v[2][c], __dmul_rn(B.t[0][c], q[0])), __dmul_rn(B.t[1][c], q[1]));
+      }
+      const double w = ((p[2] / 2.0) * (A.area * 2.0)) * ((q[2] / 2.0) * (B.area * 2.0));
+      add_point<OP>(op, x, y, p[0], p[1], q[0], q[1], cA, cB, w, acc);
     }
-  } else if (!(op.kind == BGB_OP_MAXWELL3D_DL && cls == BGB_CLASS_CF)) {  // DL on a flat face is 0
+  } else if (!(OP == BGB_OP_MAXWELL3D_DL && cls == BGB_CLASS_CF)) {  // DL on a flat face is 0
     int I[3], J[3];
     ss_permutation(cls, A, B, I, J);
-    Chart cA, cB;
-    make_chart(I, cA);
-    make_chart(J, cB);
+    Chart chA, chB;
+    make_chart(I, chA);
+    make_chart(J, chB);
+    PairGeo P;
+    make_pair_geo(A, B, chA, chB, P);
+    const double jac = (4.0 * A.area) * B.area;  // Jacobians 2A * 2A
     const int n = qs.ss[cls];
     const int n2 = n * n, n3 = n2 * n, n4 = n3 * n;
+    const int nreg = cls == BGB_CLASS_CV ? 2 : (cls == BGB_CLASS_CE ? 5 : 6);
     const double* gx = qs.gl_x[cls];
     const double* gw = qs.gl_w[cls];
     for (int idx = lane; idx < n4; idx += 32) {
-      int i = idx / n3, j = (idx / n2) % n, k = (idx / n) % n, l = idx % n;
-      double wt = gw[i] * gw[j] * gw[k] * gw[l];
-      ss_gl_point(op, cls, A, B, rsA, rsB, cA, cB, gx[i], gx[j], gx[k], gx[l], wt, L);
+      const int i = idx / n3, j = (idx / n2) % n, k = (idx / n) % n, l = idx % n;
+      const double wt = gw[i] * gw[j] * gw[k] * gw[l];
+#pragma unroll 1
+      for (int r = 0; r < nreg; ++r) {
+        double u1, u2, v1, v2, mul;
+        ss_region(cls, r, gx[i], gx[j], gx[k], gx[l], wt, u1, u2, v1, v2, mul);
+        double x[3], y[3];
+        for (int c = 0; c < 3; ++c) {
+          x[c] = P.xa[0][c] + P.xa[1][c] * u1 + P.xa[2][c] * u2;
+          y[c] = P.xb[0][c] + P.xb[1][c] * v1 + P.xb[2][c] * v2;
+        }
+        double bx1 = 0, bx2 = 0, by1 = 0, by2 = 0;
+        if (OP == BGB_OP_HELMHOLTZ3D_SL) {
+          bx1 = P.ba[0][0] + P.ba[1][0] * u1 + P.ba[2][0] * u2;
+          bx2 = P.ba[0][1] + P.ba[1][1] * u1 + P.ba[2][1] * u2;
+          by1 = P.bb[0][0] + P.bb[1][0] * v1 + P.bb[2][0] * v2;
+          by2 = P.bb[0][1] + P.bb[1][1] * v1 + P.bb[2][1] * v2;
+        }
+        add_point<OP>(op, x, y, bx1, bx2, by1, by2, cA, cB, jac * mul, acc);
+      }
     }
   }
-  warp_reduce_L(L);
+#pragma unroll
+  for (int k = 0; k < NA; ++k)
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      acc[k].x += __shfl_xor_sync(0xffffffffu, acc[k].x, off);
+      acc[k].y += __shfl_xor_sync(0xffffffffu, acc[k].y, off);
+    }
+  finalize<OP>(op, A, B, cA, cB, acc, L);
 }
 
+template <int OP>
 __global__ void __launch_bounds__(256) k_singular(OpParams op, const __grid_constant__ QuadSel qs,
-                                                  const __grid_constant__ RuleTable rules, int rsA, int rsB,
+                                                  const __grid_constant__ RuleTable rules,
                                                   const Geo64* __restrict__ tg, const Geo64* __restrict__ bg,
                                                   const int* __restrict__ ent_tau, const int* __restrict__ ent_sigma,
                                                   const int8_t* __restrict__ ent_cls, int64_t n,
@@ -346,9 +525,9 @@ __global__ void __launch_bounds__(256) k_singular(OpParams op, const __grid_cons
   const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < n; e += warps) {
     if (abort_flag && *abort_flag) return;
-    Geo64 A = tg[ent_tau[e]], B = bg[ent_sigma[e]];
+    const Geo64 A = tg[ent_tau[e]], B = bg[ent_sigma[e]];
     double2 L[3][3];
-    pair_integral64(op, qs, rules, ent_cls[e], A, B, rsA, rsB, L);
+    pair_integral64<OP>(op, qs, rules, ent_cls[e], A, B, L);
     if (lane < 9) {
       double2 v = L[0][0];
 #pragma unroll
@@ -360,8 +539,9 @@ __global__ void __launch_bounds__(256) k_singular(OpParams op, const __grid_cons
 }
 
 // Diagnostic: local matrices of a list of pairs (classified exactly or forced), FP64.
+template <int OP>
 __global__ void __launch_bounds__(256) k_local_diag64(OpParams op, const __grid_constant__ QuadSel qs,
-                                                      const __grid_constant__ RuleTable rules, int rsA, int rsB,
+                                                      const __grid_constant__ RuleTable rules,
                                                       const Geo64* __restrict__ tg, const Geo64* __restrict__ bg,
                                                       const int* __restrict__ tau, const int* __restrict__ sigma,
                                                       int64_t n, int force, double2* __restrict__ out,
@@ -369,14 +549,14 @@ __global__ void __launch_bounds__(256) k_local_diag64(OpParams op, const __grid_
   const int lane = threadIdx.x & 31;
   const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < n; e += warps) {
-    Geo64 A = tg[tau[e]], B = bg[sigma[e]];
+    const Geo64 A = tg[tau[e]], B = bg[sigma[e]];
     int cls = force >= 0 ? force : classify_exact(A, B, op.k2);
     if (cls < 0) {
       if (lane == 0) atomicOr(err, 1);
       cls = BGB_CLASS_FAR;
     }
     double2 L[3][3];
-    pair_integral64(op, qs, rules, cls, A, B, rsA, rsB, L);
+    pair_integral64<OP>(op, qs, rules, cls, A, B, L);
     if (lane < 9) {
       double2 v = L[0][0];
 #pragma unroll
@@ -422,18 +602,32 @@ void launch_classify_dense(const Geo64* tg, const Geo64* bg, int t0, int t1, int
 void launch_singular(const OpParams& op, const QuadSel& qs, const RuleTable& rules, int rsA, int rsB, const Geo64* tg,
                      const Geo64* bg, const int* et, const int* es, const int8_t* ec, int64_t n, double2* out,
                      const volatile int* abort_flag, int num_sms, cudaStream_t st) {
+  (void)rsA;
+  (void)rsB;
   if (n <= 0) return;
   int64_t blocks = (n + 7) / 8;
   if (blocks > (int64_t)num_sms * 32) blocks = (int64_t)num_sms * 32;
-  k_singular<<<(int)blocks, 256, 0, st>>>(op, qs, rules, rsA, rsB, tg, bg, et, es, ec, n, out, abort_flag);
+  if (op.kind == BGB_OP_HELMHOLTZ3D_SL)
+    k_singular<BGB_OP_HELMHOLTZ3D_SL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, et, es, ec, n, out, abort_flag);
+  else if (op.kind == BGB_OP_MAXWELL3D_SL)
+    k_singular<BGB_OP_MAXWELL3D_SL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, et, es, ec, n, out, abort_flag);
+  else
+    k_singular<BGB_OP_MAXWELL3D_DL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, et, es, ec, n, out, abort_flag);
 }
 void launch_local_diag64(const OpParams& op, const QuadSel& qs, const RuleTable& rules, int rsA, int rsB,
                          const Geo64* tg, const Geo64* bg, const int* tau, const int* sigma, int64_t n, int force,
                          double2* out, int8_t* cls, int* err, int num_sms, cudaStream_t st) {
+  (void)rsA;
+  (void)rsB;
   if (n <= 0) return;
   int64_t blocks = (n + 7) / 8;
   if (blocks > (int64_t)num_sms * 32) blocks = (int64_t)num_sms * 32;
-  k_local_diag64<<<(int)blocks, 256, 0, st>>>(op, qs, rules, rsA, rsB, tg, bg, tau, sigma, n, force, out, cls, err);
+  if (op.kind == BGB_OP_HELMHOLTZ3D_SL)
+    k_local_diag64<BGB_OP_HELMHOLTZ3D_SL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, tau, sigma, n, force, out, cls, err);
+  else if (op.kind == BGB_OP_MAXWELL3D_SL)
+    k_local_diag64<BGB_OP_MAXWELL3D_SL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, tau, sigma, n, force, out, cls, err);
+  else
+    k_local_diag64<BGB_OP_MAXWELL3D_DL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, tau, sigma, n, force, out, cls, err);
 }
 
 }  // namespace bgb

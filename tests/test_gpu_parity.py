@@ -1,0 +1,185 @@
+"""Parity of the CUDA path (through the C ABI) with the FP64 CPU oracle.
+
+Tolerances: classification bit-exact; plain FP64 kernels 1e-12 relative (Frobenius) on full
+matrices and singular-pair local matrices; mixed FP32 far pairs 1e-5 relative Frobenius (the
+target of the mixed assembler); results bit-identical across tile shapes, runs and output kinds.
+"""
+import numpy as np
+import pytest
+
+import beastgpu_gb300 as bg
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+K1 = 2 * np.pi
+FP64_TOL = 1e-12
+MIXED_TOL = 1e-5
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+@pytest.fixture(scope="module")
+def c1():
+    m = bg.icosphere(2)
+    return m, bg.raviartthomas(m), bg.lagrangec0d1(m)
+
+
+@pytest.fixture(scope="module")
+def plates():
+    # two coplanar jittered plates: near pairs from the jitter (Lagrange and RWG)
+    m = bg.two_plates(12, jitter=0.3, seed=1, gap=0.01)
+    return m, bg.raviartthomas(m), bg.lagrangec0d1(m)
+
+
+OPS = {
+    "efie": (lambda k: bg.Maxwell3D.singlelayer(wavenumber=k), 1),
+    "mfie": (lambda k: bg.Maxwell3D.doublelayer(wavenumber=k), 1),
+    "hh": (lambda k: bg.Helmholtz3D.singlelayer(wavenumber=k), 2),
+}
+
+
+def _space(sp, which):
+    return sp[which]
+
+
+@pytest.mark.parametrize("k", [K1, 30.0, 0.0])
+def test_classification_bit_exact_icosphere(c1, k):
+    m, X, _ = c1
+    np.testing.assert_array_equal(bg.classify(X, X, k * k), oracle.classify_block(X, X, k * k))
+
+
+def test_classification_bit_exact_plates_with_near_pairs(plates):
+    m, X, _ = plates
+    k = 4 * np.pi
+    got = bg.classify(X, X, k * k)
+    np.testing.assert_array_equal(got, oracle.classify_block(X, X, k * k))
+    assert (got == 4).sum() > 0, "the jittered plates should produce near pairs"
+
+
+@pytest.mark.parametrize("name", list(OPS))
+@pytest.mark.parametrize("cls", [0, 1, 2, 3])
+def test_local_matrices_per_class(c1, qs, name, cls):
+    m, X, L = c1
+    make, which = OPS[name]
+    op = make(K1)
+    sp = c1[which]
+    c = oracle.classify_block(sp, sp, K1 * K1)
+    t, s = np.nonzero(c == cls)
+    sel = np.random.default_rng(cls).choice(t.size, min(150, t.size), replace=False)
+    t, s = t[sel], s[sel]
+    ref, rc = oracle.local_matrices(op, sp, sp, qs, t, s)
+    got, gc = bg.local_matrices(op, sp, sp, t, s)
+    np.testing.assert_array_equal(gc, rc)
+    if name == "mfie" and cls == 3:
+        assert np.all(got == 0) and np.all(ref == 0)  # double layer vanishes on a flat common face
+        return
+    assert rel(got, ref) < FP64_TOL
+    # singular entries stay FP64 in the mixed mode; far pairs meet the mixed tolerance
+    gm, _ = bg.local_matrices(op, sp, sp, t, s, precision="mixed")
+    if cls == 0:
+        assert rel(gm, ref) < MIXED_TOL
+    else:
+        assert rel(gm, ref) < FP64_TOL
+
+
+@pytest.mark.parametrize("name", list(OPS))
+def test_full_assembly_icosphere(c1, qs, name):
+    m, X, L = c1
+    make, which = OPS[name]
+    op = make(K1)
+    sp = c1[which]
+    ref = oracle.assemble(op, sp, sp, qs)
+    z64 = bg.assemble_gpu(op, sp, sp, bg.GPUConfiguration(precision="fp64"))
+    assert z64.dtype == np.complex128 and z64.shape == ref.shape
+    assert rel(z64, ref) < FP64_TOL
+    zmx = bg.assemble_gpu(op, sp, sp, bg.GPUConfiguration(precision="mixed"))
+    assert zmx.dtype == np.complex64
+    assert rel(zmx.astype(np.complex128), ref) < MIXED_TOL
+
+
+@pytest.mark.parametrize("name", ["hh", "mfie", "efie"])
+def test_full_assembly_plates_near_pairs(plates, qs, name):
+    m, X, L = plates
+    make, which = OPS[name]
+    op = make(4 * np.pi)
+    sp = plates[which]
+    ref = oracle.assemble(op, sp, sp, qs)
+    z64 = bg.assemble_gpu(op, sp, sp, bg.GPUConfiguration(precision="fp64"))
+    zmx = bg.assemble_gpu(op, sp, sp, bg.GPUConfiguration(precision="mixed"))
+    if name == "mfie":
+        # the double layer vanishes on a plane: f(x) . (grad G x g(y)) = 0 for coplanar x, y, f, g
+        assert np.all(ref == 0) and np.abs(z64).max() == 0 and np.abs(zmx).max() < 1e-12
+        return
+    assert rel(z64, ref) < FP64_TOL
+    assert rel(zmx.astype(np.complex128), ref) < MIXED_TOL
+
+
+def test_bit_identical_across_tiles_runs_and_outputs(c1):
+    import torch
+    m, X, L = c1
+    op = bg.Maxwell3D.singlelayer(wavenumber=K1)
+    for prec, cfgs in (("fp64", (4, 5, 6, 8)), ("mixed", (0, 1, 2, 3, 5, 8))):
+        outs = [bg.assemble_gpu(op, X, X, bg.GPUConfiguration(precision=prec, tile_config=c)) for c in cfgs]
+        outs.append(bg.assemble_gpu(op, X, X, bg.GPUConfiguration(precision=prec)))
+        for o in outs[1:]:
+            np.testing.assert_array_equal(o, outs[0])
+        dev = bg.assemble_gpu(op, X, X, bg.GPUConfiguration(precision=prec), out="device")
+        np.testing.assert_array_equal(dev.cpu().numpy(), outs[0])
+        assert isinstance(dev, torch.Tensor)
+
+
+def test_row_windows_and_writeback_strategies(c1):
+    m, X, L = c1
+    op = bg.Maxwell3D.singlelayer(wavenumber=K1)
+    full = bg.assemble_gpu(op, X, X, bg.GPUConfiguration(precision="fp64"))
+    part = bg.assemble_gpu(op, X, X, bg.GPUConfiguration(precision="fp64"), rows=(100, 77))
+    np.testing.assert_array_equal(part, full[100:177])
+    cpuwb = bg.assemble_gpu(op, X, X, bg.GPUConfiguration(precision="fp64"), bg.GpuWriteBackFalseInstance())
+    np.testing.assert_array_equal(cpuwb, full)
+    # out-of-core: a tiny HBM budget forces many row blocks; result unchanged
+    small = bg.assemble_gpu(op, X, X, bg.GPUConfiguration(precision="fp64", total_GPU_budget=2 * 60 * 480 * 16),
+                            return_stats=True)
+    np.testing.assert_array_equal(small[0], full)
+    assert small[1]["row_blocks"] > 1
+
+
+def test_c2_sampled_rows(qs):
+    """Level-5 icosphere EFIE (30,720 RWG), k = 8 pi: 24 seeded rows against the oracle."""
+    m = bg.icosphere(5)
+    X = bg.raviartthomas(m)
+    op = bg.Maxwell3D.singlelayer(wavenumber=2 * np.pi * 4)
+    rows = np.sort(np.random.default_rng(7).choice(X.nfun, 24, replace=False)).astype(np.int32)
+    ref = oracle.assemble_rows(op, X, X, qs, rows)
+    for prec, tol in (("mixed", MIXED_TOL), ("fp64", FP64_TOL)):
+        Z = bg.assemble_gpu(op, X, X, bg.GPUConfiguration(precision=prec), out="device")
+        import torch
+        got = Z[torch.as_tensor(rows.astype(np.int64), device=Z.device)].cpu().numpy().astype(np.complex128)
+        assert rel(got, ref) < tol, prec
+        del Z
+
+
+def test_invalid_inputs_fail_cleanly_and_handle_survives(c1):
+    m, X, L = c1
+    op = bg.Maxwell3D.singlelayer(wavenumber=K1)
+    bad = bg.Space(bg.Mesh(m.vertices, m.triangles), X.refspace, X.fn_index.copy(), X.fn_coef, X.nfun)
+    bad.fn_index[5, 1] = X.nfun + 3
+    with pytest.raises(bg._lib.BGBError) as e:
+        bg.assemble_gpu(op, bad, bad)
+    assert e.value.code == -1
+    v = m.vertices.copy()
+    v[3, 1] = np.nan
+    nanmesh = bg.Space(bg.Mesh(v, m.triangles), X.refspace, X.fn_index, X.fn_coef, X.nfun)
+    with pytest.raises(bg._lib.BGBError):
+        bg.assemble_gpu(op, nanmesh, nanmesh)
+    with pytest.raises(bg._lib.BGBError) as e:
+        bg.assemble_gpu(op, X, X, quadstrat=bg.QuadStrat(far_test=5))
+    assert e.value.code == -7
+    with pytest.raises(bg._lib.BGBError) as e:
+        bg.assemble_gpu(bg.Helmholtz3D.singlelayer(wavenumber=1.0), X, X)  # Helmholtz needs Lagrange
+    assert e.value.code == -7
+    # the handle still works
+    z = bg.assemble_gpu(op, X, X, bg.GPUConfiguration(precision="mixed"))
+    assert np.isfinite(z).all()
