@@ -163,6 +163,29 @@ int bgb_local_matrices(bgb_handle* h, const bgb_operator* op, const bgb_space* t
                        const int32_t* tau, const int32_t* sigma, int32_t force_class,
                        double* out, int8_t* cls_out);
 
+/* Pair classification into a CSR for callers that cannot allocate device memory (for
+ * example a Julia or PyTorch process whose memory pool already holds the device, or an
+ * embedding that forbids allocations outside its own allocator).  No reference counterpart:
+ * it is an addition of this library.
+ * Inputs are device arrays (vertices double[nv][3], triangles int32[nt][3]); outputs are
+ * device arrays: d_offsets int64[nt_test + 1] (CSR over test triangles) and, per non-far
+ * pair, d_tau / d_sigma int32 and d_class int8 (1 CV, 2 CE, 3 CF, 4 near), sorted by trial
+ * triangle within each test triangle -- the same classes as bgb_classify_block.  *total
+ * (host) receives the number of non-far pairs; if it exceeds `capacity` the call returns
+ * BGB_ERR_CAPACITY after filling d_offsets and *total, so the caller can retry.
+ * It calls no cudaMalloc / cudaFree: its scratch is a fixed 16 MiB device array of the
+ * library (enough for about 170,000 test + trial triangles; larger inputs are rejected
+ * with BGB_ERR_CAPACITY before any work).  Every device holds that array until the
+ * process exits.  The first call on a device looks up the array's address (make that first
+ * call before any stream capture).  All calls on a device share the array: calls whose GPU
+ * work overlaps race and must be serialised by the caller.  Work is queued on `stream`
+ * (a cudaStream_t, NULL = default stream); the call waits for the pair count only. */
+int bgb_classify_csr_noalloc(const double* d_vertices_test, const int32_t* d_triangles_test,
+                             int32_t nv_test, int32_t nt_test, const double* d_vertices_trial,
+                             const int32_t* d_triangles_trial, int32_t nv_trial, int32_t nt_trial,
+                             double k2, int64_t* d_offsets, int32_t* d_tau, int32_t* d_sigma,
+                             int8_t* d_class, int64_t capacity, int64_t* total, void* stream);
+
 /* Ask a running call on this handle to stop at its next check point (BGB_ERR_ABORTED). */
 int bgb_abort(bgb_handle* h);
 
