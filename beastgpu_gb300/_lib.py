@@ -83,6 +83,10 @@ SIGNATURES = {
                       C.POINTER(Stats)], C.c_int),
     "bgb_assemble_batch": ([C.c_void_p, C.c_int32, C.POINTER(Problem), C.c_int32, C.c_int32, C.c_void_p,
                             C.POINTER(Stats)], C.c_int),
+    "bgb_batch_create": ([C.c_void_p, C.c_int32, C.POINTER(Problem), C.c_int32, C.c_int32, C.c_int32,
+                          C.POINTER(C.c_void_p), C.POINTER(Stats)], C.c_int),
+    "bgb_batch_run": ([C.c_void_p, C.c_void_p, C.POINTER(Stats)], C.c_int),
+    "bgb_batch_destroy": ([C.c_void_p], C.c_int),
     "bgb_classify_csr_noalloc": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
                                   C.c_int32, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
                                   C.POINTER(C.c_int64), C.c_void_p], C.c_int),

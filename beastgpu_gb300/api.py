@@ -238,3 +238,86 @@ def measure_issue_peaks(device: int = 0):
     a, b, c = C.c_double(), C.c_double(), C.c_double()
     _lib.check(_lib.load().bgb_measure_issue_peaks(h.ptr, C.byref(a), C.byref(b), C.byref(c)))
     return a.value, b.value, c.value
+
+
+class Batch:
+    """Plan / execute form of a batch of independent problems (bgb_batch_create / _run).
+
+    problems: list of (operator, test space, trial space).  All share the operator kind, the
+    space kind and the quadrature strategy.  On construction every problem is assembled once
+    (one classification launch, one singular-pair launch and ONE persistent far-pair launch
+    over a work queue of tiles of all problems), the tile shape and work-queue schedule are
+    autotuned (autotune=True), and the device sequence is captured in a CUDA graph that
+    run() replays.  `outputs` are the matrices (torch CUDA tensors for out="device", numpy
+    column-major arrays for out="host").
+    """
+
+    def __init__(self, problems, config: GPUConfiguration = None, *, quadstrat: QuadStrat = None, out="device",
+                 dtype=None, autotune=True):
+        config = config or GPUConfiguration()
+        self.config = config
+        prec = _precision(config.precision)
+        if dtype is None:
+            dtype = np.complex128 if prec == _lib.PREC_FP64 else np.complex64
+        dtype = np.dtype(dtype)
+        c64 = dtype == np.complex128
+        self.h = get_handle(config.device, config.total_GPU_budget, config.tile_config)
+        self._keep = _Keep()
+        arr = (_lib.Problem * len(problems))()
+        self.outputs = []
+        self._bufs = []
+        for i, (op, X, Y) in enumerate(problems):
+            qs = quadstrat or defaultquadstrat(op, X, Y)
+            arr[i].op = c_operator(op)
+            arr[i].test = c_space(X, self._keep)
+            arr[i].trial = c_space(Y, self._keep)
+            arr[i].qs = c_quadstrat(qs)
+            arr[i].ld = max(1, X.nfun)
+            if out == "device":
+                import torch
+                t = torch.empty((Y.nfun, max(1, X.nfun)), dtype=torch.complex128 if c64 else torch.complex64,
+                                device=f"cuda:{config.device}")
+                self._bufs.append(t)
+                arr[i].out = t.data_ptr()
+                self.outputs.append(t.T)
+            elif out == "host":
+                Z = np.empty((X.nfun, Y.nfun), dtype=dtype, order="F")
+                self._bufs.append(Z)
+                arr[i].out = Z.ctypes.data
+                self.outputs.append(Z)
+            else:
+                raise ValueError("out must be 'host' or 'device'")
+        self._arr = arr
+        kind = (_lib.OUT_DEVICE_C64 if c64 else _lib.OUT_DEVICE_C32) if out == "device" else \
+            (_lib.OUT_HOST_C64 if c64 else _lib.OUT_HOST_C32)
+        self.ptr = C.c_void_p()
+        st = _lib.Stats()
+        _lib.check(_lib.load().bgb_batch_create(self.h.ptr, len(problems), arr, prec, kind, 1 if autotune else 0,
+                                                C.byref(self.ptr), C.byref(st)))
+        self.create_stats = st.as_dict()
+
+    def run(self, stream=None):
+        """Replay the captured graph (re-assembles every problem); returns the stats."""
+        st = _lib.Stats()
+        _lib.check(_lib.load().bgb_batch_run(self.ptr, C.c_void_p(stream) if stream else None, C.byref(st)))
+        return st.as_dict()
+
+    def close(self):
+        if self.ptr:
+            _lib.load().bgb_batch_destroy(self.ptr)
+            self.ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def assemble_batch(problems, config: GPUConfiguration = None, *, quadstrat: QuadStrat = None, out="device", dtype=None,
+                   autotune=False):
+    """Assemble independent problems [(op, X, Y), ...] with one persistent far-pair launch."""
+    b = Batch(problems, config, quadstrat=quadstrat, out=out, dtype=dtype, autotune=autotune)
+    outs = b.outputs
+    b.close()
+    return outs

@@ -1,7 +1,7 @@
 // C ABI of libbeastgb: handles, validation, host-side tile planning and the assembly pipeline
 //
 //   upload spaces -> k_prepare_geo64 -> k_prepare_bounds -> k_classify (count, scan, fill)
-//   -> k_singular (FP64 Sauter-Schwab / near pairs) -> k_prepare_rec -> k_far_tiles
+//   -> k_singular (FP64 Sauter-Schwab / near pairs) -> k_prepare_rec -> k_far_persistent
 //   (FP64 or mixed) -> output on the device, or row blocks copied to the host.
 //
 // The pipeline mirrors assemble_gpu (assamble_gpu.jl:25-137) and assemblechunk_body_gpu!
@@ -9,7 +9,7 @@
 // reference, the write-back is a deterministic gather inside the far kernel (no FP64 atomics
 // into a 2 x N x N buffer, no make_complex pass) and non-far pairs of class "near" are integrated
 // (the reference drops them, quadrule_determine.jl:76 with doubleQuadRuleMainCase.jl:154).
-#include "bgb_kernels.cuh"
+#include "bgb_host.h"
 #include "trirules.h"
 
 #include <algorithm>
@@ -42,61 +42,14 @@ int cuda_fail(cudaError_t e, const char* what) {
   return e == cudaErrorMemoryAllocation ? BGB_ERR_OOM : BGB_ERR_CUDA;
 }
 
-// ----------------------------------------------------------------------------------------
-// Device buffers (grow-only, owned by the handle)
-// ----------------------------------------------------------------------------------------
-struct DevBuf {
-  void* p = nullptr;
-  size_t cap = 0;
-  int ensure(size_t bytes) {
-    if (bytes <= cap && p) return 0;
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-    size_t want = std::max<size_t>(bytes, 256);
-    cudaError_t e = cudaMalloc(&p, want);
-    if (e != cudaSuccess) {
-      p = nullptr;
-      return cuda_fail(e, "cudaMalloc");
-    }
-    cap = want;
-    return 0;
-  }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-  }
-  template <class T>
-  T* as() const { return (T*)p; }
-};
-
 }  // namespace bgb
-
-struct bgb_handle {
-  int device = 0;
-  int num_sms = 0;
-  cudaStream_t stream = nullptr;
-  cudaStream_t copy_stream = nullptr;
-  bgb_config cfg{};
-  volatile int* abort_host = nullptr;
-  int* abort_dev = nullptr;
-  std::mutex mu;
-  // buffers
-  bgb::DevBuf verts_t, tris_t, verts_b, tris_b, geo_t, geo_b, bnd_t, bnd_b, rec_t, rec_b;
-  bgb::DevBuf cls_count, cls_off, ent_tau, ent_sigma, ent_cls, sing_L, err;
-  bgb::DevBuf plan_i, plan_l, plan_d, plan_f;
-  bgb::DevBuf stage[2];
-  bgb::DevBuf diag_a, diag_b, diag_c, diag_d;
-  cudaEvent_t ev[8] = {};
-};
 
 namespace bgb {
 
 // ----------------------------------------------------------------------------------------
 // Validation
 // ----------------------------------------------------------------------------------------
-static int validate_space(const bgb_space* s, const char* name) {
+int validate_space(const bgb_space* s, const char* name) {
   if (!s) { set_error("%s space is NULL", name); return BGB_ERR_INVALID; }
   if (s->refspace != BGB_REFSPACE_LAGRANGE_C0D1 && s->refspace != BGB_REFSPACE_RT) {
     set_error("%s space: unknown refspace %d", name, s->refspace);
@@ -134,7 +87,7 @@ static int rule_index(int npoints) {
   return -1;
 }
 
-static RuleTable make_rules() {
+RuleTable make_rules() {
   RuleTable R{};
   for (int r = 0; r < BGB_TRIRULE_COUNT; ++r) {
     R.npoints[r] = bgb_trirule_npoints[r];
@@ -175,7 +128,7 @@ static void gauss_legendre01(int n, double* x, double* w) {
   }
 }
 
-static int make_quadsel(const bgb_quadstrat* qs, QuadSel* out) {
+int make_quadsel(const bgb_quadstrat* qs, QuadSel* out) {
   QuadSel q{};
   q.far_t = rule_index(qs->far_test);
   q.far_b = rule_index(qs->far_trial);
@@ -199,7 +152,7 @@ static int make_quadsel(const bgb_quadstrat* qs, QuadSel* out) {
   return 0;
 }
 
-static int make_opparams(const bgb_operator* op, const bgb_space* a, const bgb_space* b, OpParams* out) {
+int make_opparams(const bgb_operator* op, const bgb_space* a, const bgb_space* b, OpParams* out) {
   if (!op) { set_error("operator is NULL"); return BGB_ERR_INVALID; }
   if (op->kind == BGB_OP_HELMHOLTZ3D_SL) {
     if (a->refspace != BGB_REFSPACE_LAGRANGE_C0D1 || b->refspace != BGB_REFSPACE_LAGRANGE_C0D1) {
@@ -232,7 +185,7 @@ static int make_opparams(const bgb_operator* op, const bgb_space* a, const bgb_s
   return 0;
 }
 
-static FarConst make_farconst(const OpParams& op, const RuleTable& R, const QuadSel& qs) {
+FarConst make_farconst(const OpParams& op, const RuleTable& R, const QuadSel& qs) {
   FarConst k{};
   k.op_kind = op.kind;
   k.qt = R.npoints[qs.far_t];
@@ -277,7 +230,7 @@ static inline uint64_t spread3(uint64_t x) {
 }
 
 // Morton position of every triangle (rank in the order of 3-D Morton codes of centroids).
-static std::vector<int> morton_rank(const bgb_space* s) {
+std::vector<int> morton_rank(const bgb_space* s) {
   const int nt = s->nt;
   std::vector<double> c(3 * (size_t)nt);
   double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
@@ -307,13 +260,7 @@ static std::vector<int> morton_rank(const bgb_space* s) {
   return rank;
 }
 
-struct Supports {
-  std::vector<int64_t> off;  // [nfun + 1]
-  std::vector<int> tri, loc;
-  std::vector<double> coef;
-};
-
-static Supports build_supports(const bgb_space* s) {
+Supports build_supports(const bgb_space* s) {
   Supports S;
   S.off.assign((size_t)s->nfun + 1, 0);
   for (int64_t t = 0; t < s->nt; ++t)
@@ -339,7 +286,7 @@ static Supports build_supports(const bgb_space* s) {
 }
 
 // Functions [f_begin, f_end) ordered by the Morton rank of their first support.
-static std::vector<int> order_functions(const Supports& S, const std::vector<int>& rank, int f_begin, int f_end) {
+std::vector<int> order_functions(const Supports& S, const std::vector<int>& rank, int f_begin, int f_end) {
   std::vector<std::pair<int64_t, int>> key;
   key.reserve(f_end - f_begin);
   for (int f = f_begin; f < f_end; ++f) {
@@ -353,20 +300,7 @@ static std::vector<int> order_functions(const Supports& S, const std::vector<int
   return out;
 }
 
-struct HostPlan {
-  // test side
-  std::vector<int> tb_off, tb_tris, tb_fn_off, fs_off, fs_code;
-  std::vector<double> fs_coef;
-  std::vector<int64_t> rows;
-  // trial side
-  std::vector<int> bb_off, bb_tris, bb_fn_off, bb_chunk_off, ch_grp_off, grp_fn, grp_sup_off, gs_code;
-  std::vector<double> gs_coef;
-  std::vector<int64_t> cols;
-  int tmax = 0, nmax = 0, MAXS = 1, gmax = 1, gsmax = 1;
-  int64_t pairs = 0;  // triangle pairs computed by the tiles (incl. halo)
-};
-
-static void plan_test_side(const Supports& S, const std::vector<int>& order, int FM, int64_t row0, HostPlan& P) {
+void plan_test_side(const Supports& S, const std::vector<int>& order, int FM, int64_t row0, HostPlan& P) {
   P.tb_off.push_back(0);
   P.tb_fn_off.push_back(0);
   P.fs_off.push_back(0);
@@ -400,7 +334,7 @@ static void plan_test_side(const Supports& S, const std::vector<int>& order, int
   }
 }
 
-static void plan_trial_side(const Supports& S, const std::vector<int>& order, int FN, int SC, HostPlan& P) {
+void plan_trial_side(const Supports& S, const std::vector<int>& order, int FN, int SC, HostPlan& P) {
   P.bb_off.push_back(0);
   P.bb_fn_off.push_back(0);
   P.bb_chunk_off.push_back(0);
@@ -461,8 +395,7 @@ static void plan_trial_side(const Supports& S, const std::vector<int>& order, in
 }
 
 // Tile configurations: (FM, FN, SC) per precision.
-struct TileCfg { int FM, FN, SC; };
-static const TileCfg kTileCfgs[] = {
+const TileCfg kTileCfgs[] = {
     {64, 64, 16},   // 0: mixed, RWG
     {64, 64, 8},    // 1
     {128, 64, 8},   // 2
@@ -478,9 +411,11 @@ static const TileCfg kTileCfgs[] = {
     {56, 56, 8},    // 12
 };
 // Preference order when the caller does not pin a tile: the first whose shared memory fits.
-static const int kPrefMixed[] = {8, 1, 5, 6, 7};
-static const int kPrefFp64[] = {4, 8, 5, 6, 7};
-static const int kNumTileCfgs = sizeof(kTileCfgs) / sizeof(kTileCfgs[0]);
+const int kPrefMixed[] = {4, 8, 1, 5, 6, 7};
+const int kNumPrefMixed = sizeof(kPrefMixed) / sizeof(int);
+const int kPrefFp64[] = {4, 8, 5, 6, 7};
+const int kNumPrefFp64 = sizeof(kPrefFp64) / sizeof(int);
+const int kNumTileCfgs = sizeof(kTileCfgs) / sizeof(kTileCfgs[0]);
 
 // ----------------------------------------------------------------------------------------
 // Upload helpers
@@ -504,7 +439,7 @@ static int upload_space(bgb_handle* h, const bgb_space* s, DevBuf& verts, DevBuf
   return 0;
 }
 
-static bool same_space(const bgb_space* a, const bgb_space* b) {
+bool same_space(const bgb_space* a, const bgb_space* b) {
   return a == b || (a->vertices == b->vertices && a->triangles == b->triangles && a->nv == b->nv && a->nt == b->nt);
 }
 
@@ -552,7 +487,7 @@ static int classify_all(bgb_handle* h, const bgb_space* test, const bgb_space* t
   return 0;
 }
 
-static double event_ms(cudaEvent_t a, cudaEvent_t b) {
+double event_ms(cudaEvent_t a, cudaEvent_t b) {
   float ms = 0.f;
   cudaEventElapsedTime(&ms, a, b);
   return ms;
@@ -619,7 +554,7 @@ int bgb_destroy(bgb_handle* h) {
   if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
   DevBuf* bufs[] = {&h->verts_t, &h->tris_t, &h->verts_b, &h->tris_b, &h->geo_t, &h->geo_b, &h->bnd_t, &h->bnd_b,
                     &h->rec_t, &h->rec_b, &h->cls_count, &h->cls_off, &h->ent_tau, &h->ent_sigma, &h->ent_cls,
-                    &h->sing_L, &h->err, &h->plan_i, &h->plan_l, &h->plan_d, &h->plan_f, &h->stage[0], &h->stage[1],
+                    &h->sing_L, &h->err, &h->plan_i, &h->plan_l, &h->plan_d, &h->plan_f, &h->far_items, &h->far_const, &h->stage[0], &h->stage[1],
                     &h->diag_a, &h->diag_b, &h->diag_c, &h->diag_d};
   for (DevBuf* b : bufs) b->release();
   for (int i = 0; i < 8; ++i)
@@ -948,9 +883,33 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
     T.out = dst;
     T.ld = dld;
     cudaEventRecord(h->ev[3], h->stream);
-    if ((rc = launch_far_tiles(precision, K, T, h->stream))) return rc;
+    // the single problem runs through the same persistent work-queue kernel as batches
+    // (one far kernel, so batched and single assemblies are bit-identical); tiles are
+    // queued row block fastest so concurrent CTAs write neighbouring rows of a column
+    std::vector<int4> items;
+    items.reserve((size_t)T.n_tblocks * T.n_bblocks);
+    for (int bn = 0; bn < T.n_bblocks; ++bn)
+      for (int bm = 0; bm < T.n_tblocks; ++bm) items.push_back(make_int4(0, bm, bn, 0));
+    if ((rc = h->far_items.ensure(sizeof(int4) * std::max<size_t>(1, items.size()))) ||
+        (rc = h->far_const.ensure(sizeof(FarConst) + sizeof(TilePlan) + sizeof(int) * 4)))
+      return rc;
+    FarConst* dK = (FarConst*)h->far_const.p;
+    TilePlan* dT = (TilePlan*)((char*)h->far_const.p + sizeof(FarConst));
+    int* dctr = (int*)((char*)h->far_const.p + sizeof(FarConst) + sizeof(TilePlan));
+    BGB_CUDA(cudaMemcpyAsync(dK, &K, sizeof(FarConst), cudaMemcpyHostToDevice, h->stream));
+    BGB_CUDA(cudaMemcpyAsync(dT, &T, sizeof(TilePlan), cudaMemcpyHostToDevice, h->stream));
+    if (!items.empty())
+      BGB_CUDA(cudaMemcpyAsync(h->far_items.p, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice, h->stream));
+    BGB_CUDA(cudaMemsetAsync(dctr, 0, sizeof(int), h->stream));
+    int per_sm = 0;
+    if ((rc = far_persistent_occupancy(precision, K.op_kind, gen, smem, &per_sm))) return rc;
+    const int ctas = (int)std::min<int64_t>((int64_t)items.size(), (int64_t)std::max(1, per_sm) * h->num_sms);
+    if ((rc = launch_far_persistent(precision, K.op_kind, gen, dK, dT, (const int4*)h->far_items.p, (int)items.size(),
+                                    dctr, smem, std::max(1, ctas), h->abort_dev, h->stream)))
+      return rc;
     ++launches;
     cudaEventRecord(h->ev[4], h->stream);
+    BGB_CUDA(cudaStreamSynchronize(h->stream));  // plan, items and constants are reused by the next row block
     if (host_out) {
       char* hdst = (char*)out + (size_t)(r0 - row0) * esz;
       BGB_CUDA(cudaMemcpy2DAsync(hdst, (size_t)ld * esz, dst, (size_t)nr * esz, (size_t)nr * esz, (size_t)trial->nfun,
@@ -985,30 +944,6 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
   st.ms_total = std::chrono::duration<double, std::milli>(clk::now() - t_start).count();
   st.kernel_launches = launches;
   if (stats) *stats = st;
-  return 0;
-}
-
-int bgb_assemble_batch(bgb_handle* h, int32_t n, const bgb_problem* problems, int32_t precision, int32_t out_kind,
-                       void* stream, bgb_stats* stats) {
-  if (!h || n < 0 || (n && !problems)) { set_error("invalid argument"); return BGB_ERR_INVALID; }
-  bgb_stats acc{};
-  for (int i = 0; i < n; ++i) {
-    bgb_stats s1{};
-    const bgb_problem& p = problems[i];
-    int rc = bgb_assemble(h, &p.op, &p.test, &p.trial, &p.qs, precision, p.out, out_kind, p.ld, 0, -1, stream, &s1);
-    if (rc) return rc;
-    acc.pairs_total += s1.pairs_total;
-    acc.pairs_computed += s1.pairs_computed;
-    for (int c = 0; c < 5; ++c) acc.pairs_class[c] += s1.pairs_class[c];
-    acc.ms_classify += s1.ms_classify;
-    acc.ms_singular += s1.ms_singular;
-    acc.ms_far += s1.ms_far;
-    acc.ms_copy += s1.ms_copy;
-    acc.ms_total += s1.ms_total;
-    acc.row_blocks += s1.row_blocks;
-    acc.kernel_launches += s1.kernel_launches;
-  }
-  if (stats) *stats = acc;
   return 0;
 }
 

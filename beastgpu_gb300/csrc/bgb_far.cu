@@ -11,17 +11,6 @@ BGB_FAR_EXTERN(PFp64, 1)
 BGB_FAR_EXTERN(PFp64, 2)
 
 template <class P, int QT, int QB>
-static int dispatch_op(const FarConst& K, const TilePlan& p, cudaStream_t st) {
-  switch (K.op_kind) {
-    case BGB_OP_HELMHOLTZ3D_SL: return launch_tiles_t<P, BGB_OP_HELMHOLTZ3D_SL, QT, QB>(K, p, st);
-    case BGB_OP_MAXWELL3D_SL: return launch_tiles_t<P, BGB_OP_MAXWELL3D_SL, QT, QB>(K, p, st);
-    case BGB_OP_MAXWELL3D_DL: return launch_tiles_t<P, BGB_OP_MAXWELL3D_DL, QT, QB>(K, p, st);
-  }
-  set_error("unknown operator kind %d", K.op_kind);
-  return BGB_ERR_INVALID;
-}
-
-template <class P, int QT, int QB>
 static int dispatch_diag(const FarConst& K, const void* rt, const void* rb, const int* tau, const int* sigma,
                          int64_t n, double2* out, cudaStream_t st) {
   switch (K.op_kind) {
@@ -32,9 +21,52 @@ static int dispatch_diag(const FarConst& K, const void* rt, const void* rb, cons
   set_error("unknown operator kind %d", K.op_kind);
   return BGB_ERR_INVALID;
 }
+template <class P, int QT, int QB>
+static int dispatch_persistent(int op_kind, const FarConst* Ks, const TilePlan* plans, const int4* items, int nitems,
+                               int* counter, size_t smem, int ctas, const volatile int* ab, cudaStream_t st) {
+  switch (op_kind) {
+    case BGB_OP_HELMHOLTZ3D_SL:
+      return launch_persistent_t<P, BGB_OP_HELMHOLTZ3D_SL, QT, QB>(Ks, plans, items, nitems, counter, smem, ctas, ab, st);
+    case BGB_OP_MAXWELL3D_SL:
+      return launch_persistent_t<P, BGB_OP_MAXWELL3D_SL, QT, QB>(Ks, plans, items, nitems, counter, smem, ctas, ab, st);
+    case BGB_OP_MAXWELL3D_DL:
+      return launch_persistent_t<P, BGB_OP_MAXWELL3D_DL, QT, QB>(Ks, plans, items, nitems, counter, smem, ctas, ab, st);
+  }
+  set_error("unknown operator kind %d", op_kind);
+  return BGB_ERR_INVALID;
+}
+
+template <class P, int QT, int QB>
+static int dispatch_occupancy(int op_kind, size_t smem, int* per_sm) {
+  switch (op_kind) {
+    case BGB_OP_HELMHOLTZ3D_SL: return occupancy_t<P, BGB_OP_HELMHOLTZ3D_SL, QT, QB>(smem, per_sm);
+    case BGB_OP_MAXWELL3D_SL: return occupancy_t<P, BGB_OP_MAXWELL3D_SL, QT, QB>(smem, per_sm);
+    case BGB_OP_MAXWELL3D_DL: return occupancy_t<P, BGB_OP_MAXWELL3D_DL, QT, QB>(smem, per_sm);
+  }
+  set_error("unknown operator kind %d", op_kind);
+  return BGB_ERR_INVALID;
+}
 }  // namespace farimpl
 
 using namespace farimpl;
+
+int launch_far_persistent(int precision, int op_kind, int generic, const FarConst* Ks, const TilePlan* plans,
+                          const int4* items, int nitems, int* counter, size_t smem_bytes, int ctas,
+                          const volatile int* abort_flag, cudaStream_t st) {
+  if (precision == BGB_PREC_MIXED)
+    return generic ? dispatch_persistent<PMixed, BGB_MAXQ, BGB_MAXQ>(op_kind, Ks, plans, items, nitems, counter, smem_bytes, ctas, abort_flag, st)
+                   : dispatch_persistent<PMixed, 3, 4>(op_kind, Ks, plans, items, nitems, counter, smem_bytes, ctas, abort_flag, st);
+  return generic ? dispatch_persistent<PFp64, BGB_MAXQ, BGB_MAXQ>(op_kind, Ks, plans, items, nitems, counter, smem_bytes, ctas, abort_flag, st)
+                 : dispatch_persistent<PFp64, 3, 4>(op_kind, Ks, plans, items, nitems, counter, smem_bytes, ctas, abort_flag, st);
+}
+
+int far_persistent_occupancy(int precision, int op_kind, int generic, size_t smem_bytes, int* per_sm) {
+  if (precision == BGB_PREC_MIXED)
+    return generic ? dispatch_occupancy<PMixed, BGB_MAXQ, BGB_MAXQ>(op_kind, smem_bytes, per_sm)
+                   : dispatch_occupancy<PMixed, 3, 4>(op_kind, smem_bytes, per_sm);
+  return generic ? dispatch_occupancy<PFp64, BGB_MAXQ, BGB_MAXQ>(op_kind, smem_bytes, per_sm)
+                 : dispatch_occupancy<PFp64, 3, 4>(op_kind, smem_bytes, per_sm);
+}
 
 int far_generic_q(int qt, int qb) { return !(qt == 3 && qb == 4); }
 
@@ -48,13 +80,6 @@ size_t far_smem_bytes(int precision, int qt, int qb, const TilePlan& p) {
   if (precision == BGB_PREC_MIXED)
     return gen ? smem_t<PMixed, 0, BGB_MAXQ, BGB_MAXQ>(p) : smem_t<PMixed, 0, 3, 4>(p);
   return gen ? smem_t<PFp64, 0, BGB_MAXQ, BGB_MAXQ>(p) : smem_t<PFp64, 0, 3, 4>(p);
-}
-
-int launch_far_tiles(int precision, const FarConst& k, const TilePlan& p, cudaStream_t st) {
-  const bool gen = far_generic_q(k.qt, k.qb);
-  if (precision == BGB_PREC_MIXED)
-    return gen ? dispatch_op<PMixed, BGB_MAXQ, BGB_MAXQ>(k, p, st) : dispatch_op<PMixed, 3, 4>(k, p, st);
-  return gen ? dispatch_op<PFp64, BGB_MAXQ, BGB_MAXQ>(k, p, st) : dispatch_op<PFp64, 3, 4>(k, p, st);
 }
 
 int launch_far_pairs_diag(int precision, const FarConst& k, const void* rt, const void* rb, const int* tau,

@@ -51,6 +51,7 @@ struct Off64 {
 struct PMixed {
   using R = float;
   using C = float2;
+  static constexpr int kMinBlocks = 3;  // 3 CTAs of 256 threads per SM (<= 85 registers)
   template <int Q>
   static constexpr int rec() { return Off32<Q>::SIZE; }
   static __device__ __forceinline__ C mk(double a, double b) { return make_float2((float)a, (float)b); }
@@ -58,6 +59,7 @@ struct PMixed {
 struct PFp64 {
   using R = double;
   using C = double2;
+  static constexpr int kMinBlocks = 1;
   template <int Q>
   static constexpr int rec() { return Off64<Q>::SIZE; }
   static __device__ __forceinline__ C mk(double a, double b) { return make_double2(a, b); }
@@ -67,7 +69,8 @@ struct PFp64 {
 // Mixed FP32 far pair
 // ----------------------------------------------------------------------------------------
 template <int OP, int QT, int QB>
-__device__ __forceinline__ void far_pair_mixed(const FarConst& K, const float* __restrict__ a,
+__device__ __forceinline__ void far_pair_mixed(const FarScalars& K, const float (*__restrict__ shpT)[3],
+                                               const float (*__restrict__ shpB)[3], const float* __restrict__ a,
                                                const float* __restrict__ b, float2 L[9]) {
   using OA = Off32<QT>;
   using OB = Off32<QB>;
@@ -150,7 +153,7 @@ __device__ __forceinline__ void far_pair_mixed(const FarConst& K, const float* _
       if (OP == BGB_OP_HELMHOLTZ3D_SL) {
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
-          const float g = K.shpB[J][j];
+          const float g = shpB[J][j];
           M[j].x = fmaf(gr, g, M[j].x);
           M[j].y = fmaf(gi, g, M[j].y);
         }
@@ -178,7 +181,7 @@ __device__ __forceinline__ void far_pair_mixed(const FarConst& K, const float* _
     if (OP == BGB_OP_HELMHOLTZ3D_SL) {
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
-        const float f = K.shpT[I][i];
+        const float f = shpT[I][i];
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
           L[i * 3 + j].x = fmaf(f, M[j].x, L[i * 3 + j].x);
@@ -280,7 +283,8 @@ __device__ __forceinline__ void far_pair_mixed(const FarConst& K, const float* _
 // Plain FP64 far pair (same accumulation structure, FP64 throughout, CUDA sincos / exp)
 // ----------------------------------------------------------------------------------------
 template <int OP, int QT, int QB>
-__device__ __forceinline__ void far_pair_fp64(const FarConst& K, const double* __restrict__ a,
+__device__ __forceinline__ void far_pair_fp64(const FarScalars& K, const double (*__restrict__ shpT)[3],
+                                              const double (*__restrict__ shpB)[3], const double* __restrict__ a,
                                               const double* __restrict__ b, double2 L[9]) {
   using OA = Off64<QT>;
   using OB = Off64<QB>;
@@ -320,7 +324,7 @@ __device__ __forceinline__ void far_pair_fp64(const FarConst& K, const double* _
       if (OP == BGB_OP_HELMHOLTZ3D_SL) {
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
-          const double g = K.shpB64[J][j];
+          const double g = shpB[J][j];
           M[j].x = fma(gr, g, M[j].x);
           M[j].y = fma(gi, g, M[j].y);
         }
@@ -346,7 +350,7 @@ __device__ __forceinline__ void far_pair_fp64(const FarConst& K, const double* _
     if (OP == BGB_OP_HELMHOLTZ3D_SL) {
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
-        const double f = K.shpT64[I][i];
+        const double f = shpT[I][i];
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
           L[i * 3 + j].x = fma(f, M[j].x, L[i * 3 + j].x);
@@ -440,13 +444,32 @@ __device__ __forceinline__ void far_pair_fp64(const FarConst& K, const double* _
   }
 }
 
+__device__ __forceinline__ FarScalars far_scalars(const FarConst& K) {
+  FarScalars S;
+  S.qt = K.qt;
+  S.qb = K.qb;
+  S.lossy = K.lossy;
+  S.pad = 0;
+  S.k_hi = K.k_hi;
+  S.k_lo = K.k_lo;
+  S.gre = K.gre;
+  for (int c = 0; c < 2; ++c) {
+    S.alpha32[c] = K.alpha32[c];
+    S.beta32[c] = K.beta32[c];
+    S.alpha[c] = K.alpha[c];
+    S.beta[c] = K.beta[c];
+    S.gamma[c] = K.gamma[c];
+  }
+  return S;
+}
+
 template <class P, int OP, int QT, int QB>
-__device__ __forceinline__ void far_pair(const FarConst& K, const typename P::R* a, const typename P::R* b,
-                                         typename P::C L[9]) {
+__device__ __forceinline__ void far_pair(const FarScalars& S, const FarConst& K, const typename P::R* a,
+                                         const typename P::R* b, typename P::C L[9]) {
   if constexpr (sizeof(typename P::R) == 4)
-    far_pair_mixed<OP, QT, QB>(K, a, b, L);
+    far_pair_mixed<OP, QT, QB>(S, K.shpT, K.shpB, a, b, L);
   else
-    far_pair_fp64<OP, QT, QB>(K, a, b, L);
+    far_pair_fp64<OP, QT, QB>(S, K.shpT64, K.shpB64, a, b, L);
 }
 
 __device__ __forceinline__ int64_t find_sigma(const int64_t* __restrict__ off, const int* __restrict__ sig, int tau,
@@ -519,19 +542,18 @@ __host__ __device__ inline size_t carve(unsigned char* base, int tmax, int nmax,
   return off;
 }
 
+// One output tile (test-function block bm x trial-function block bn).
 template <class P, int OP, int QT, int QB>
-__global__ void __launch_bounds__(kThreads) k_far_tiles(const __grid_constant__ FarConst K,
-                                                        const __grid_constant__ TilePlan p) {
+__device__ __forceinline__ void tile_body(const FarConst& K, const TilePlan& p, int bm, int bn, unsigned char* smem) {
   using R = typename P::R;
   using C = typename P::C;
   constexpr int RT = P::template rec<QT>();
   constexpr int RB = P::template rec<QB>();
-  extern __shared__ __align__(16) unsigned char smem[];
   const int tid = threadIdx.x;
-  const int bm = blockIdx.x, bn = blockIdx.y;
-  if (p.abort_flag && *p.abort_flag) return;
+  const FarScalars S = far_scalars(K);  // registers, not shared-memory loads in the pair loop
+  const int SC = p.SC, MAXS = p.MAXS;
   Smem<P> s;
-  carve<P>(smem, p.tmax, p.nmax, RT, RB, p.FM, p.FN, p.MAXS, p.SC, p.gmax, p.gsmax, &s);
+  carve<P>(smem, p.tmax, p.nmax, RT, RB, p.FM, p.FN, MAXS, SC, p.gmax, p.gsmax, &s);
 
   const int t0 = p.tb_off[bm], tm = p.tb_off[bm + 1] - t0;
   const int b0 = p.bb_off[bn], nbk = p.bb_off[bn + 1] - b0;
@@ -561,11 +583,11 @@ __global__ void __launch_bounds__(kThreads) k_far_tiles(const __grid_constant__ 
   const bool f32 = sizeof(R) == 4;
   for (int m = tid; m < fm; m += kThreads) {
     const int a0 = p.fs_off[f0 + m], a1 = p.fs_off[f0 + m + 1];
-    const int cnt = min(a1 - a0, p.MAXS);
+    const int cnt = min(a1 - a0, MAXS);
     s.fcnt[m] = cnt;
     for (int k = 0; k < cnt; ++k) {
-      s.fcode[m * p.MAXS + k] = p.fs_code[a0 + k];
-      s.fcoef[m * p.MAXS + k] = f32 ? (R)p.fs_coef32[a0 + k] : (R)p.fs_coef[a0 + k];
+      s.fcode[m * MAXS + k] = p.fs_code[a0 + k];
+      s.fcoef[m * MAXS + k] = f32 ? (R)p.fs_coef32[a0 + k] : (R)p.fs_coef[a0 + k];
     }
   }
   // the trial block's gather groups (all chunks), block-relative
@@ -585,10 +607,10 @@ __global__ void __launch_bounds__(kThreads) k_far_tiles(const __grid_constant__ 
   for (int i = tid; i < fm * fn; i += kThreads) s.Zs[i] = P::mk(0.0, 0.0);
   __syncthreads();
 
-  const int LS = p.tmax * p.SC;
+  const int LS = p.tmax * SC;
   for (int c = c0; c < c1; ++c) {
-    const int sbase = (c - c0) * p.SC;
-    const int scn = min(p.SC, nbk - sbase);
+    const int sbase = (c - c0) * SC;
+    const int scn = min(SC, nbk - sbase);
     const int np = tm * scn;
     for (int q = tid; q < np; q += kThreads) {
       const int ti = q / scn, si = q - ti * scn;
@@ -606,8 +628,8 @@ __global__ void __launch_bounds__(kThreads) k_far_tiles(const __grid_constant__ 
           done = true;
         }
       }
-      if (!done) far_pair<P, OP, QT, QB>(K, s.recT + ti * RT, s.recB + sb * RB, L);
-      const int li = ti * p.SC + si;
+      if (!done) far_pair<P, OP, QT, QB>(S, K, s.recT + ti * RT, s.recB + sb * RB, L);
+      const int li = ti * SC + si;
 #pragma unroll
       for (int k = 0; k < 9; ++k) s.Lbuf[k * LS + li] = L[k];
     }
@@ -625,10 +647,10 @@ __global__ void __launch_bounds__(kThreads) k_far_tiles(const __grid_constant__ 
         const int sl = (code >> 2) - sbase, j = code & 3;
         const R cb = s.gsCoef[bsup];
         for (int a = 0; a < cnt; ++a) {
-          const int fc = s.fcode[m * p.MAXS + a];
+          const int fc = s.fcode[m * MAXS + a];
           const int ta = fc >> 2, i = fc & 3;
-          const R w = s.fcoef[m * p.MAXS + a] * cb;
-          const C l = s.Lbuf[(i * 3 + j) * LS + ta * p.SC + sl];
+          const R w = s.fcoef[m * MAXS + a] * cb;
+          const C l = s.Lbuf[(i * 3 + j) * LS + ta * SC + sl];
           acc.x = fma(w, l.x, acc.x);
           acc.y = fma(w, l.y, acc.y);
         }
@@ -643,6 +665,37 @@ __global__ void __launch_bounds__(kThreads) k_far_tiles(const __grid_constant__ 
     const C v = s.Zs[i];
     if (p.out_c64) ((double2*)p.out)[idx] = make_double2(v.x, v.y);
     else ((float2*)p.out)[idx] = make_float2((float)v.x, (float)v.y);
+  }
+}
+
+// The far kernel: persistent CTAs pull tiles (problem, bm, bn) from a work queue (an atomic
+// counter; no CTA ever waits on another).  A single assembly is a one-problem queue.  Each
+// problem has its own constants (wave number, alpha, beta) and plan; the tile shape and rules
+// are common to the launch.  The problem's constants and plan are copied to shared memory
+// per tile.
+template <class P, int OP, int QT, int QB>
+__global__ void __launch_bounds__(kThreads, P::kMinBlocks) k_far_persistent(const FarConst* __restrict__ Ks,
+                                                             const TilePlan* __restrict__ plans,
+                                                             const int4* __restrict__ items, int nitems,
+                                                             int* __restrict__ counter,
+                                                             const volatile int* abort_flag) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int next;
+  __shared__ FarConst sK;
+  __shared__ TilePlan sP;
+  for (;;) {
+    if (threadIdx.x == 0) next = (abort_flag && *abort_flag) ? nitems : atomicAdd(counter, 1);
+    __syncthreads();
+    const int t = next;
+    if (t >= nitems) return;
+    const int4 it = items[t];
+    for (int i = threadIdx.x; i < (int)(sizeof(FarConst) / 4); i += kThreads)
+      ((int*)&sK)[i] = ((const int*)&Ks[it.x])[i];
+    for (int i = threadIdx.x; i < (int)(sizeof(TilePlan) / 4); i += kThreads)
+      ((int*)&sP)[i] = ((const int*)&plans[it.x])[i];
+    __syncthreads();
+    tile_body<P, OP, QT, QB>(sK, sP, it.y, it.z, smem);
+    __syncthreads();
   }
 }
 
@@ -725,26 +778,31 @@ __global__ void k_far_pairs_diag(const __grid_constant__ FarConst K, const typen
   constexpr int RB = P::template rec<QB>();
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
     typename P::C L[9];
-    far_pair<P, OP, QT, QB>(K, rt + (int64_t)tau[e] * RT, rb + (int64_t)sigma[e] * RB, L);
+    far_pair<P, OP, QT, QB>(far_scalars(K), K, rt + (int64_t)tau[e] * RT, rb + (int64_t)sigma[e] * RB, L);
 #pragma unroll
     for (int k = 0; k < 9; ++k) out[e * 9 + k] = make_double2(L[k].x, L[k].y);
   }
 }
 
 template <class P, int OP, int QT, int QB>
-int launch_tiles_t(const FarConst& K, const TilePlan& p, cudaStream_t st) {
-  constexpr int RT = P::template rec<QT>();
-  constexpr int RB = P::template rec<QB>();
-  const size_t bytes = carve<P>(nullptr, p.tmax, p.nmax, RT, RB, p.FM, p.FN, p.MAXS, p.SC, p.gmax, p.gsmax, nullptr);
-  auto kern = k_far_tiles<P, OP, QT, QB>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(far tiles)");
-  if (p.n_tblocks <= 0 || p.n_bblocks <= 0) return 0;
-  dim3 grid(p.n_tblocks, p.n_bblocks);
-  kern<<<grid, kThreads, bytes, st>>>(K, p);
+int launch_persistent_t(const FarConst* Ks, const TilePlan* plans, const int4* items, int nitems, int* counter,
+                        size_t smem_bytes, int ctas, const volatile int* abort_flag, cudaStream_t st) {
+  auto kern = k_far_persistent<P, OP, QT, QB>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(far persistent)");
+  if (nitems <= 0) return 0;
+  kern<<<ctas, kThreads, smem_bytes, st>>>(Ks, plans, items, nitems, counter, abort_flag);
   e = cudaGetLastError();
-  if (e != cudaSuccess) return cuda_fail(e, "k_far_tiles launch");
-  return 0;
+  return e == cudaSuccess ? 0 : cuda_fail(e, "k_far_persistent launch");
+}
+
+template <class P, int OP, int QT, int QB>
+int occupancy_t(size_t smem_bytes, int* per_sm) {
+  cudaError_t e = cudaFuncSetAttribute(k_far_persistent<P, OP, QT, QB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem_bytes);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(far persistent)");
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_far_persistent<P, OP, QT, QB>, kThreads, smem_bytes);
+  return e == cudaSuccess ? 0 : cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
 }
 
 template <class P, int OP, int QT, int QB>
@@ -766,13 +824,18 @@ int launch_diag_t(const FarConst& K, const void* rt, const void* rb, const int* 
 
 // Instances live in bgb_far_{mixed,fp64}_op{0,1,2}.cu.
 #define BGB_FAR_EXTERN(P, OP)                                                                                   \
-  extern template int launch_tiles_t<P, OP, 3, 4>(const FarConst&, const TilePlan&, cudaStream_t);             \
-  extern template int launch_tiles_t<P, OP, BGB_MAXQ, BGB_MAXQ>(const FarConst&, const TilePlan&, cudaStream_t); \
   extern template int launch_diag_t<P, OP, 3, 4>(const FarConst&, const void*, const void*, const int*,        \
                                                  const int*, int64_t, double2*, cudaStream_t);                \
   extern template int launch_diag_t<P, OP, BGB_MAXQ, BGB_MAXQ>(const FarConst&, const void*, const void*,      \
                                                                const int*, const int*, int64_t, double2*,     \
-                                                               cudaStream_t);
+                                                               cudaStream_t);                                 \
+  extern template int launch_persistent_t<P, OP, 3, 4>(const FarConst*, const TilePlan*, const int4*, int, int*, \
+                                                       size_t, int, const volatile int*, cudaStream_t);        \
+  extern template int launch_persistent_t<P, OP, BGB_MAXQ, BGB_MAXQ>(const FarConst*, const TilePlan*,       \
+                                                                     const int4*, int, int*, size_t, int,      \
+                                                                     const volatile int*, cudaStream_t);       \
+  extern template int occupancy_t<P, OP, 3, 4>(size_t, int*);                                                 \
+  extern template int occupancy_t<P, OP, BGB_MAXQ, BGB_MAXQ>(size_t, int*);
 
 }  // namespace farimpl
 }  // namespace bgb

@@ -1,0 +1,101 @@
+// Host-side declarations shared by the C-ABI translation units (handle, buffers, planning).
+#pragma once
+
+#include "bgb_kernels.cuh"
+
+#include <mutex>
+#include <vector>
+
+namespace bgb {
+
+// ----------------------------------------------------------------------------------------
+// Device buffers (grow-only, owned by the handle)
+// ----------------------------------------------------------------------------------------
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  int ensure(size_t bytes) {
+    if (bytes <= cap && p) return 0;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = std::max<size_t>(bytes, 256);
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return cuda_fail(e, "cudaMalloc");
+    }
+    cap = want;
+    return 0;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <class T>
+  T* as() const { return (T*)p; }
+};
+
+}  // namespace bgb
+
+struct bgb_handle {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  cudaStream_t copy_stream = nullptr;
+  bgb_config cfg{};
+  volatile int* abort_host = nullptr;
+  int* abort_dev = nullptr;
+  std::mutex mu;
+  // buffers
+  bgb::DevBuf verts_t, tris_t, verts_b, tris_b, geo_t, geo_b, bnd_t, bnd_b, rec_t, rec_b;
+  bgb::DevBuf cls_count, cls_off, ent_tau, ent_sigma, ent_cls, sing_L, err;
+  bgb::DevBuf plan_i, plan_l, plan_d, plan_f, far_items, far_const;
+  bgb::DevBuf stage[2];
+  bgb::DevBuf diag_a, diag_b, diag_c, diag_d;
+  cudaEvent_t ev[8] = {};
+};
+
+
+namespace bgb {
+
+struct Supports {
+  std::vector<int64_t> off;  // [nfun + 1]
+  std::vector<int> tri, loc;
+  std::vector<double> coef;
+};
+
+struct HostPlan {
+  std::vector<int> tb_off, tb_tris, tb_fn_off, fs_off, fs_code;
+  std::vector<double> fs_coef;
+  std::vector<int64_t> rows;
+  std::vector<int> bb_off, bb_tris, bb_fn_off, bb_chunk_off, ch_grp_off, grp_fn, grp_sup_off, gs_code;
+  std::vector<double> gs_coef;
+  std::vector<int64_t> cols;
+  int tmax = 0, nmax = 0, MAXS = 1, gmax = 1, gsmax = 1;
+  int64_t pairs = 0;
+};
+
+struct TileCfg { int FM, FN, SC; };
+extern const TileCfg kTileCfgs[];
+extern const int kNumTileCfgs;
+extern const int kPrefMixed[];
+extern const int kNumPrefMixed;
+extern const int kPrefFp64[];
+extern const int kNumPrefFp64;
+
+int validate_space(const bgb_space* s, const char* name);
+int make_quadsel(const bgb_quadstrat* qs, QuadSel* out);
+int make_opparams(const bgb_operator* op, const bgb_space* a, const bgb_space* b, OpParams* out);
+RuleTable make_rules();
+FarConst make_farconst(const OpParams& op, const RuleTable& R, const QuadSel& qs);
+std::vector<int> morton_rank(const bgb_space* s);
+Supports build_supports(const bgb_space* s);
+std::vector<int> order_functions(const Supports& S, const std::vector<int>& rank, int f_begin, int f_end);
+void plan_test_side(const Supports& S, const std::vector<int>& order, int FM, int64_t row0, HostPlan& P);
+void plan_trial_side(const Supports& S, const std::vector<int>& order, int FN, int SC, HostPlan& P);
+bool same_space(const bgb_space* a, const bgb_space* b);
+double event_ms(cudaEvent_t a, cudaEvent_t b);
+
+}  // namespace bgb

@@ -21,6 +21,17 @@ void launch_local_diag64(const OpParams& op, const QuadSel& qs, const RuleTable&
                          const Geo64* tg, const Geo64* bg, const int* tau, const int* sigma, int64_t n, int force,
                          double2* out, int8_t* cls, int* err, int num_sms, cudaStream_t st);
 
+void launch_prepare_bounds_batched(const Geo64* g, int nt, const int* tri_problem, const double* prob_k2, int trial_side,
+                                   float4* out, cudaStream_t st);
+void launch_classify_batched(bool fill, const float4* tb, const float4* bb, const Geo64* tg, const Geo64* bg, int nt,
+                             const int* tri_problem, const int2* prob_trial, const double* prob_k2, int* count,
+                             const int64_t* offset, int* out_tau, int* out_sigma, int8_t* out_cls, int* err,
+                             int num_sms, cudaStream_t st);
+void launch_singular_batched(int op_kind, const OpParams* ops, const QuadSel& qs, const RuleTable& rules,
+                             const Geo64* tg, const Geo64* bg, const int* tri_problem, const int* et, const int* es,
+                             const int8_t* ec, int64_t n, double2* out, const volatile int* abort_flag, int num_sms,
+                             cudaStream_t st);
+
 // ---- bgb_far.cu ------------------------------------------------------------------------
 // Constants of the far-pair kernels (passed by value).
 struct FarConst {
@@ -32,6 +43,14 @@ struct FarConst {
   float k_hi, k_lo, gre;       // gamma_im as double-float, gamma_re
   float shpT[BGB_MAXQ][3], shpB[BGB_MAXQ][3];     // Lagrange hats at rule points
   double shpT64[BGB_MAXQ][3], shpB64[BGB_MAXQ][3];
+};
+
+// The scalar constants of a far launch, copied into registers per tile.
+struct FarScalars {
+  int qt, qb, lossy, pad;
+  float k_hi, k_lo, gre;
+  float alpha32[2], beta32[2];
+  double alpha[2], beta[2], gamma[2];
 };
 
 // Device-side plan of one tiled assembly (all arrays device pointers).
@@ -80,7 +99,11 @@ struct TilePlan {
 };
 
 size_t far_smem_bytes(int precision, int qt, int qb, const TilePlan& p);
-int launch_far_tiles(int precision, const FarConst& k, const TilePlan& p, cudaStream_t st);
+// Persistent batched launch over a work queue of (problem, bm, bn) items (device arrays).
+int launch_far_persistent(int precision, int op_kind, int generic, const FarConst* Ks, const TilePlan* plans,
+                          const int4* items, int nitems, int* counter, size_t smem_bytes, int ctas,
+                          const volatile int* abort_flag, cudaStream_t st);
+int far_persistent_occupancy(int precision, int op_kind, int generic, size_t smem_bytes, int* per_sm);
 void launch_prepare_rec(int precision, int side, int q, const Geo64* g, int nt, const RuleTable& rules, int rule,
                         double wscale, void* out, cudaStream_t st);
 int far_generic_q(int qt, int qb);  // 1 when the (qt, qb) pair uses the generic instance

@@ -569,6 +569,103 @@ __global__ void __launch_bounds__(256) k_local_diag64(OpParams op, const __grid_
 }
 
 // ----------------------------------------------------------------------------------------
+// Batched variants: the triangles of all problems are concatenated; tri_problem[t] names the
+// problem of test triangle t, prob_trial[p] its trial-triangle range and prob_k2[p] its k^2.
+// Pairs never cross problems.
+// ----------------------------------------------------------------------------------------
+__global__ void k_prepare_bounds_batched(const Geo64* __restrict__ g, int nt, const int* __restrict__ tri_problem,
+                                         const double* __restrict__ prob_k2, int trial_side, float4* __restrict__ out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nt) return;
+  const Geo64& T = g[t];
+  const double k2 = prob_k2[tri_problem[t]];
+  double c[3], r = 0.0;
+  for (int k = 0; k < 3; ++k) c[k] = (T.v[0][k] + T.v[1][k] + T.v[2][k]) / 3.0;
+  for (int a = 0; a < 3; ++a) {
+    const double d0 = T.v[a][0] - c[0], d1 = T.v[a][1] - c[1], d2 = T.v[a][2] - c[2];
+    r = fmax(r, sqrt(d0 * d0 + d1 * d1 + d2 * d2));
+  }
+  const double cn = sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+  if (trial_side) {
+    double lim = 0.64 * T.area;
+    if (k2 > 0.0) lim = fmin(lim, 0.04 / k2);
+    r += sqrt(lim);
+  }
+  r = r * (1.0 + 1e-6) + 4e-7 * (cn + 1.0) + 1e-30;
+  out[t] = make_float4((float)c[0], (float)c[1], (float)c[2], (float)r);
+}
+
+template <bool FILL>
+__global__ void __launch_bounds__(256) k_classify_batched(const float4* __restrict__ tb, const float4* __restrict__ bb,
+                                                          const Geo64* __restrict__ tg, const Geo64* __restrict__ bg,
+                                                          int nt, const int* __restrict__ tri_problem,
+                                                          const int2* __restrict__ prob_trial,
+                                                          const double* __restrict__ prob_k2, int* __restrict__ count,
+                                                          const int64_t* __restrict__ offset, int* __restrict__ out_tau,
+                                                          int* __restrict__ out_sigma, int8_t* __restrict__ out_cls,
+                                                          int* __restrict__ err) {
+  const int lane = threadIdx.x & 31;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  for (int tau = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; tau < nt; tau += warps) {
+    const float4 a = tb[tau];
+    const int pr = tri_problem[tau];
+    const int2 rg = prob_trial[pr];
+    const double k2 = prob_k2[pr];
+    int64_t base = FILL ? offset[tau] : 0;
+    int n = 0;
+    for (int s0 = rg.x; s0 < rg.y; s0 += 32) {
+      const int s = s0 + lane;
+      int cls = 0;
+      if (s < rg.y && sphere_candidate(a, bb[s])) {
+        cls = classify_exact(tg[tau], bg[s], k2);
+        if (cls < 0) {
+          atomicOr(err, 1);
+          cls = 0;
+        }
+      }
+      const unsigned bal = __ballot_sync(0xffffffffu, cls != 0);
+      if (FILL && cls != 0) {
+        const int64_t pos = base + n + __popc(bal & ((1u << lane) - 1u));
+        out_tau[pos] = tau;
+        out_sigma[pos] = s;
+        out_cls[pos] = (int8_t)cls;
+      }
+      n += __popc(bal);
+    }
+    if (!FILL && lane == 0) count[tau] = n;
+  }
+}
+
+template <int OP>
+__global__ void __launch_bounds__(256) k_singular_batched(const OpParams* __restrict__ ops,
+                                                          const __grid_constant__ QuadSel qs,
+                                                          const __grid_constant__ RuleTable rules,
+                                                          const Geo64* __restrict__ tg, const Geo64* __restrict__ bg,
+                                                          const int* __restrict__ tri_problem,
+                                                          const int* __restrict__ ent_tau,
+                                                          const int* __restrict__ ent_sigma,
+                                                          const int8_t* __restrict__ ent_cls, int64_t n,
+                                                          double2* __restrict__ out, const volatile int* abort_flag) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < n; e += warps) {
+    if (abort_flag && *abort_flag) return;
+    const int tau = ent_tau[e];
+    const OpParams op = ops[tri_problem[tau]];
+    const Geo64 A = tg[tau], B = bg[ent_sigma[e]];
+    double2 L[3][3];
+    pair_integral64<OP>(op, qs, rules, ent_cls[e], A, B, L);
+    if (lane < 9) {
+      double2 v = L[0][0];
+#pragma unroll
+      for (int q = 1; q < 9; ++q)
+        if (lane == q) v = L[q / 3][q % 3];
+      out[e * 9 + lane] = v;
+    }
+  }
+}
+
+// ----------------------------------------------------------------------------------------
 // Host launchers
 // ----------------------------------------------------------------------------------------
 void launch_prepare_geo64(const double* verts, const int32_t* tris, int nt, Geo64* out, cudaStream_t st) {
@@ -628,6 +725,39 @@ void launch_local_diag64(const OpParams& op, const QuadSel& qs, const RuleTable&
     k_local_diag64<BGB_OP_MAXWELL3D_SL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, tau, sigma, n, force, out, cls, err);
   else
     k_local_diag64<BGB_OP_MAXWELL3D_DL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, tau, sigma, n, force, out, cls, err);
+}
+
+void launch_prepare_bounds_batched(const Geo64* g, int nt, const int* tri_problem, const double* prob_k2, int trial_side,
+                                   float4* out, cudaStream_t st) {
+  if (nt > 0) k_prepare_bounds_batched<<<(nt + 255) / 256, 256, 0, st>>>(g, nt, tri_problem, prob_k2, trial_side, out);
+}
+void launch_classify_batched(bool fill, const float4* tb, const float4* bb, const Geo64* tg, const Geo64* bg, int nt,
+                             const int* tri_problem, const int2* prob_trial, const double* prob_k2, int* count,
+                             const int64_t* offset, int* out_tau, int* out_sigma, int8_t* out_cls, int* err,
+                             int num_sms, cudaStream_t st) {
+  if (nt <= 0) return;
+  int blocks = (nt + 7) / 8;
+  blocks = blocks < num_sms * 16 ? blocks : num_sms * 16;
+  if (fill)
+    k_classify_batched<true><<<blocks, 256, 0, st>>>(tb, bb, tg, bg, nt, tri_problem, prob_trial, prob_k2, count, offset,
+                                                     out_tau, out_sigma, out_cls, err);
+  else
+    k_classify_batched<false><<<blocks, 256, 0, st>>>(tb, bb, tg, bg, nt, tri_problem, prob_trial, prob_k2, count,
+                                                      offset, out_tau, out_sigma, out_cls, err);
+}
+void launch_singular_batched(int op_kind, const OpParams* ops, const QuadSel& qs, const RuleTable& rules,
+                             const Geo64* tg, const Geo64* bg, const int* tri_problem, const int* et, const int* es,
+                             const int8_t* ec, int64_t n, double2* out, const volatile int* abort_flag, int num_sms,
+                             cudaStream_t st) {
+  if (n <= 0) return;
+  int64_t blocks = (n + 7) / 8;
+  if (blocks > (int64_t)num_sms * 32) blocks = (int64_t)num_sms * 32;
+  if (op_kind == BGB_OP_HELMHOLTZ3D_SL)
+    k_singular_batched<BGB_OP_HELMHOLTZ3D_SL><<<(int)blocks, 256, 0, st>>>(ops, qs, rules, tg, bg, tri_problem, et, es, ec, n, out, abort_flag);
+  else if (op_kind == BGB_OP_MAXWELL3D_SL)
+    k_singular_batched<BGB_OP_MAXWELL3D_SL><<<(int)blocks, 256, 0, st>>>(ops, qs, rules, tg, bg, tri_problem, et, es, ec, n, out, abort_flag);
+  else
+    k_singular_batched<BGB_OP_MAXWELL3D_DL><<<(int)blocks, 256, 0, st>>>(ops, qs, rules, tg, bg, tri_problem, et, es, ec, n, out, abort_flag);
 }
 
 }  // namespace bgb

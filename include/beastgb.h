@@ -140,11 +140,28 @@ typedef struct {
   int64_t ld;
 } bgb_problem;
 
-/* Assemble n independent problems (uneven sizes and wavenumbers) with one persistent launch
- * per kernel stage over a shared work queue.  No reference counterpart: the reference
+/* Assemble n independent problems (uneven sizes and wave numbers) in one go: one launch
+ * classifies all pairs, one integrates all singular / near pairs, and ONE persistent
+ * far-pair launch pulls (problem, row block, column block) tiles from a work queue.  All
+ * problems share the operator kind, the spaces' kind and the quadrature strategy; each has
+ * its own operator parameters, mesh and output (ld >= rows).  Results are bit-identical to
+ * assembling each problem with bgb_assemble.  No reference counterpart: the reference
  * assembles one operator per call (assamble_gpu.jl:25). */
 int bgb_assemble_batch(bgb_handle* h, int32_t n, const bgb_problem* problems, int32_t precision,
                        int32_t out_kind, void* stream, bgb_stats* stats);
+
+/* Plan / execute form of the batch: bgb_batch_create does the planning, runs every stage
+ * once (the batch is assembled on return), optionally autotunes the tile shape and the
+ * work-queue schedule (flags & 1: every fitting candidate is timed on this batch), and
+ * captures the whole device sequence in a CUDA graph; bgb_batch_run replays that graph
+ * (re-assembling the same problems into the same outputs) and copies host outputs.
+ * stats->tile_config / row_blocks report the chosen tile shape / schedule (0 problem-major,
+ * 1 largest tiles first); stats->ms_total of bgb_batch_run is the graph's device time. */
+typedef struct bgb_batch bgb_batch;
+int bgb_batch_create(bgb_handle* h, int32_t n, const bgb_problem* problems, int32_t precision,
+                     int32_t out_kind, int32_t flags, bgb_batch** out, bgb_stats* stats);
+int bgb_batch_run(bgb_batch* batch, void* stream, bgb_stats* stats);
+int bgb_batch_destroy(bgb_batch* batch);
 
 /* Pair classes of a block of triangle pairs on the device, out[(t - t0) * (s1 - s0) + (s - s0)]
  * (host int8 buffer).  Replaces: determine_quadrule_types / quadrule_determine_type

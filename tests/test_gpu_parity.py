@@ -183,3 +183,25 @@ def test_invalid_inputs_fail_cleanly_and_handle_survives(c1):
     # the handle still works
     z = bg.assemble_gpu(op, X, X, bg.GPUConfiguration(precision="mixed"))
     assert np.isfinite(z).all()
+
+
+def test_batch_bit_identical_to_single_assemblies(qs):
+    """Uneven batch (ellipsoids of levels 1-2, different k): one persistent far launch over a work
+    queue equals assembling each problem alone, for both precisions; the graph replay too."""
+    import torch
+    probs = []
+    for m, k in bg.ellipsoid_batch(6, seed=3, levels=(1, 2)):
+        X = bg.raviartthomas(m)
+        probs.append((bg.Maxwell3D.singlelayer(wavenumber=k), X, X))
+    for prec in ("mixed", "fp64"):
+        b = bg.Batch(probs, bg.GPUConfiguration(precision=prec), out="device", autotune=True)
+        first = [o.clone() for o in b.outputs]
+        b.run()
+        for (op, X, Y), o, f in zip(probs, b.outputs, first):
+            z = bg.assemble_gpu(op, X, Y, bg.GPUConfiguration(precision=prec), out="device")
+            assert torch.equal(z, o) and torch.equal(z, f)
+        b.close()
+    # host outputs of a one-shot batch, against the oracle
+    outs = bg.assemble_batch(probs[:2], bg.GPUConfiguration(precision="fp64"), out="host")
+    for (op, X, Y), z in zip(probs[:2], outs):
+        assert rel(z, oracle.assemble(op, X, Y, qs)) < FP64_TOL
