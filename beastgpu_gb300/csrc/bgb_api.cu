@@ -443,6 +443,23 @@ bool same_space(const bgb_space* a, const bgb_space* b) {
   return a == b || (a->vertices == b->vertices && a->triangles == b->triangles && a->nv == b->nv && a->nt == b->nt);
 }
 
+double max_edge(const bgb_space* s) {
+  double m = 0.0;
+  for (int64_t t = 0; t < s->nt; ++t)
+    for (int a = 0; a < 3; ++a) {
+      const double* p = s->vertices + 3 * (int64_t)s->triangles[3 * t + a];
+      const double* q = s->vertices + 3 * (int64_t)s->triangles[3 * t + (a + 1) % 3];
+      const double d = std::sqrt((p[0] - q[0]) * (p[0] - q[0]) + (p[1] - q[1]) * (p[1] - q[1]) + (p[2] - q[2]) * (p[2] - q[2]));
+      m = std::max(m, d);
+    }
+  return m;
+}
+
+bool df_singular_ok(const OpParams& op, double edge_t, double edge_b) {
+  // singular / near pairs have R <= (edge_t + edge_b) * 2 at most; df_sincos covers |k R| < 400
+  return op.gamma[0] == 0.0 && std::fabs(op.gamma[1]) * 2.0 * (edge_t + edge_b) < 350.0;
+}
+
 static int check_abort(bgb_handle* h) {
   if (h->abort_host && *h->abort_host) {
     set_error("aborted by bgb_abort");
@@ -554,7 +571,7 @@ int bgb_destroy(bgb_handle* h) {
   if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
   DevBuf* bufs[] = {&h->verts_t, &h->tris_t, &h->verts_b, &h->tris_b, &h->geo_t, &h->geo_b, &h->bnd_t, &h->bnd_b,
                     &h->rec_t, &h->rec_b, &h->cls_count, &h->cls_off, &h->ent_tau, &h->ent_sigma, &h->ent_cls,
-                    &h->sing_L, &h->err, &h->plan_i, &h->plan_l, &h->plan_d, &h->plan_f, &h->far_items, &h->far_const, &h->stage[0], &h->stage[1],
+                    &h->sing_L, &h->err, &h->plan_i, &h->plan_l, &h->plan_d, &h->plan_f, &h->far_items, &h->far_const, &h->df_tab, &h->stage[0], &h->stage[1],
                     &h->diag_a, &h->diag_b, &h->diag_c, &h->diag_d};
   for (DevBuf* b : bufs) b->release();
   for (int i = 0; i < 8; ++i)
@@ -646,6 +663,17 @@ int bgb_local_matrices(bgb_handle* h, const bgb_operator* op, const bgb_space* t
   launch_local_diag64(opp, qsel, R, test->refspace, trial->refspace, h->geo_t.as<Geo64>(), h->geo_b.as<Geo64>(),
                       h->diag_a.as<int>(), h->diag_b.as<int>(), npairs, force_class, h->diag_c.as<double2>(), dcls,
                       h->err.as<int>(), h->num_sms, h->stream);
+  // mixed: singular / near pairs through the double-float kernel (far pairs are replaced below)
+  std::vector<float> dftab;
+  if (precision == BGB_PREC_MIXED && df_singular_ok(opp, max_edge(test), max_edge(trial))) {
+    DfTables M;
+    build_df_tables(qsel, R, dftab, M);
+    if ((rc = h->df_tab.ensure(sizeof(float) * dftab.size()))) return rc;
+    BGB_CUDA(cudaMemcpyAsync(h->df_tab.p, dftab.data(), sizeof(float) * dftab.size(), cudaMemcpyHostToDevice, h->stream));
+    launch_singular_df(opp.kind, opp, nullptr, nullptr, M, h->df_tab.as<float>(), h->geo_t.as<Geo64>(),
+                       h->geo_b.as<Geo64>(), h->diag_a.as<int>(), h->diag_b.as<int>(), dcls, npairs,
+                       h->diag_c.as<double2>(), nullptr, h->num_sms, h->stream);
+  }
   // far pairs through the far-kernel pair code of the requested precision
   FarConst K = make_farconst(opp, R, qsel);
   const int gen = far_generic_q(K.qt, K.qb);
@@ -730,10 +758,23 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
   if ((rc = classify_all(h, test, trial, gt, gb, opp.k2, &nsing))) return rc;
   launches += 6;  // 2 bounds, 2 classify passes, scan (+1 singular below)
   cudaEventRecord(h->ev[1], h->stream);
-  // 2. singular / near pairs (FP64)
+  // 2. singular / near pairs: FP64 kernel (plain path), double-float kernel (mixed path)
   if ((rc = h->sing_L.ensure(sizeof(double2) * 9 * std::max<int64_t>(1, nsing)))) return rc;
-  launch_singular(opp, qsel, R, test->refspace, trial->refspace, gt, gb, h->ent_tau.as<int>(), h->ent_sigma.as<int>(),
-                  h->ent_cls.as<int8_t>(), nsing, h->sing_L.as<double2>(), h->abort_dev, h->num_sms, h->stream);
+  const bool use_df = precision == BGB_PREC_MIXED && df_singular_ok(opp, max_edge(test), same ? max_edge(test) : max_edge(trial));
+  if (use_df) {
+    std::vector<float> tab;
+    DfTables M;
+    build_df_tables(qsel, R, tab, M);
+    if ((rc = h->df_tab.ensure(sizeof(float) * tab.size()))) return rc;
+    BGB_CUDA(cudaMemcpyAsync(h->df_tab.p, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice, h->stream));
+    launch_singular_df(opp.kind, opp, nullptr, nullptr, M, h->df_tab.as<float>(), gt, gb, h->ent_tau.as<int>(),
+                       h->ent_sigma.as<int>(), h->ent_cls.as<int8_t>(), nsing, h->sing_L.as<double2>(), h->abort_dev,
+                       h->num_sms, h->stream);
+    BGB_CUDA(cudaStreamSynchronize(h->stream));  // the host table buffer goes out of scope
+  } else {
+    launch_singular(opp, qsel, R, test->refspace, trial->refspace, gt, gb, h->ent_tau.as<int>(), h->ent_sigma.as<int>(),
+                    h->ent_cls.as<int8_t>(), nsing, h->sing_L.as<double2>(), h->abort_dev, h->num_sms, h->stream);
+  }
   BGB_CUDA(cudaGetLastError());
   cudaEventRecord(h->ev[2], h->stream);
   if ((rc = check_abort(h))) return rc;

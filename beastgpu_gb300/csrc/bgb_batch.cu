@@ -25,7 +25,9 @@ struct bgb_batch {
   bgb::DevBuf verts_t, tris_t, verts_b, tris_b, geo_t, geo_b, bnd_t, bnd_b, rec_t, rec_b;
   bgb::DevBuf tri_problem, prob_trial, prob_k2, ops, Ks, plans, items, counter;
   bgb::DevBuf cls_count, cls_off, ent_tau, ent_sigma, ent_cls, sing_L, err;
-  bgb::DevBuf plan_i, plan_l, plan_d, plan_f, stage;
+  bgb::DevBuf plan_i, plan_l, plan_d, plan_f, stage, df_tab;
+  bool use_df = false;
+  bgb::DfTables dfm{};
   int nt_t = 0, nt_b = 0, nv_t = 0, nv_b = 0, nitems = 0;
   bool shared_trial = false;
   int64_t nsing = 0;
@@ -46,7 +48,7 @@ struct bgb_batch {
     bgb::DevBuf* bufs[] = {&verts_t, &verts_b, &tris_t, &tris_b, &geo_t, &geo_b, &bnd_t, &bnd_b, &rec_t, &rec_b,
                            &tri_problem, &prob_trial, &prob_k2, &ops, &Ks, &plans, &items, &counter, &cls_count,
                            &cls_off, &ent_tau, &ent_sigma, &ent_cls, &sing_L, &err, &plan_i, &plan_l, &plan_d,
-                           &plan_f, &stage};
+                           &plan_f, &stage, &df_tab};
     for (auto* b : bufs) b->release();
   }
 };
@@ -92,9 +94,14 @@ int enqueue_device_work(bgb_batch* B, cudaStream_t st, bool far_only) {
                             B->prob_trial.as<int2>(), B->prob_k2.as<double>(), B->cls_count.as<int>(),
                             B->cls_off.as<int64_t>(), B->ent_tau.as<int>(), B->ent_sigma.as<int>(),
                             B->ent_cls.as<int8_t>(), B->err.as<int>(), h->num_sms, st);
-    launch_singular_batched(B->op_kind, B->ops.as<OpParams>(), B->qsel, B->rules, gt, gb, tp_t, B->ent_tau.as<int>(),
-                            B->ent_sigma.as<int>(), B->ent_cls.as<int8_t>(), B->nsing, B->sing_L.as<double2>(),
-                            h->abort_dev, h->num_sms, st);
+    if (B->use_df)
+      launch_singular_df(B->op_kind, OpParams{}, B->ops.as<OpParams>(), tp_t, B->dfm, B->df_tab.as<float>(), gt, gb,
+                         B->ent_tau.as<int>(), B->ent_sigma.as<int>(), B->ent_cls.as<int8_t>(), B->nsing,
+                         B->sing_L.as<double2>(), h->abort_dev, h->num_sms, st);
+    else
+      launch_singular_batched(B->op_kind, B->ops.as<OpParams>(), B->qsel, B->rules, gt, gb, tp_t, B->ent_tau.as<int>(),
+                              B->ent_sigma.as<int>(), B->ent_cls.as<int8_t>(), B->nsing, B->sing_L.as<double2>(),
+                              h->abort_dev, h->num_sms, st);
     const int qt = B->rules.npoints[B->qsel.far_t], qb = B->rules.npoints[B->qsel.far_b];
     launch_prepare_rec(B->precision, 0, B->generic ? BGB_MAXQ : qt, gt, B->nt_t, B->rules, B->qsel.far_t, 1.0,
                        B->rec_t.p, st);
@@ -307,6 +314,17 @@ int bgb_batch_create(bgb_handle* h, int32_t n, const bgb_problem* problems, int3
     }
     prob_trial[p] = make_int2(bbase[p], bbase[p] + q.trial.nt);
     pairs_total += (int64_t)q.test.nt * q.trial.nt;
+  }
+  if (precision == BGB_PREC_MIXED) {
+    B->use_df = true;
+    for (int p = 0; p < n; ++p)
+      B->use_df &= df_singular_ok(ops[p], max_edge(&problems[p].test), max_edge(&problems[p].trial));
+    if (B->use_df) {
+      std::vector<float> tab;
+      build_df_tables(B->qsel, B->rules, tab, B->dfm);
+      if ((rc = put(st, B->df_tab, tab))) return fail(rc);
+      BGB_CUDA(cudaStreamSynchronize(st));
+    }
   }
   B->nt_t = (int)(tt.size() / 3);
   B->nv_t = (int)(vt.size() / 3);

@@ -51,7 +51,7 @@ struct bgb_handle {
   // buffers
   bgb::DevBuf verts_t, tris_t, verts_b, tris_b, geo_t, geo_b, bnd_t, bnd_b, rec_t, rec_b;
   bgb::DevBuf cls_count, cls_off, ent_tau, ent_sigma, ent_cls, sing_L, err;
-  bgb::DevBuf plan_i, plan_l, plan_d, plan_f, far_items, far_const;
+  bgb::DevBuf plan_i, plan_l, plan_d, plan_f, far_items, far_const, df_tab;
   bgb::DevBuf stage[2];
   bgb::DevBuf diag_a, diag_b, diag_c, diag_d;
   cudaEvent_t ev[8] = {};
@@ -96,6 +96,11 @@ std::vector<int> order_functions(const Supports& S, const std::vector<int>& rank
 void plan_test_side(const Supports& S, const std::vector<int>& order, int FM, int64_t row0, HostPlan& P);
 void plan_trial_side(const Supports& S, const std::vector<int>& order, int FN, int SC, HostPlan& P);
 bool same_space(const bgb_space* a, const bgb_space* b);
+// Largest triangle edge of a space (host), for the argument range of the double-float sincos.
+double max_edge(const bgb_space* s);
+// True when the mixed path may integrate singular / near pairs in double-float: no lossy
+// wave number and k R below the range of the df sin / cos.
+bool df_singular_ok(const OpParams& op, double edge_t, double edge_b);
 double event_ms(cudaEvent_t a, cudaEvent_t b);
 
 }  // namespace bgb

@@ -2,6 +2,9 @@
 #pragma once
 
 #include "bgb_common.cuh"
+#include "bgb_df.cuh"
+
+#include <vector>
 
 namespace bgb {
 
@@ -31,6 +34,23 @@ void launch_singular_batched(int op_kind, const OpParams* ops, const QuadSel& qs
                              const Geo64* tg, const Geo64* bg, const int* tri_problem, const int* et, const int* es,
                              const int8_t* ec, int64_t n, double2* out, const volatile int* abort_flag, int num_sms,
                              cudaStream_t st);
+
+// ---- bgb_singular_df.cu ----------------------------------------------------------------
+// Host-built tables of the double-float singular kernel (one float buffer): Sauter-Schwab
+// region points (u1, u2, v1, v2, weight as df) per class, near-rule points (u, v, w as df) and
+// the sin / cos table.
+struct DfTables {
+  int ss_off[4], ss_cnt[4];
+  int near_t_off, near_b_off, near_qt, near_qb;
+  int trig_off, total_floats;
+  DfTrig trig;
+};
+void build_df_tables(const QuadSel& qs, const RuleTable& R, std::vector<float>& buf, DfTables& M);
+// ops / tri_problem non-NULL: batched (operator of the test triangle's problem).
+void launch_singular_df(int op_kind, const OpParams& op, const OpParams* ops, const int* tri_problem,
+                        const DfTables& M, const float* dtab, const Geo64* tg, const Geo64* bg, const int* et,
+                        const int* es, const int8_t* ec, int64_t n, double2* out, const volatile int* abort_flag,
+                        int num_sms, cudaStream_t st);
 
 // ---- bgb_far.cu ------------------------------------------------------------------------
 // Constants of the far-pair kernels (passed by value).

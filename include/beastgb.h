@@ -170,8 +170,10 @@ int bgb_classify_block(bgb_handle* h, const bgb_space* test, const bgb_space* tr
                        int32_t t0, int32_t t1, int32_t s0, int32_t s1, int8_t* out);
 
 /* Local 3x3 complex matrices of a list of triangle pairs (out: double[npairs][9][2], host),
- * with the rule chosen by classification or forced (force_class >= 0).  Singular and near
- * pairs always use the FP64 kernels; far pairs use the far kernel's pair code of `precision`.
+ * with the rule chosen by classification or forced (force_class >= 0), computed by the
+ * kernels bgb_assemble uses for `precision`: singular and near pairs by the FP64 kernel
+ * (BGB_PREC_FP64) or the double-float kernel (BGB_PREC_MIXED), far pairs by the far
+ * kernel's pair code.
  * Replaces the per-pair integrals of sauterschwab_parameterized_gpu_outside_loop_kernel!
  * (SauterSchwab.jl:212-262) and doubleQuadRuleMainCaseKernel! (doubleQuadRuleMainCase.jl:60-105)
  * before their scatter. */
