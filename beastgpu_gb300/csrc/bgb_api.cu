@@ -496,9 +496,10 @@ static int classify_all(bgb_handle* h, const bgb_space* test, const bgb_space* t
   if ((rc = h->ent_tau.ensure(sizeof(int) * (size_t)std::max<int64_t>(1, tot)))) return rc;
   if ((rc = h->ent_sigma.ensure(sizeof(int) * (size_t)std::max<int64_t>(1, tot)))) return rc;
   if ((rc = h->ent_cls.ensure((size_t)std::max<int64_t>(1, tot)))) return rc;
+  if ((rc = h->ent_mask.ensure(sizeof(int16_t) * (size_t)std::max<int64_t>(1, tot)))) return rc;
   launch_classify(true, h->bnd_t.as<float4>(), h->bnd_b.as<float4>(), gt, gb, nt, nb, k2, h->cls_count.as<int>(),
                   h->cls_off.as<int64_t>(), h->ent_tau.as<int>(), h->ent_sigma.as<int>(), h->ent_cls.as<int8_t>(),
-                  h->err.as<int>(), h->num_sms, h->stream);
+                  h->err.as<int>(), h->num_sms, h->stream, h->ent_mask.as<int16_t>());
   BGB_CUDA(cudaGetLastError());
   *total = tot;
   return 0;
@@ -570,7 +571,7 @@ int bgb_destroy(bgb_handle* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
   DevBuf* bufs[] = {&h->verts_t, &h->tris_t, &h->verts_b, &h->tris_b, &h->geo_t, &h->geo_b, &h->bnd_t, &h->bnd_b,
-                    &h->rec_t, &h->rec_b, &h->cls_count, &h->cls_off, &h->ent_tau, &h->ent_sigma, &h->ent_cls,
+                    &h->rec_t, &h->rec_b, &h->cls_count, &h->cls_off, &h->ent_tau, &h->ent_sigma, &h->ent_cls, &h->ent_mask, &h->geodf_t, &h->geodf_b,
                     &h->sing_L, &h->err, &h->plan_i, &h->plan_l, &h->plan_d, &h->plan_f, &h->far_items, &h->far_const, &h->df_tab, &h->stage[0], &h->stage[1],
                     &h->diag_a, &h->diag_b, &h->diag_c, &h->diag_d};
   for (DevBuf* b : bufs) b->release();
@@ -654,7 +655,7 @@ int bgb_local_matrices(bgb_handle* h, const bgb_operator* op, const bgb_space* t
   RuleTable R = make_rules();
   if ((rc = h->diag_a.ensure(sizeof(int) * npairs)) || (rc = h->diag_b.ensure(sizeof(int) * npairs)) ||
       (rc = h->diag_c.ensure(sizeof(double2) * 9 * npairs)) || (rc = h->diag_d.ensure(sizeof(double2) * 9 * npairs + npairs)) ||
-      (rc = h->err.ensure(sizeof(int) * 4)))
+      (rc = h->ent_mask.ensure(sizeof(int16_t) * npairs)) || (rc = h->err.ensure(sizeof(int) * 4)))
     return rc;
   BGB_CUDA(cudaMemcpyAsync(h->diag_a.p, tau, sizeof(int) * npairs, cudaMemcpyHostToDevice, h->stream));
   BGB_CUDA(cudaMemcpyAsync(h->diag_b.p, sigma, sizeof(int) * npairs, cudaMemcpyHostToDevice, h->stream));
@@ -662,7 +663,7 @@ int bgb_local_matrices(bgb_handle* h, const bgb_operator* op, const bgb_space* t
   int8_t* dcls = (int8_t*)((char*)h->diag_d.p + sizeof(double2) * 9 * npairs);
   launch_local_diag64(opp, qsel, R, test->refspace, trial->refspace, h->geo_t.as<Geo64>(), h->geo_b.as<Geo64>(),
                       h->diag_a.as<int>(), h->diag_b.as<int>(), npairs, force_class, h->diag_c.as<double2>(), dcls,
-                      h->err.as<int>(), h->num_sms, h->stream);
+                      h->err.as<int>(), h->num_sms, h->stream, h->ent_mask.as<int16_t>());
   // mixed: singular / near pairs through the double-float kernel (far pairs are replaced below)
   std::vector<float> dftab;
   if (precision == BGB_PREC_MIXED && df_singular_ok(opp, max_edge(test), max_edge(trial))) {
@@ -670,9 +671,14 @@ int bgb_local_matrices(bgb_handle* h, const bgb_operator* op, const bgb_space* t
     build_df_tables(qsel, R, dftab, M);
     if ((rc = h->df_tab.ensure(sizeof(float) * dftab.size()))) return rc;
     BGB_CUDA(cudaMemcpyAsync(h->df_tab.p, dftab.data(), sizeof(float) * dftab.size(), cudaMemcpyHostToDevice, h->stream));
-    launch_singular_df(opp.kind, opp, nullptr, nullptr, M, h->df_tab.as<float>(), h->geo_t.as<Geo64>(),
-                       h->geo_b.as<Geo64>(), h->diag_a.as<int>(), h->diag_b.as<int>(), dcls, npairs,
-                       h->diag_c.as<double2>(), nullptr, h->num_sms, h->stream);
+    if ((rc = h->geodf_t.ensure(sizeof(GeoDf) * std::max(1, test->nt))) ||
+        (rc = h->geodf_b.ensure(sizeof(GeoDf) * std::max(1, trial->nt))))
+      return rc;
+    launch_prepare_geodf(h->geo_t.as<Geo64>(), test->nt, h->geodf_t.as<GeoDf>(), h->stream);
+    launch_prepare_geodf(h->geo_b.as<Geo64>(), trial->nt, h->geodf_b.as<GeoDf>(), h->stream);
+    launch_singular_df(opp.kind, make_opdf(opp), nullptr, nullptr, M, h->df_tab.as<float>(), h->geodf_t.as<GeoDf>(),
+                       h->geodf_b.as<GeoDf>(), h->diag_a.as<int>(), h->diag_b.as<int>(), dcls,
+                       h->ent_mask.as<int16_t>(), npairs, h->diag_c.as<double2>(), nullptr, h->num_sms, h->stream);
   }
   // far pairs through the far-kernel pair code of the requested precision
   FarConst K = make_farconst(opp, R, qsel);
@@ -767,9 +773,17 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
     build_df_tables(qsel, R, tab, M);
     if ((rc = h->df_tab.ensure(sizeof(float) * tab.size()))) return rc;
     BGB_CUDA(cudaMemcpyAsync(h->df_tab.p, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice, h->stream));
-    launch_singular_df(opp.kind, opp, nullptr, nullptr, M, h->df_tab.as<float>(), gt, gb, h->ent_tau.as<int>(),
-                       h->ent_sigma.as<int>(), h->ent_cls.as<int8_t>(), nsing, h->sing_L.as<double2>(), h->abort_dev,
-                       h->num_sms, h->stream);
+    if ((rc = h->geodf_t.ensure(sizeof(GeoDf) * std::max(1, test->nt))) ||
+        (!same && (rc = h->geodf_b.ensure(sizeof(GeoDf) * std::max(1, trial->nt)))))
+      return rc;
+    launch_prepare_geodf(gt, test->nt, h->geodf_t.as<GeoDf>(), h->stream);
+    if (!same) launch_prepare_geodf(gb, trial->nt, h->geodf_b.as<GeoDf>(), h->stream);
+    const GeoDf* dgt = h->geodf_t.as<GeoDf>();
+    const GeoDf* dgb = same ? dgt : h->geodf_b.as<GeoDf>();
+    launch_singular_df(opp.kind, make_opdf(opp), nullptr, nullptr, M, h->df_tab.as<float>(), dgt, dgb,
+                       h->ent_tau.as<int>(), h->ent_sigma.as<int>(), h->ent_cls.as<int8_t>(),
+                       h->ent_mask.as<int16_t>(), nsing, h->sing_L.as<double2>(), h->abort_dev, h->num_sms, h->stream);
+    launches += 1 + (same ? 0 : 1);
     BGB_CUDA(cudaStreamSynchronize(h->stream));  // the host table buffer goes out of scope
   } else {
     launch_singular(opp, qsel, R, test->refspace, trial->refspace, gt, gb, h->ent_tau.as<int>(), h->ent_sigma.as<int>(),

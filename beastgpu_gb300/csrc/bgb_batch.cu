@@ -24,7 +24,7 @@ struct bgb_batch {
   // device buffers
   bgb::DevBuf verts_t, tris_t, verts_b, tris_b, geo_t, geo_b, bnd_t, bnd_b, rec_t, rec_b;
   bgb::DevBuf tri_problem, prob_trial, prob_k2, ops, Ks, plans, items, counter;
-  bgb::DevBuf cls_count, cls_off, ent_tau, ent_sigma, ent_cls, sing_L, err;
+  bgb::DevBuf cls_count, cls_off, ent_tau, ent_sigma, ent_cls, ent_mask, sing_L, err, geodf_t, geodf_b, opdf;
   bgb::DevBuf plan_i, plan_l, plan_d, plan_f, stage, df_tab;
   bool use_df = false;
   bgb::DfTables dfm{};
@@ -47,7 +47,7 @@ struct bgb_batch {
       if (e) cudaEventDestroy(e);
     bgb::DevBuf* bufs[] = {&verts_t, &verts_b, &tris_t, &tris_b, &geo_t, &geo_b, &bnd_t, &bnd_b, &rec_t, &rec_b,
                            &tri_problem, &prob_trial, &prob_k2, &ops, &Ks, &plans, &items, &counter, &cls_count,
-                           &cls_off, &ent_tau, &ent_sigma, &ent_cls, &sing_L, &err, &plan_i, &plan_l, &plan_d,
+                           &cls_off, &ent_tau, &ent_sigma, &ent_cls, &ent_mask, &sing_L, &err, &geodf_t, &geodf_b, &opdf, &plan_i, &plan_l, &plan_d,
                            &plan_f, &stage, &df_tab};
     for (auto* b : bufs) b->release();
   }
@@ -93,12 +93,16 @@ int enqueue_device_work(bgb_batch* B, cudaStream_t st, bool far_only) {
     launch_classify_batched(true, B->bnd_t.as<float4>(), B->bnd_b.as<float4>(), gt, gb, B->nt_t, tp_t,
                             B->prob_trial.as<int2>(), B->prob_k2.as<double>(), B->cls_count.as<int>(),
                             B->cls_off.as<int64_t>(), B->ent_tau.as<int>(), B->ent_sigma.as<int>(),
-                            B->ent_cls.as<int8_t>(), B->err.as<int>(), h->num_sms, st);
-    if (B->use_df)
-      launch_singular_df(B->op_kind, OpParams{}, B->ops.as<OpParams>(), tp_t, B->dfm, B->df_tab.as<float>(), gt, gb,
-                         B->ent_tau.as<int>(), B->ent_sigma.as<int>(), B->ent_cls.as<int8_t>(), B->nsing,
-                         B->sing_L.as<double2>(), h->abort_dev, h->num_sms, st);
-    else
+                            B->ent_cls.as<int8_t>(), B->err.as<int>(), h->num_sms, st, B->ent_mask.as<int16_t>());
+    if (B->use_df) {
+      launch_prepare_geodf(gt, B->nt_t, B->geodf_t.as<GeoDf>(), st);
+      if (!B->shared_trial) launch_prepare_geodf(gb, B->nt_b, B->geodf_b.as<GeoDf>(), st);
+      const GeoDf* dgt = B->geodf_t.as<GeoDf>();
+      const GeoDf* dgb = B->shared_trial ? dgt : B->geodf_b.as<GeoDf>();
+      launch_singular_df(B->op_kind, OpDf{}, B->opdf.as<OpDf>(), tp_t, B->dfm, B->df_tab.as<float>(), dgt, dgb,
+                         B->ent_tau.as<int>(), B->ent_sigma.as<int>(), B->ent_cls.as<int8_t>(),
+                         B->ent_mask.as<int16_t>(), B->nsing, B->sing_L.as<double2>(), h->abort_dev, h->num_sms, st);
+    } else
       launch_singular_batched(B->op_kind, B->ops.as<OpParams>(), B->qsel, B->rules, gt, gb, tp_t, B->ent_tau.as<int>(),
                               B->ent_sigma.as<int>(), B->ent_cls.as<int8_t>(), B->nsing, B->sing_L.as<double2>(),
                               h->abort_dev, h->num_sms, st);
@@ -322,7 +326,9 @@ int bgb_batch_create(bgb_handle* h, int32_t n, const bgb_problem* problems, int3
     if (B->use_df) {
       std::vector<float> tab;
       build_df_tables(B->qsel, B->rules, tab, B->dfm);
-      if ((rc = put(st, B->df_tab, tab))) return fail(rc);
+      std::vector<OpDf> od(n);
+      for (int p = 0; p < n; ++p) od[p] = make_opdf(ops[p]);
+      if ((rc = put(st, B->df_tab, tab)) || (rc = put(st, B->opdf, od))) return fail(rc);
       BGB_CUDA(cudaStreamSynchronize(st));
     }
   }
@@ -381,6 +387,9 @@ int bgb_batch_create(bgb_handle* h, int32_t n, const bgb_problem* problems, int3
   if ((rc = B->ent_tau.ensure(sizeof(int) * std::max<int64_t>(1, tot))) ||
       (rc = B->ent_sigma.ensure(sizeof(int) * std::max<int64_t>(1, tot))) ||
       (rc = B->ent_cls.ensure(std::max<int64_t>(1, tot))) ||
+      (rc = B->ent_mask.ensure(sizeof(int16_t) * std::max<int64_t>(1, tot))) ||
+      (B->use_df && (rc = B->geodf_t.ensure(sizeof(GeoDf) * std::max(1, B->nt_t)))) ||
+      (B->use_df && !B->shared_trial && (rc = B->geodf_b.ensure(sizeof(GeoDf) * std::max(1, B->nt_b)))) ||
       (rc = B->sing_L.ensure(sizeof(double2) * 9 * std::max<int64_t>(1, tot))))
     return fail(rc);
   // outputs

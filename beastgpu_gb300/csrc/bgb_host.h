@@ -50,7 +50,7 @@ struct bgb_handle {
   std::mutex mu;
   // buffers
   bgb::DevBuf verts_t, tris_t, verts_b, tris_b, geo_t, geo_b, bnd_t, bnd_b, rec_t, rec_b;
-  bgb::DevBuf cls_count, cls_off, ent_tau, ent_sigma, ent_cls, sing_L, err;
+  bgb::DevBuf cls_count, cls_off, ent_tau, ent_sigma, ent_cls, ent_mask, sing_L, err, geodf_t, geodf_b;
   bgb::DevBuf plan_i, plan_l, plan_d, plan_f, far_items, far_const, df_tab;
   bgb::DevBuf stage[2];
   bgb::DevBuf diag_a, diag_b, diag_c, diag_d;

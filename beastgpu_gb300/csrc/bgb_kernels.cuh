@@ -13,7 +13,7 @@ void launch_prepare_geo64(const double* verts, const int32_t* tris, int nt, Geo6
 void launch_prepare_bounds(const Geo64* g, int nt, double k2, int trial_side, float4* out, cudaStream_t st);
 void launch_classify(bool fill, const float4* tb, const float4* bb, const Geo64* tg, const Geo64* bg, int nt, int nb,
                      double k2, int* count, const int64_t* offset, int* out_tau, int* out_sigma, int8_t* out_cls,
-                     int* err, int num_sms, cudaStream_t st);
+                     int* err, int num_sms, cudaStream_t st, int16_t* out_mask = nullptr);
 void launch_scan(const int* counts, int n, int64_t* offsets, cudaStream_t st);
 void launch_classify_dense(const Geo64* tg, const Geo64* bg, int t0, int t1, int s0, int s1, double k2, int8_t* out,
                            int* err, cudaStream_t st);
@@ -22,14 +22,14 @@ void launch_singular(const OpParams& op, const QuadSel& qs, const RuleTable& rul
                      const volatile int* abort_flag, int num_sms, cudaStream_t st);
 void launch_local_diag64(const OpParams& op, const QuadSel& qs, const RuleTable& rules, int rsA, int rsB,
                          const Geo64* tg, const Geo64* bg, const int* tau, const int* sigma, int64_t n, int force,
-                         double2* out, int8_t* cls, int* err, int num_sms, cudaStream_t st);
+                         double2* out, int8_t* cls, int* err, int num_sms, cudaStream_t st, int16_t* mask = nullptr);
 
 void launch_prepare_bounds_batched(const Geo64* g, int nt, const int* tri_problem, const double* prob_k2, int trial_side,
                                    float4* out, cudaStream_t st);
 void launch_classify_batched(bool fill, const float4* tb, const float4* bb, const Geo64* tg, const Geo64* bg, int nt,
                              const int* tri_problem, const int2* prob_trial, const double* prob_k2, int* count,
                              const int64_t* offset, int* out_tau, int* out_sigma, int8_t* out_cls, int* err,
-                             int num_sms, cudaStream_t st);
+                             int num_sms, cudaStream_t st, int16_t* out_mask = nullptr);
 void launch_singular_batched(int op_kind, const OpParams* ops, const QuadSel& qs, const RuleTable& rules,
                              const Geo64* tg, const Geo64* bg, const int* tri_problem, const int* et, const int* es,
                              const int8_t* ec, int64_t n, double2* out, const volatile int* abort_flag, int num_sms,
@@ -46,11 +46,23 @@ struct DfTables {
   DfTrig trig;
 };
 void build_df_tables(const QuadSel& qs, const RuleTable& R, std::vector<float>& buf, DfTables& M);
-// ops / tri_problem non-NULL: batched (operator of the test triangle's problem).
-void launch_singular_df(int op_kind, const OpParams& op, const OpParams* ops, const int* tri_problem,
-                        const DfTables& M, const float* dtab, const Geo64* tg, const Geo64* bg, const int* et,
-                        const int* es, const int8_t* ec, int64_t n, double2* out, const volatile int* abort_flag,
-                        int num_sms, cudaStream_t st);
+// Per-triangle double-float geometry: vertices (df), area and 1 / area (df).
+struct GeoDf {
+  float v[3][3][2];
+  float area[2], inv_area[2];
+};
+void launch_prepare_geodf(const Geo64* g, int nt, GeoDf* out, cudaStream_t st);
+// Operator constants as df: alpha, beta (complex), k = Im gamma.
+struct OpDf {
+  float alpha[2][2], beta[2][2], k[2];
+  int kind, oscill;
+};
+OpDf make_opdf(const OpParams& op);
+// opdf_array / tri_problem non-NULL: batched (constants of the test triangle's problem).
+void launch_singular_df(int op_kind, const OpDf& op, const OpDf* opdf_array, const int* tri_problem,
+                        const DfTables& M, const float* dtab, const GeoDf* tg, const GeoDf* bg, const int* et,
+                        const int* es, const int8_t* ec, const int16_t* emask, int64_t n, double2* out,
+                        const volatile int* abort_flag, int num_sms, cudaStream_t st);
 
 // ---- bgb_far.cu ------------------------------------------------------------------------
 // Constants of the far-pair kernels (passed by value).

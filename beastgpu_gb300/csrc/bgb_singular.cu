@@ -69,12 +69,14 @@ __global__ void k_prepare_bounds(const Geo64* __restrict__ g, int nt, double k2,
 
 // ----------------------------------------------------------------------------------------
 // Exact FP64 predicate (doubleQuadRuleMainCase.jl:324-339; codes quadrule_determine.jl:76).
-// Rounded like the Julia code: no contraction, IEEE sqrt and division.
+// Rounded like the Julia code: no contraction, IEEE sqrt and division.  *mask (optional)
+// receives the coincident vertex pairs, bit u1 * 3 + u2 (the same test as the reference's
+// vertex matching, pulledback_integrand_gpu.jl:41-51).
 // ----------------------------------------------------------------------------------------
-__device__ int classify_exact(const Geo64& a, const Geo64& b, double k2) {
+__device__ int classify_exact(const Geo64& a, const Geo64& b, double k2, int* mask = nullptr) {
   const double dtol = 2.220446049250313e-16 * 1.0e3;
   const double xtol2 = 0.2 * 0.2;
-  int hits = 0;
+  int hits = 0, m = 0;
   double dmin2 = 1.7976931348623157e308;  // floatmax(Float64)
 #pragma unroll
   for (int u1 = 0; u1 < 3; ++u1)
@@ -84,13 +86,16 @@ __device__ int classify_exact(const Geo64& a, const Geo64& b, double k2) {
       double dy = __dsub_rn(a.v[u1][1], b.v[u2][1]);
       double dz = __dsub_rn(a.v[u1][2], b.v[u2][2]);
       double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-      hits += (__dsqrt_rn(d2) < dtol);
+      const bool hit = __dsqrt_rn(d2) < dtol;
+      hits += hit;
+      m |= (int)hit << (u1 * 3 + u2);
       dmin2 = fmin(dmin2, d2);
     }
+  if (mask) *mask = m;
   if (hits > 3) return -1;
   if (hits > 0) return hits;
-  double m = fmax(__dmul_rn(dmin2, k2), __ddiv_rn(dmin2, __dmul_rn(16.0, b.area)));
-  return (m >= xtol2) ? BGB_CLASS_FAR : BGB_CLASS_NEAR;
+  const double mx = fmax(__dmul_rn(dmin2, k2), __ddiv_rn(dmin2, __dmul_rn(16.0, b.area)));
+  return (mx >= xtol2) ? BGB_CLASS_FAR : BGB_CLASS_NEAR;
 }
 
 template <bool FILL>
@@ -99,7 +104,7 @@ __global__ void __launch_bounds__(256) k_classify(const float4* __restrict__ tb,
                                                   int nt, int nb, double k2, int* __restrict__ count,
                                                   const int64_t* __restrict__ offset, int* __restrict__ out_tau,
                                                   int* __restrict__ out_sigma, int8_t* __restrict__ out_cls,
-                                                  int* __restrict__ err) {
+                                                  int16_t* __restrict__ out_mask, int* __restrict__ err) {
   const int lane = threadIdx.x & 31;
   const int warps = (gridDim.x * blockDim.x) >> 5;
   for (int tau = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; tau < nt; tau += warps) {
@@ -108,10 +113,10 @@ __global__ void __launch_bounds__(256) k_classify(const float4* __restrict__ tb,
     int n = 0;
     for (int s0 = 0; s0 < nb; s0 += 32) {
       int s = s0 + lane;
-      int cls = 0;
+      int cls = 0, mask = 0;
       if (s < nb) {
         if (sphere_candidate(a, bb[s])) {
-          cls = classify_exact(tg[tau], bg[s], k2);
+          cls = classify_exact(tg[tau], bg[s], k2, &mask);
           if (cls < 0) {
             atomicOr(err, 1);
             cls = 0;
@@ -124,6 +129,7 @@ __global__ void __launch_bounds__(256) k_classify(const float4* __restrict__ tb,
         out_tau[pos] = tau;
         out_sigma[pos] = s;
         out_cls[pos] = (int8_t)cls;
+        if (out_mask) out_mask[pos] = (int16_t)mask;
       }
       n += __popc(bal);
     }
@@ -443,12 +449,16 @@ __global__ void __launch_bounds__(256) k_local_diag64(OpParams op, const __grid_
                                                       const Geo64* __restrict__ tg, const Geo64* __restrict__ bg,
                                                       const int* __restrict__ tau, const int* __restrict__ sigma,
                                                       int64_t n, int force, double2* __restrict__ out,
-                                                      int8_t* __restrict__ cls_out, int* __restrict__ err) {
+                                                      int8_t* __restrict__ cls_out, int16_t* __restrict__ mask_out,
+                                                      int* __restrict__ err) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < n; e += warps) {
     const Geo64 A = tg[tau[e]], B = bg[sigma[e]];
-    int cls = force >= 0 ? force : classify_exact(A, B, op.k2);
+    int mask = 0;
+    const int exact = classify_exact(A, B, op.k2, &mask);
+    int cls = force >= 0 ? force : exact;
+    if (lane == 0 && mask_out) mask_out[e] = (int16_t)mask;
     if (cls < 0) {
       if (lane == 0) atomicOr(err, 1);
       cls = BGB_CLASS_FAR;
@@ -501,7 +511,7 @@ __global__ void __launch_bounds__(256) k_classify_batched(const float4* __restri
                                                           const double* __restrict__ prob_k2, int* __restrict__ count,
                                                           const int64_t* __restrict__ offset, int* __restrict__ out_tau,
                                                           int* __restrict__ out_sigma, int8_t* __restrict__ out_cls,
-                                                          int* __restrict__ err) {
+                                                          int16_t* __restrict__ out_mask, int* __restrict__ err) {
   const int lane = threadIdx.x & 31;
   const int warps = (gridDim.x * blockDim.x) >> 5;
   for (int tau = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; tau < nt; tau += warps) {
@@ -513,9 +523,9 @@ __global__ void __launch_bounds__(256) k_classify_batched(const float4* __restri
     int n = 0;
     for (int s0 = rg.x; s0 < rg.y; s0 += 32) {
       const int s = s0 + lane;
-      int cls = 0;
+      int cls = 0, mask = 0;
       if (s < rg.y && sphere_candidate(a, bb[s])) {
-        cls = classify_exact(tg[tau], bg[s], k2);
+        cls = classify_exact(tg[tau], bg[s], k2, &mask);
         if (cls < 0) {
           atomicOr(err, 1);
           cls = 0;
@@ -527,6 +537,7 @@ __global__ void __launch_bounds__(256) k_classify_batched(const float4* __restri
         out_tau[pos] = tau;
         out_sigma[pos] = s;
         out_cls[pos] = (int8_t)cls;
+        if (out_mask) out_mask[pos] = (int16_t)mask;
       }
       n += __popc(bal);
     }
@@ -574,14 +585,16 @@ void launch_prepare_bounds(const Geo64* g, int nt, double k2, int trial_side, fl
 }
 void launch_classify(bool fill, const float4* tb, const float4* bb, const Geo64* tg, const Geo64* bg, int nt, int nb,
                      double k2, int* count, const int64_t* offset, int* out_tau, int* out_sigma, int8_t* out_cls,
-                     int* err, int num_sms, cudaStream_t st) {
+                     int* err, int num_sms, cudaStream_t st, int16_t* out_mask) {
   if (nt <= 0) return;
   int blocks = (nt + 7) / 8;
   blocks = blocks < num_sms * 16 ? blocks : num_sms * 16;
   if (fill)
-    k_classify<true><<<blocks, 256, 0, st>>>(tb, bb, tg, bg, nt, nb, k2, count, offset, out_tau, out_sigma, out_cls, err);
+    k_classify<true><<<blocks, 256, 0, st>>>(tb, bb, tg, bg, nt, nb, k2, count, offset, out_tau, out_sigma, out_cls,
+                                              out_mask, err);
   else
-    k_classify<false><<<blocks, 256, 0, st>>>(tb, bb, tg, bg, nt, nb, k2, count, offset, out_tau, out_sigma, out_cls, err);
+    k_classify<false><<<blocks, 256, 0, st>>>(tb, bb, tg, bg, nt, nb, k2, count, offset, out_tau, out_sigma, out_cls,
+                                               nullptr, err);
 }
 void launch_scan(const int* counts, int n, int64_t* offsets, cudaStream_t st) {
   k_scan_counts<<<1, 1024, 0, st>>>(counts, n, offsets);
@@ -611,18 +624,18 @@ void launch_singular(const OpParams& op, const QuadSel& qs, const RuleTable& rul
 }
 void launch_local_diag64(const OpParams& op, const QuadSel& qs, const RuleTable& rules, int rsA, int rsB,
                          const Geo64* tg, const Geo64* bg, const int* tau, const int* sigma, int64_t n, int force,
-                         double2* out, int8_t* cls, int* err, int num_sms, cudaStream_t st) {
+                         double2* out, int8_t* cls, int* err, int num_sms, cudaStream_t st, int16_t* mask) {
   (void)rsA;
   (void)rsB;
   if (n <= 0) return;
   int64_t blocks = (n + 7) / 8;
   if (blocks > (int64_t)num_sms * 32) blocks = (int64_t)num_sms * 32;
   if (op.kind == BGB_OP_HELMHOLTZ3D_SL)
-    k_local_diag64<BGB_OP_HELMHOLTZ3D_SL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, tau, sigma, n, force, out, cls, err);
+    k_local_diag64<BGB_OP_HELMHOLTZ3D_SL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, tau, sigma, n, force, out, cls, mask, err);
   else if (op.kind == BGB_OP_MAXWELL3D_SL)
-    k_local_diag64<BGB_OP_MAXWELL3D_SL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, tau, sigma, n, force, out, cls, err);
+    k_local_diag64<BGB_OP_MAXWELL3D_SL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, tau, sigma, n, force, out, cls, mask, err);
   else
-    k_local_diag64<BGB_OP_MAXWELL3D_DL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, tau, sigma, n, force, out, cls, err);
+    k_local_diag64<BGB_OP_MAXWELL3D_DL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, tau, sigma, n, force, out, cls, mask, err);
 }
 
 void launch_prepare_bounds_batched(const Geo64* g, int nt, const int* tri_problem, const double* prob_k2, int trial_side,
@@ -632,16 +645,16 @@ void launch_prepare_bounds_batched(const Geo64* g, int nt, const int* tri_proble
 void launch_classify_batched(bool fill, const float4* tb, const float4* bb, const Geo64* tg, const Geo64* bg, int nt,
                              const int* tri_problem, const int2* prob_trial, const double* prob_k2, int* count,
                              const int64_t* offset, int* out_tau, int* out_sigma, int8_t* out_cls, int* err,
-                             int num_sms, cudaStream_t st) {
+                             int num_sms, cudaStream_t st, int16_t* out_mask) {
   if (nt <= 0) return;
   int blocks = (nt + 7) / 8;
   blocks = blocks < num_sms * 16 ? blocks : num_sms * 16;
   if (fill)
     k_classify_batched<true><<<blocks, 256, 0, st>>>(tb, bb, tg, bg, nt, tri_problem, prob_trial, prob_k2, count, offset,
-                                                     out_tau, out_sigma, out_cls, err);
+                                                     out_tau, out_sigma, out_cls, out_mask, err);
   else
     k_classify_batched<false><<<blocks, 256, 0, st>>>(tb, bb, tg, bg, nt, tri_problem, prob_trial, prob_k2, count,
-                                                      offset, out_tau, out_sigma, out_cls, err);
+                                                      offset, out_tau, out_sigma, out_cls, nullptr, err);
 }
 void launch_singular_batched(int op_kind, const OpParams* ops, const QuadSel& qs, const RuleTable& rules,
                              const Geo64* tg, const Geo64* bg, const int* tri_problem, const int* et, const int* es,

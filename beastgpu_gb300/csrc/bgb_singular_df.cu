@@ -29,10 +29,6 @@ constexpr int kSsEntryFloats = 10;   // u1, u2, v1, v2, w (df each)
 constexpr int kNearEntryFloats = 6;  // u, v, w (df each)
 
 __device__ __forceinline__ dfl ldf(const float* p) { return dfl{p[0], p[1]}; }
-__device__ __forceinline__ dfl df_of(double x) {
-  const float hi = (float)x;
-  return dfl{hi, (float)(x - (double)hi)};
-}
 
 template <int OP>
 struct DfAcc {
@@ -99,77 +95,87 @@ __device__ __forceinline__ void df_point(const dfl X[3], const dfl Y[3], const d
   }
 }
 
-// FP64 local matrix from the moments (same as finalize<OP> of k_singular, moments about the
-// chart origins oa / ob).
+__device__ __forceinline__ dfl gdf(const float* p) { return dfl{p[0], p[1]}; }
+
+// Local matrix entry (i, j) from the reduced moments, in df (moments about the chart origins).
 template <int OP>
-__device__ void df_finalize(const OpParams& op, const Geo64& A, const Geo64& B, const double oa[3], const double ob[3],
-                            const double2* m, double2 L[3][3]) {
-  const double2 alpha = make_double2(op.alpha[0], op.alpha[1]);
+__device__ __forceinline__ double2 df_entry(const OpDf& op, const GeoDf& A, const GeoDf& B, const dfl oa[3],
+                                            const dfl ob[3], const dfl* mr, const dfl* mi, int i, int j) {
+  const dfl ar = gdf(op.alpha[0]), ai = gdf(op.alpha[1]);
+  dfl tr, ti;
   if (OP == BGB_OP_HELMHOLTZ3D_SL) {
-    const double Tm[3][3] = {{0, 1, 0}, {0, 0, 1}, {1, -1, -1}};
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) {
-        double2 s = make_double2(0, 0);
-        for (int a = 0; a < 3; ++a)
-          for (int b = 0; b < 3; ++b) {
-            const double t = Tm[i][a] * Tm[j][b];
-            s.x += t * m[a * 3 + b].x;
-            s.y += t * m[a * 3 + b].y;
-          }
-        L[i][j] = cmul(alpha, s);
-      }
-    return;
-  }
-  const double inv4AA = 1.0 / (4.0 * A.area * B.area);
-  double V[3][3], W[3][3];
-  for (int i = 0; i < 3; ++i)
-    for (int c = 0; c < 3; ++c) {
-      V[i][c] = A.v[i][c] - oa[c];
-      W[i][c] = B.v[i][c] - ob[c];
-    }
-  const double2 ca = cscale(alpha, inv4AA);
-  if (OP == BGB_OP_MAXWELL3D_SL) {
-    const double2 S = m[0], P0 = m[7];
-    const double2 tb = cmul(cscale(make_double2(op.beta[0], op.beta[1]), 4.0 * inv4AA), P0);
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) {
-        double2 t = S;
-        for (int c = 0; c < 3; ++c) {
-          t.x -= V[i][c] * m[4 + c].x + W[j][c] * m[1 + c].x;
-          t.y -= V[i][c] * m[4 + c].y + W[j][c] * m[1 + c].y;
+    // f = T p with T = [[0,1,0],[0,0,1],[1,-1,-1]]
+    const int Tm[3][3] = {{0, 1, 0}, {0, 0, 1}, {1, -1, -1}};
+    tr = ti = dfl{0.f, 0.f};
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) {
+        const int t = Tm[i][a] * Tm[j][b];
+        if (t > 0) {
+          tr = df_add(tr, mr[a * 3 + b]);
+          ti = df_add(ti, mi[a * 3 + b]);
+        } else if (t < 0) {
+          tr = df_sub(tr, mr[a * 3 + b]);
+          ti = df_sub(ti, mi[a * 3 + b]);
         }
-        const double vw = V[i][0] * W[j][0] + V[i][1] * W[j][1] + V[i][2] * W[j][2];
-        t.x += vw * P0.x;
-        t.y += vw * P0.y;
-        L[i][j] = cadd(cmul(ca, t), tb);
       }
-    return;
+    const dfl Lr = df_sub(df_mul(ar, tr), df_mul(ai, ti)), Li = df_add(df_mul(ar, ti), df_mul(ai, tr));
+    return make_double2(df_to_double(Lr), df_to_double(Li));
   }
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) {
-      double2 t = m[0];
-      const double* w = W[j];
-      const double* v = V[i];
-      for (int c = 0; c < 3; ++c) {
-        t.x -= w[c] * m[4 + c].x + v[c] * m[1 + c].x;
-        t.y -= w[c] * m[4 + c].y + v[c] * m[1 + c].y;
-      }
-      const double2 x0 = make_double2(m[8].x * w[2] - m[9].x * w[1], m[8].y * w[2] - m[9].y * w[1]);
-      const double2 x1 = make_double2(m[9].x * w[0] - m[7].x * w[2], m[9].y * w[0] - m[7].y * w[2]);
-      const double2 x2 = make_double2(m[7].x * w[1] - m[8].x * w[0], m[7].y * w[1] - m[8].y * w[0]);
-      t.x += v[0] * x0.x + v[1] * x1.x + v[2] * x2.x;
-      t.y += v[0] * x0.y + v[1] * x1.y + v[2] * x2.y;
-      L[i][j] = cmul(ca, t);
+  dfl V[3], W[3];
+  for (int c = 0; c < 3; ++c) {
+    V[c] = df_sub(gdf(A.v[i][c]), oa[c]);
+    W[c] = df_sub(gdf(B.v[j][c]), ob[c]);
+  }
+  const dfl inv4AA = df_mulf(df_mul(gdf(A.inv_area), gdf(B.inv_area)), 0.25f);
+  if (OP == BGB_OP_MAXWELL3D_SL) {
+    tr = mr[0];
+    ti = mi[0];
+    for (int c = 0; c < 3; ++c) {
+      tr = df_sub(tr, df_add(df_mul(V[c], mr[4 + c]), df_mul(W[c], mr[1 + c])));
+      ti = df_sub(ti, df_add(df_mul(V[c], mi[4 + c]), df_mul(W[c], mi[1 + c])));
     }
+    const dfl vw = df_add(df_add(df_mul(V[0], W[0]), df_mul(V[1], W[1])), df_mul(V[2], W[2]));
+    tr = df_add(tr, df_mul(vw, mr[7]));
+    ti = df_add(ti, df_mul(vw, mi[7]));
+    const dfl car = df_mul(ar, inv4AA), cai = df_mul(ai, inv4AA);
+    const dfl invAA = df_mulf(inv4AA, 4.f);
+    const dfl cbr = df_mul(gdf(op.beta[0]), invAA), cbi = df_mul(gdf(op.beta[1]), invAA);
+    dfl Lr = df_sub(df_mul(car, tr), df_mul(cai, ti));
+    dfl Li = df_add(df_mul(car, ti), df_mul(cai, tr));
+    Lr = df_add(Lr, df_sub(df_mul(cbr, mr[7]), df_mul(cbi, mi[7])));
+    Li = df_add(Li, df_add(df_mul(cbr, mi[7]), df_mul(cbi, mr[7])));
+    return make_double2(df_to_double(Lr), df_to_double(Li));
+  }
+  // MFIE: A1 - W.C - V.B + V.(E x W)
+  tr = mr[0];
+  ti = mi[0];
+  for (int c = 0; c < 3; ++c) {
+    tr = df_sub(tr, df_add(df_mul(W[c], mr[4 + c]), df_mul(V[c], mr[1 + c])));
+    ti = df_sub(ti, df_add(df_mul(W[c], mi[4 + c]), df_mul(V[c], mi[1 + c])));
+  }
+  const dfl* Er = mr + 7;
+  const dfl* Ei = mi + 7;
+  const dfl xr[3] = {df_sub(df_mul(Er[1], W[2]), df_mul(Er[2], W[1])), df_sub(df_mul(Er[2], W[0]), df_mul(Er[0], W[2])),
+                     df_sub(df_mul(Er[0], W[1]), df_mul(Er[1], W[0]))};
+  const dfl xi[3] = {df_sub(df_mul(Ei[1], W[2]), df_mul(Ei[2], W[1])), df_sub(df_mul(Ei[2], W[0]), df_mul(Ei[0], W[2])),
+                     df_sub(df_mul(Ei[0], W[1]), df_mul(Ei[1], W[0]))};
+  for (int c = 0; c < 3; ++c) {
+    tr = df_add(tr, df_mul(V[c], xr[c]));
+    ti = df_add(ti, df_mul(V[c], xi[c]));
+  }
+  const dfl car = df_mul(ar, inv4AA), cai = df_mul(ai, inv4AA);
+  const dfl Lr = df_sub(df_mul(car, tr), df_mul(cai, ti)), Li = df_add(df_mul(car, ti), df_mul(cai, tr));
+  return make_double2(df_to_double(Lr), df_to_double(Li));
 }
 
 template <int OP, bool BATCH>
-__global__ void __launch_bounds__(256) k_singular_df(OpParams op1, const OpParams* __restrict__ ops,
+__global__ void __launch_bounds__(256) k_singular_df(OpDf op1, const OpDf* __restrict__ ops,
                                                      const int* __restrict__ tri_problem, const __grid_constant__ DfTables M,
-                                                     const float* __restrict__ tab, const Geo64* __restrict__ tg,
-                                                     const Geo64* __restrict__ bg, const int* __restrict__ ent_tau,
+                                                     const float* __restrict__ tab, const GeoDf* __restrict__ tg,
+                                                     const GeoDf* __restrict__ bg, const int* __restrict__ ent_tau,
                                                      const int* __restrict__ ent_sigma, const int8_t* __restrict__ ent_cls,
-                                                     int64_t n, double2* __restrict__ out, const volatile int* abort_flag) {
+                                                     const int16_t* __restrict__ ent_mask, int64_t n,
+                                                     double2* __restrict__ out, const volatile int* abort_flag) {
   __shared__ float4 trig[128];
   for (int i = threadIdx.x; i < 128; i += blockDim.x) trig[i] = ((const float4*)(tab + M.trig_off))[i];
   __syncthreads();
@@ -179,29 +185,27 @@ __global__ void __launch_bounds__(256) k_singular_df(OpParams op1, const OpParam
   for (int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < n; e += warps) {
     if (abort_flag && *abort_flag) return;
     const int tau = ent_tau[e];
-    const OpParams op = BATCH ? ops[tri_problem[tau]] : op1;
-    const Geo64 A = tg[tau], B = bg[ent_sigma[e]];
+    const OpDf op = BATCH ? ops[tri_problem[tau]] : op1;
+    const GeoDf A = tg[tau], B = bg[ent_sigma[e]];
     const int cls = ent_cls[e];
     DfAcc<OP> acc;
 #pragma unroll
     for (int k = 0; k < NA; ++k) acc.re[k] = acc.im[k] = dfl{0.f, 0.f};
-    const dfl kd = df_of(op.gamma[1]);
-    const bool oscill = op.gamma[1] != 0.0;
-    double oa[3], ob[3];
+    const dfl kd = gdf(op.k);
+    const bool oscill = op.oscill != 0;
+    dfl oa[3], ob[3];
     if (cls == BGB_CLASS_NEAR) {
-      for (int c = 0; c < 3; ++c) {
-        oa[c] = A.v[2][c];
-        ob[c] = B.v[2][c];
-      }
       dfl ea[2][3], eb[2][3], D0[3];
       for (int c = 0; c < 3; ++c) {
-        ea[0][c] = df_of(A.t[0][c]);
-        ea[1][c] = df_of(A.t[1][c]);
-        eb[0][c] = df_of(B.t[0][c]);
-        eb[1][c] = df_of(B.t[1][c]);
-        D0[c] = df_of(oa[c] - ob[c]);
+        oa[c] = gdf(A.v[2][c]);
+        ob[c] = gdf(B.v[2][c]);
+        ea[0][c] = df_sub(gdf(A.v[0][c]), oa[c]);
+        ea[1][c] = df_sub(gdf(A.v[1][c]), oa[c]);
+        eb[0][c] = df_sub(gdf(B.v[0][c]), ob[c]);
+        eb[1][c] = df_sub(gdf(B.v[1][c]), ob[c]);
+        D0[c] = df_sub(oa[c], ob[c]);
       }
-      const dfl AB = df_of(A.area * B.area);
+      const dfl AB = df_mul(gdf(A.area), gdf(B.area));
       const float* tt = tab + M.near_t_off;
       const float* tb = tab + M.near_b_off;
       for (int idx = lane; idx < M.near_qt * M.near_qb; idx += 32) {
@@ -220,28 +224,30 @@ __global__ void __launch_bounds__(256) k_singular_df(OpParams op1, const OpParam
       }
     } else if (!(OP == BGB_OP_MAXWELL3D_DL && cls == BGB_CLASS_CF)) {
       int I[3], J[3];
-      ss_permutation(cls, A, B, I, J);
-      Chart chA, chB;
-      make_chart(I, chA);
-      make_chart(J, chB);
+      ss_permutation_mask(cls, ent_mask[e], I, J);
+      for (int k = 0; k < 3; ++k) {  // guard against an inconsistent mask
+        I[k] = I[k] < 1 ? 1 : (I[k] > 3 ? 3 : I[k]);
+        J[k] = J[k] < 1 ? 1 : (J[k] > 3 ? 3 : J[k]);
+      }
       const int ia0 = I[2] - 1, ia1 = I[0] - 1, ia2 = I[1] - 1;
       const int ib0 = J[2] - 1, ib1 = J[0] - 1, ib2 = J[1] - 1;
       dfl ea[2][3], eb[2][3], D0[3];
       for (int c = 0; c < 3; ++c) {
-        oa[c] = A.v[ia0][c];
-        ob[c] = B.v[ib0][c];
-        ea[0][c] = df_of(A.v[ia1][c] - oa[c]);
-        ea[1][c] = df_of(A.v[ia2][c] - oa[c]);
-        eb[0][c] = df_of(B.v[ib1][c] - ob[c]);
-        eb[1][c] = df_of(B.v[ib2][c] - ob[c]);
-        D0[c] = df_of(oa[c] - ob[c]);
+        oa[c] = gdf(A.v[ia0][c]);
+        ob[c] = gdf(B.v[ib0][c]);
+        ea[0][c] = df_sub(gdf(A.v[ia1][c]), oa[c]);
+        ea[1][c] = df_sub(gdf(A.v[ia2][c]), oa[c]);
+        eb[0][c] = df_sub(gdf(B.v[ib1][c]), ob[c]);
+        eb[1][c] = df_sub(gdf(B.v[ib2][c]), ob[c]);
+        D0[c] = df_sub(oa[c], ob[c]);
       }
-      // barycentric chart coordinates: b = cv3 + (cv1 - cv3) u1 + (cv2 - cv3) u2, integer coefficients
-      const float ba0 = (float)chA.cv[2][0], ba1 = (float)chA.cv[2][1];
-      const float bb0 = (float)chB.cv[2][0], bb1 = (float)chB.cv[2][1];
-      const float cax1 = (float)chA.ct[0][0], cax2 = (float)chA.ct[1][0], cay1 = (float)chA.ct[0][1], cay2 = (float)chA.ct[1][1];
-      const float cbx1 = (float)chB.ct[0][0], cbx2 = (float)chB.ct[1][0], cby1 = (float)chB.ct[0][1], cby2 = (float)chB.ct[1][1];
-      const dfl jac = df_of((4.0 * A.area) * B.area);
+      // barycentric chart coordinates b = cv3 + (cv1 - cv3) u1 + (cv2 - cv3) u2 with the
+      // reference-triangle vertices (1,0), (0,1), (0,0) (integer coefficients)
+      const float VX[3] = {1.f, 0.f, 0.f}, VY[3] = {0.f, 1.f, 0.f};
+      const float ba0 = VX[ia0], ba1 = VY[ia0], bb0 = VX[ib0], bb1 = VY[ib0];
+      const float cax1 = VX[ia1] - ba0, cax2 = VX[ia2] - ba0, cay1 = VY[ia1] - ba1, cay2 = VY[ia2] - ba1;
+      const float cbx1 = VX[ib1] - bb0, cbx2 = VX[ib2] - bb0, cby1 = VY[ib1] - bb1, cby2 = VY[ib2] - bb1;
+      const dfl jac = df_mulf(df_mul(gdf(A.area), gdf(B.area)), 4.f);
       const float* tbl = tab + M.ss_off[cls];
       const int cnt = M.ss_cnt[cls];
       for (int idx = lane; idx < cnt; idx += 32) {
@@ -263,28 +269,38 @@ __global__ void __launch_bounds__(256) k_singular_df(OpParams op1, const OpParam
         df_point<OP>(X, Y, d, bx1, bx2, by1, by2, df_mul(jac, mul), kd, oscill, trig, M.trig, acc);
       }
     } else {
-      for (int c = 0; c < 3; ++c) oa[c] = ob[c] = 0.0;
+      for (int c = 0; c < 3; ++c) oa[c] = ob[c] = dfl{0.f, 0.f};
     }
-    double2 m[NA];
+    // warp reduction in df
 #pragma unroll
-    for (int k = 0; k < NA; ++k) {
-      m[k] = make_double2(df_to_double(acc.re[k]), df_to_double(acc.im[k]));
+    for (int k = 0; k < NA; ++k)
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) {
-        m[k].x += __shfl_xor_sync(0xffffffffu, m[k].x, off);
-        m[k].y += __shfl_xor_sync(0xffffffffu, m[k].y, off);
+        const dfl orr{__shfl_xor_sync(0xffffffffu, acc.re[k].hi, off), __shfl_xor_sync(0xffffffffu, acc.re[k].lo, off)};
+        const dfl oii{__shfl_xor_sync(0xffffffffu, acc.im[k].hi, off), __shfl_xor_sync(0xffffffffu, acc.im[k].lo, off)};
+        acc.re[k] = df_add(acc.re[k], orr);
+        acc.im[k] = df_add(acc.im[k], oii);
       }
-    }
-    double2 L[3][3];
-    df_finalize<OP>(op, A, B, oa, ob, m, L);
-    if (lane < 9) {
-      double2 v = L[0][0];
-#pragma unroll
-      for (int q = 1; q < 9; ++q)
-        if (lane == q) v = L[q / 3][q % 3];
-      out[e * 9 + lane] = v;
-    }
+    if (lane < 9) out[e * 9 + lane] = df_entry<OP>(op, A, B, oa, ob, acc.re, acc.im, lane / 3, lane % 3);
   }
+}
+
+__global__ void k_prepare_geodf(const Geo64* __restrict__ g, int nt, GeoDf* __restrict__ out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nt) return;
+  GeoDf r;
+  for (int a = 0; a < 3; ++a)
+    for (int c = 0; c < 3; ++c) {
+      const double x = g[t].v[a][c];
+      r.v[a][c][0] = (float)x;
+      r.v[a][c][1] = (float)(x - (double)r.v[a][c][0]);
+    }
+  const double A = g[t].area, iA = 1.0 / A;
+  r.area[0] = (float)A;
+  r.area[1] = (float)(A - (double)r.area[0]);
+  r.inv_area[0] = (float)iA;
+  r.inv_area[1] = (float)(iA - (double)r.inv_area[0]);
+  out[t] = r;
 }
 
 void split(double x, float* out) {
@@ -384,21 +400,37 @@ void build_df_tables(const QuadSel& qs, const RuleTable& R, std::vector<float>& 
   M.total_floats = (int)buf.size();
 }
 
-void launch_singular_df(int op_kind, const OpParams& op, const OpParams* ops, const int* tri_problem,
-                        const DfTables& M, const float* dtab, const Geo64* tg, const Geo64* bg, const int* et,
-                        const int* es, const int8_t* ec, int64_t n, double2* out, const volatile int* abort_flag,
-                        int num_sms, cudaStream_t st) {
+void launch_prepare_geodf(const Geo64* g, int nt, GeoDf* out, cudaStream_t st) {
+  if (nt > 0) k_prepare_geodf<<<(nt + 255) / 256, 256, 0, st>>>(g, nt, out);
+}
+
+OpDf make_opdf(const OpParams& op) {
+  OpDf r{};
+  for (int c = 0; c < 2; ++c) {
+    split(op.alpha[c], r.alpha[c]);
+    split(op.beta[c], r.beta[c]);
+  }
+  split(op.gamma[1], r.k);
+  r.kind = op.kind;
+  r.oscill = op.gamma[1] != 0.0;
+  return r;
+}
+
+void launch_singular_df(int op_kind, const OpDf& op, const OpDf* opdf_array, const int* tri_problem,
+                        const DfTables& M, const float* dtab, const GeoDf* tg, const GeoDf* bg, const int* et,
+                        const int* es, const int8_t* ec, const int16_t* emask, int64_t n, double2* out,
+                        const volatile int* abort_flag, int num_sms, cudaStream_t st) {
   if (n <= 0) return;
   int64_t blocks = (n + 7) / 8;
   if (blocks > (int64_t)num_sms * 32) blocks = (int64_t)num_sms * 32;
-  const bool batch = ops != nullptr;
-#define BGB_LAUNCH_DF(OPK)                                                                                      \
-  if (batch)                                                                                                    \
-    k_singular_df<OPK, true><<<(int)blocks, 256, 0, st>>>(op, ops, tri_problem, M, dtab, tg, bg, et, es, ec, n, out, \
-                                                          abort_flag);                                          \
-  else                                                                                                          \
-    k_singular_df<OPK, false><<<(int)blocks, 256, 0, st>>>(op, ops, tri_problem, M, dtab, tg, bg, et, es, ec, n, out, \
-                                                           abort_flag);
+  const bool batch = opdf_array != nullptr;
+#define BGB_LAUNCH_DF(OPK)                                                                                        \
+  if (batch)                                                                                                      \
+    k_singular_df<OPK, true><<<(int)blocks, 256, 0, st>>>(op, opdf_array, tri_problem, M, dtab, tg, bg, et, es, ec, \
+                                                          emask, n, out, abort_flag);                             \
+  else                                                                                                            \
+    k_singular_df<OPK, false><<<(int)blocks, 256, 0, st>>>(op, opdf_array, tri_problem, M, dtab, tg, bg, et, es, ec, \
+                                                           emask, n, out, abort_flag);
   if (op_kind == BGB_OP_HELMHOLTZ3D_SL) {
     BGB_LAUNCH_DF(BGB_OP_HELMHOLTZ3D_SL)
   } else if (op_kind == BGB_OP_MAXWELL3D_SL) {

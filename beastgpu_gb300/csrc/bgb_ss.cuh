@@ -110,4 +110,43 @@ __host__ __device__ __forceinline__ void ss_region(int cls, int r, double h1, do
   }
 }
 
+// The same permutation from the coincident-vertex mask recorded by the classifier (bit
+// (i-1) * 3 + (j-1) set when test vertex i and trial vertex j coincide): pure integer logic.
+__host__ __device__ inline void ss_permutation_mask(int cls, int mask, int I[3], int J[3]) {
+  I[0] = I[1] = I[2] = 0;
+  J[0] = J[1] = J[2] = 0;
+  const int cap = (cls == BGB_CLASS_CE) ? 3 : 2;
+  int e = 1;
+  for (int i = 1; i <= 3; ++i)
+    for (int j = 1; j <= 3; ++j)
+      if ((mask >> ((i - 1) * 3 + (j - 1))) & 1) {
+        if (cls == BGB_CLASS_CF) {
+          J[i - 1] = j;
+        } else if (e <= cap) {
+          J[e - 1] = j;
+          I[e - 1] = i;
+          e += 1;
+        }
+      }
+  if (cls == BGB_CLASS_CF) {
+    I[0] = 1;
+    I[1] = 2;
+    I[2] = 3;
+    return;
+  }
+  for (int k = 0; k < 2; ++k) {
+    int* a = k ? I : J;
+    const bool e1 = (e == 1), e2 = (e == 2);
+    a[0] = e1 ? 1 : a[0];
+    a[1] = e1 ? 2 : (e2 ? (a[0] == 1 ? 2 : 1) : a[1]);
+    a[2] = 6 - a[0] - a[1];
+    if (cls == BGB_CLASS_CE) {
+      const int t = a[0];
+      a[0] = a[1];
+      a[1] = a[2];
+      a[2] = t;
+    }
+  }
+}
+
 }  // namespace bgb
