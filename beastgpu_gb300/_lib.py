@@ -16,6 +16,8 @@ STATUS = {0: "OK", -1: "INVALID", -2: "OOM", -3: "CUDA", -4: "TIMEOUT", -5: "ABO
           -7: "NOT_SUPPORTED"}
 PREC_FP64, PREC_MIXED = 0, 1
 OUT_HOST_C64, OUT_HOST_C32, OUT_DEVICE_C64, OUT_DEVICE_C32 = 0, 1, 2, 3
+CFG_PAGEABLE_VIA_RING = 1
+ABI_VERSION = 2  # BGB_ABI_VERSION of include/beastgb.h
 
 
 class BGBError(RuntimeError):
@@ -47,15 +49,17 @@ class Config(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("pairs_total", C.c_int64), ("pairs_class", C.c_int64 * 5), ("pairs_computed", C.c_int64),
                 ("ms_classify", C.c_double), ("ms_singular", C.c_double), ("ms_far", C.c_double),
-                ("ms_copy", C.c_double), ("ms_total", C.c_double), ("row_blocks", C.c_int32),
-                ("tile_config", C.c_int32), ("kernel_launches", C.c_int32), ("reserved", C.c_int32)]
+                ("ms_copy", C.c_double), ("ms_total", C.c_double), ("ms_pipeline", C.c_double),
+                ("ms_plan", C.c_double), ("out_blocks", C.c_int32), ("tile_config", C.c_int32),
+                ("kernel_launches", C.c_int32), ("schedule", C.c_int32)]
 
     def as_dict(self):
         return {"pairs_total": self.pairs_total, "pairs_class": list(self.pairs_class),
                 "pairs_computed": self.pairs_computed, "ms_classify": self.ms_classify,
                 "ms_singular": self.ms_singular, "ms_far": self.ms_far, "ms_copy": self.ms_copy,
-                "ms_total": self.ms_total, "row_blocks": self.row_blocks, "tile_config": self.tile_config,
-                "kernel_launches": self.kernel_launches}
+                "ms_total": self.ms_total, "ms_pipeline": self.ms_pipeline, "ms_plan": self.ms_plan,
+                "out_blocks": self.out_blocks, "tile_config": self.tile_config,
+                "kernel_launches": self.kernel_launches, "schedule": self.schedule}
 
 
 class Problem(C.Structure):
@@ -107,6 +111,8 @@ def load():
             fn = getattr(lib, name)
             fn.argtypes = args
             fn.restype = res
+        if lib.bgb_abi_version() != ABI_VERSION:
+            raise RuntimeError(f"{LIB_PATH} has ABI {lib.bgb_abi_version()}, the bindings expect {ABI_VERSION}: rebuild it")
         _lib = lib
     return _lib
 

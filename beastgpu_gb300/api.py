@@ -55,7 +55,11 @@ class GPUConfiguration:
     precision: "fp64" (plain all-FP64 kernels, the drop-in) or "mixed" (FP32 far pairs with
     double-float phase base, FP64 singular and near pairs).
     total_GPU_budget: HBM bytes the call may use for the output staging (0 = 90% of free);
-    host outputs larger than half of it are produced in row blocks.
+    host outputs are produced in blocks of columns of at most a quarter of it (two device
+    staging buffers), and large outputs in about 16 blocks so that copies overlap the fill.
+    pinned_ring_bytes: size of each half of the pinned host ring that pageable host outputs
+    are copied through when the device cannot write pageable memory directly (0 = 512 MiB).
+    pageable_via_ring: use the ring even where the device writes pageable memory directly.
     """
     writeBackStrategy: GpuWriteBack = None
     precision: str = "fp64"
@@ -63,6 +67,8 @@ class GPUConfiguration:
     total_GPU_budget: int = 0
     tile_config: int = -1
     makeCompexWithGPU: bool = True
+    pinned_ring_bytes: int = 0
+    pageable_via_ring: bool = False
 
     def __post_init__(self):
         if self.writeBackStrategy is None:
@@ -78,10 +84,11 @@ _hlock = threading.Lock()
 class Handle:
     """Owns one bgb_handle (device scratch, streams)."""
 
-    def __init__(self, device: int = 0, hbm_budget: int = 0, tile_config: int = -1):
+    def __init__(self, device: int = 0, hbm_budget: int = 0, tile_config: int = -1, pinned_ring: int = 0,
+                 flags: int = 0):
         lib = _lib.load()
         self.ptr = C.c_void_p()
-        cfg = _lib.Config(device, int(hbm_budget), 0, int(tile_config), 0)
+        cfg = _lib.Config(device, int(hbm_budget), int(pinned_ring), int(tile_config), int(flags))
         _lib.check(lib.bgb_create(C.byref(self.ptr), C.byref(cfg)))
         self.device = device
 
@@ -97,12 +104,13 @@ class Handle:
             pass
 
 
-def get_handle(device: int = 0, hbm_budget: int = 0, tile_config: int = -1) -> Handle:
-    key = (device, int(hbm_budget), int(tile_config))
+def get_handle(device: int = 0, hbm_budget: int = 0, tile_config: int = -1, pinned_ring: int = 0,
+               flags: int = 0) -> Handle:
+    key = (device, int(hbm_budget), int(tile_config), int(pinned_ring), int(flags))
     with _hlock:
         h = _handles.get(key)
         if h is None:
-            h = Handle(device, hbm_budget, tile_config)
+            h = Handle(device, hbm_budget, tile_config, pinned_ring, flags)
             _handles[key] = h
         return h
 
@@ -162,7 +170,8 @@ def assemble_gpu(operator: Operator, test_functions: Space, trial_functions: Spa
     c64 = dtype == np.complex128
     row0, nrows = (0, test_functions.nfun) if rows is None else (int(rows[0]), int(rows[1]))
     ncols = trial_functions.nfun
-    h = get_handle(config.device, config.total_GPU_budget, config.tile_config)
+    h = get_handle(config.device, config.total_GPU_budget, config.tile_config, config.pinned_ring_bytes,
+                   _lib.CFG_PAGEABLE_VIA_RING if config.pageable_via_ring else 0)
     keep = _Keep()
     cop, ct, cb, cq = c_operator(operator), c_space(test_functions, keep), c_space(trial_functions, keep), \
         c_quadstrat(quadstrat)
@@ -261,7 +270,8 @@ class Batch:
             dtype = np.complex128 if prec == _lib.PREC_FP64 else np.complex64
         dtype = np.dtype(dtype)
         c64 = dtype == np.complex128
-        self.h = get_handle(config.device, config.total_GPU_budget, config.tile_config)
+        self.h = get_handle(config.device, config.total_GPU_budget, config.tile_config, config.pinned_ring_bytes,
+                   _lib.CFG_PAGEABLE_VIA_RING if config.pageable_via_ring else 0)
         self._keep = _Keep()
         arr = (_lib.Problem * len(problems))()
         self.outputs = []

@@ -12,9 +12,13 @@
 #include "bgb_host.h"
 #include "trirules.h"
 
+#include <sys/mman.h>
+#include <unistd.h>
+
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <condition_variable>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -22,6 +26,7 @@
 #include <mutex>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace bgb {
@@ -219,181 +224,6 @@ FarConst make_farconst(const OpParams& op, const RuleTable& R, const QuadSel& qs
 // ----------------------------------------------------------------------------------------
 // Host planning: Morton-ordered function blocks and their triangle sets
 // ----------------------------------------------------------------------------------------
-static inline uint64_t spread3(uint64_t x) {
-  x &= 0x1fffff;
-  x = (x | x << 32) & 0x1f00000000ffffULL;
-  x = (x | x << 16) & 0x1f0000ff0000ffULL;
-  x = (x | x << 8) & 0x100f00f00f00f00fULL;
-  x = (x | x << 4) & 0x10c30c30c30c30c3ULL;
-  x = (x | x << 2) & 0x1249249249249249ULL;
-  return x;
-}
-
-// Morton position of every triangle (rank in the order of 3-D Morton codes of centroids).
-std::vector<int> morton_rank(const bgb_space* s) {
-  const int nt = s->nt;
-  std::vector<double> c(3 * (size_t)nt);
-  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-  for (int t = 0; t < nt; ++t)
-    for (int k = 0; k < 3; ++k) {
-      double v = 0;
-      for (int a = 0; a < 3; ++a) v += s->vertices[3 * (int64_t)s->triangles[3 * (int64_t)t + a] + k];
-      v /= 3.0;
-      c[3 * (size_t)t + k] = v;
-      lo[k] = std::min(lo[k], v);
-      hi[k] = std::max(hi[k], v);
-    }
-  double span = std::max({hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2], 1e-300});
-  std::vector<std::pair<uint64_t, int>> key(nt);
-  for (int t = 0; t < nt; ++t) {
-    uint64_t code = 0;
-    for (int k = 0; k < 3; ++k) {
-      double f = (c[3 * (size_t)t + k] - lo[k]) / span;
-      uint64_t q = (uint64_t)std::min(std::max(f, 0.0) * 2097151.0, 2097151.0);
-      code |= spread3(q) << k;
-    }
-    key[t] = {code, t};
-  }
-  std::sort(key.begin(), key.end());
-  std::vector<int> rank(nt);
-  for (int i = 0; i < nt; ++i) rank[key[i].second] = i;
-  return rank;
-}
-
-Supports build_supports(const bgb_space* s) {
-  Supports S;
-  S.off.assign((size_t)s->nfun + 1, 0);
-  for (int64_t t = 0; t < s->nt; ++t)
-    for (int i = 0; i < 3; ++i) {
-      int f = s->fn_index[3 * t + i];
-      if (f >= 0) S.off[f + 1]++;
-    }
-  for (int f = 0; f < s->nfun; ++f) S.off[f + 1] += S.off[f];
-  S.tri.resize(S.off[s->nfun]);
-  S.loc.resize(S.off[s->nfun]);
-  S.coef.resize(S.off[s->nfun]);
-  std::vector<int64_t> fill(S.off.begin(), S.off.end() - 1);
-  for (int64_t t = 0; t < s->nt; ++t)  // triangles ascending -> supports sorted by triangle
-    for (int i = 0; i < 3; ++i) {
-      int f = s->fn_index[3 * t + i];
-      if (f < 0) continue;
-      int64_t k = fill[f]++;
-      S.tri[k] = (int)t;
-      S.loc[k] = i;
-      S.coef[k] = s->fn_coef[3 * t + i];
-    }
-  return S;
-}
-
-// Functions [f_begin, f_end) ordered by the Morton rank of their first support.
-std::vector<int> order_functions(const Supports& S, const std::vector<int>& rank, int f_begin, int f_end) {
-  std::vector<std::pair<int64_t, int>> key;
-  key.reserve(f_end - f_begin);
-  for (int f = f_begin; f < f_end; ++f) {
-    int64_t first = INT64_MAX;
-    for (int64_t k = S.off[f]; k < S.off[f + 1]; ++k) first = std::min<int64_t>(first, rank[S.tri[k]]);
-    key.push_back({first, f});
-  }
-  std::sort(key.begin(), key.end());
-  std::vector<int> out(key.size());
-  for (size_t i = 0; i < key.size(); ++i) out[i] = key[i].second;
-  return out;
-}
-
-void plan_test_side(const Supports& S, const std::vector<int>& order, int FM, int64_t row0, HostPlan& P) {
-  P.tb_off.push_back(0);
-  P.tb_fn_off.push_back(0);
-  P.fs_off.push_back(0);
-  std::vector<int> tris;
-  for (size_t b0 = 0; b0 < order.size(); b0 += FM) {
-    size_t b1 = std::min(order.size(), b0 + FM);
-    tris.clear();
-    for (size_t i = b0; i < b1; ++i) {
-      int f = order[i];
-      for (int64_t k = S.off[f]; k < S.off[f + 1]; ++k) tris.push_back(S.tri[k]);
-    }
-    std::sort(tris.begin(), tris.end());
-    tris.erase(std::unique(tris.begin(), tris.end()), tris.end());
-    for (size_t i = b0; i < b1; ++i) {
-      int f = order[i];
-      int cnt = 0;
-      for (int64_t k = S.off[f]; k < S.off[f + 1]; ++k) {
-        int slot = (int)(std::lower_bound(tris.begin(), tris.end(), S.tri[k]) - tris.begin());
-        P.fs_code.push_back(slot << 2 | S.loc[k]);
-        P.fs_coef.push_back(S.coef[k]);
-        ++cnt;
-      }
-      P.MAXS = std::max(P.MAXS, cnt);
-      P.fs_off.push_back((int)P.fs_code.size());
-      P.rows.push_back((int64_t)f - row0);
-    }
-    P.tb_tris.insert(P.tb_tris.end(), tris.begin(), tris.end());
-    P.tb_off.push_back((int)P.tb_tris.size());
-    P.tb_fn_off.push_back((int)b1);
-    P.tmax = std::max(P.tmax, (int)tris.size());
-  }
-}
-
-void plan_trial_side(const Supports& S, const std::vector<int>& order, int FN, int SC, HostPlan& P) {
-  P.bb_off.push_back(0);
-  P.bb_fn_off.push_back(0);
-  P.bb_chunk_off.push_back(0);
-  P.ch_grp_off.push_back(0);
-  P.grp_sup_off.push_back(0);
-  std::vector<int> tris;
-  struct Ent { int chunk, nl, slot, loc; double coef; };
-  std::vector<Ent> ents;
-  for (size_t b0 = 0; b0 < order.size(); b0 += FN) {
-    size_t b1 = std::min(order.size(), b0 + FN);
-    tris.clear();
-    for (size_t i = b0; i < b1; ++i) {
-      int f = order[i];
-      for (int64_t k = S.off[f]; k < S.off[f + 1]; ++k) tris.push_back(S.tri[k]);
-    }
-    std::sort(tris.begin(), tris.end());
-    tris.erase(std::unique(tris.begin(), tris.end()), tris.end());
-    ents.clear();
-    for (size_t i = b0; i < b1; ++i) {
-      int f = order[i];
-      for (int64_t k = S.off[f]; k < S.off[f + 1]; ++k) {
-        int slot = (int)(std::lower_bound(tris.begin(), tris.end(), S.tri[k]) - tris.begin());
-        ents.push_back({slot / SC, (int)(i - b0), slot, S.loc[k], S.coef[k]});
-      }
-    }
-    // groups: per chunk, per local function, supports by slot (= trial triangle) ascending
-    std::sort(ents.begin(), ents.end(), [](const Ent& a, const Ent& b) {
-      if (a.chunk != b.chunk) return a.chunk < b.chunk;
-      if (a.nl != b.nl) return a.nl < b.nl;
-      return a.slot < b.slot;
-    });
-    int nchunks = ((int)tris.size() + SC - 1) / SC;
-    size_t e = 0;
-    for (int c = 0; c < nchunks; ++c) {
-      while (e < ents.size() && ents[e].chunk == c) {
-        int nl = ents[e].nl;
-        P.grp_fn.push_back(nl);
-        while (e < ents.size() && ents[e].chunk == c && ents[e].nl == nl) {
-          P.gs_code.push_back(ents[e].slot << 2 | ents[e].loc);
-          P.gs_coef.push_back(ents[e].coef);
-          ++e;
-        }
-        P.grp_sup_off.push_back((int)P.gs_code.size());
-      }
-      P.ch_grp_off.push_back((int)P.grp_fn.size());
-    }
-    for (size_t i = b0; i < b1; ++i) P.cols.push_back(order[i]);
-    const int g_lo = P.ch_grp_off[P.ch_grp_off.size() - 1 - nchunks];
-    const int g_hi = P.ch_grp_off.back();
-    P.gmax = std::max(P.gmax, g_hi - g_lo);
-    P.gsmax = std::max(P.gsmax, P.grp_sup_off[g_hi] - P.grp_sup_off[g_lo]);
-    P.bb_tris.insert(P.bb_tris.end(), tris.begin(), tris.end());
-    P.bb_off.push_back((int)P.bb_tris.size());
-    P.bb_fn_off.push_back((int)b1);
-    P.bb_chunk_off.push_back(P.bb_chunk_off.back() + nchunks);
-    P.nmax = std::max(P.nmax, (int)tris.size());
-  }
-}
-
 // Tile configurations: (FM, FN, SC) per precision.
 const TileCfg kTileCfgs[] = {
     {64, 64, 16},   // 0: mixed, RWG
@@ -459,6 +289,91 @@ bool df_singular_ok(const OpParams& op, double edge_t, double edge_b) {
   // singular / near pairs have R <= (edge_t + edge_b) * 2 at most; df_sincos covers |k R| < 400
   return op.gamma[0] == 0.0 && std::fabs(op.gamma[1]) * 2.0 * (edge_t + edge_b) < 350.0;
 }
+
+static int ensure_ring(bgb_handle* h, size_t bytes) {
+  if (h->ring && h->ring_bytes >= bytes) return 0;
+  if (h->ring) cudaFreeHost(h->ring);
+  h->ring = nullptr;
+  h->ring_bytes = 0;
+  cudaError_t e = cudaHostAlloc(&h->ring, bytes, cudaHostAllocDefault);
+  if (e != cudaSuccess) {
+    h->ring = nullptr;
+    return cuda_fail(e, "cudaHostAlloc(pinned ring)");
+  }
+  h->ring_bytes = bytes;
+  return 0;
+}
+
+// Copy ncols column segments (seg bytes each) from a contiguous source into a strided
+// destination, split over host threads (by byte ranges when both sides are contiguous).
+static void parallel_copy_columns(char* dst, size_t dpitch, const char* src, size_t spitch, size_t seg, int64_t ncols) {
+  const int64_t total = (int64_t)seg * ncols;
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const int nth = (int)std::min<int64_t>(std::min<unsigned>(16u, hw), std::max<int64_t>(1, total / ((int64_t)16 << 20)));
+  const bool contiguous = dpitch == seg && spitch == seg;
+  auto work = [&](int t) {
+    if (contiguous) {
+      const int64_t b0 = total * t / nth, b1 = total * (t + 1) / nth;
+      std::memcpy(dst + b0, src + b0, (size_t)(b1 - b0));
+      return;
+    }
+    const int64_t c0 = ncols * t / nth, c1 = ncols * (t + 1) / nth;
+    for (int64_t c = c0; c < c1; ++c) std::memcpy(dst + (size_t)c * dpitch, src + (size_t)c * spitch, seg);
+  };
+  if (nth == 1) {
+    work(0);
+    return;
+  }
+  std::vector<std::thread> th;
+  for (int t = 1; t < nth; ++t) th.emplace_back(work, t);
+  work(0);
+  for (auto& x : th) x.join();
+}
+
+// Fault in the pages of [p, p + n) that are not resident (mincore) by writing one byte inside
+// the range per page, in host threads.  The range belongs to the output being assembled.
+static void prefault_range(char* p, size_t n, int nth) {
+  if (n == 0) return;
+  static const size_t page = (size_t)sysconf(_SC_PAGESIZE);
+  const uintptr_t a = (uintptr_t)p & ~(uintptr_t)(page - 1);
+  const size_t len = (((uintptr_t)p + n - a) + page - 1) & ~(page - 1);
+  const size_t np = len / page;
+  std::vector<unsigned char> vec(np);
+  const bool have = mincore((void*)a, len, vec.data()) == 0;
+  if (have) {
+    bool all = true;
+    for (unsigned char v : vec) all = all && (v & 1);
+    if (all) return;
+  }
+  nth = (int)std::max<size_t>(1, std::min<size_t>((size_t)nth, np / 64));
+  auto work = [&](int t) {
+    for (size_t k = np * t / nth; k < np * (t + 1) / nth; ++k) {
+      if (have && (vec[k] & 1)) continue;
+      char* q = std::max(p, (char*)(a + k * page));
+      *(volatile char*)q = 0;
+    }
+  };
+  std::vector<std::thread> th;
+  for (int t = 1; t < nth; ++t) th.emplace_back(work, t);
+  work(0);
+  for (auto& x : th) x.join();
+}
+
+// Progress of the host thread that faults in the pages of the output blocks in order.
+struct PrefaultProgress {
+  std::mutex m;
+  std::condition_variable cv;
+  int done = 0;
+  std::atomic<bool> stop{false};
+  void advance() {
+    { std::lock_guard<std::mutex> g(m); ++done; }
+    cv.notify_all();
+  }
+  void wait_for(int blocks) {
+    std::unique_lock<std::mutex> g(m);
+    cv.wait(g, [&] { return done >= blocks; });
+  }
+};
 
 static int check_abort(bgb_handle* h) {
   if (h->abort_host && *h->abort_host) {
@@ -547,7 +462,10 @@ int bgb_create(bgb_handle** out, const bgb_config* cfg) {
     rc = cuda_fail(e, "cudaStreamCreate");
   }
   for (int i = 0; i < 8 && !rc; ++i)
-    if ((e = cudaEventCreate(&h->ev[i])) != cudaSuccess) rc = cuda_fail(e, "cudaEventCreate");
+    if ((e = cudaEventCreate(&h->ev[i])) != cudaSuccess || (e = cudaEventCreate(&h->ev2[i])) != cudaSuccess)
+      rc = cuda_fail(e, "cudaEventCreate");
+  for (int i = 0; i < 2 && !rc; ++i)
+    if ((e = cudaEventCreateWithFlags(&h->ring_ev[i], cudaEventDisableTiming)) != cudaSuccess) rc = cuda_fail(e, "cudaEventCreate");
   if (!rc) {
     int* p = nullptr;
     if ((e = cudaHostAlloc((void**)&p, sizeof(int), cudaHostAllocMapped)) != cudaSuccess) rc = cuda_fail(e, "cudaHostAlloc");
@@ -572,11 +490,16 @@ int bgb_destroy(bgb_handle* h) {
   if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
   DevBuf* bufs[] = {&h->verts_t, &h->tris_t, &h->verts_b, &h->tris_b, &h->geo_t, &h->geo_b, &h->bnd_t, &h->bnd_b,
                     &h->rec_t, &h->rec_b, &h->cls_count, &h->cls_off, &h->ent_tau, &h->ent_sigma, &h->ent_cls, &h->ent_mask, &h->geodf_t, &h->geodf_b,
-                    &h->sing_L, &h->err, &h->plan_i, &h->plan_l, &h->plan_d, &h->plan_f, &h->far_items, &h->far_const, &h->df_tab, &h->stage[0], &h->stage[1],
+                    &h->sing_L, &h->err, &h->plan_i[0], &h->plan_l[0], &h->plan_d[0], &h->plan_f[0], &h->far_items[0], &h->far_const[0], &h->plan_i[1], &h->plan_l[1], &h->plan_d[1], &h->plan_f[1], &h->far_items[1], &h->far_const[1], &h->df_tab, &h->stage[0], &h->stage[1], &h->tplan_i, &h->tplan_l, &h->tplan_d, &h->tplan_f,
                     &h->diag_a, &h->diag_b, &h->diag_c, &h->diag_d};
   for (DevBuf* b : bufs) b->release();
-  for (int i = 0; i < 8; ++i)
+  for (int i = 0; i < 8; ++i) {
     if (h->ev[i]) cudaEventDestroy(h->ev[i]);
+    if (h->ev2[i]) cudaEventDestroy(h->ev2[i]);
+  }
+  for (int i = 0; i < 2; ++i)
+    if (h->ring_ev[i]) cudaEventDestroy(h->ring_ev[i]);
+  if (h->ring) cudaFreeHost(h->ring);
   if (h->stream) cudaStreamDestroy(h->stream);
   if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
   if (h->abort_host) cudaFreeHost((void*)h->abort_host);
@@ -747,11 +670,174 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
   }
 
   RuleTable R = make_rules();
+  const FarConst K = make_farconst(opp, R, qsel);
+  const int gen = far_generic_q(K.qt, K.qb);
+  const bool same = same_space(test, trial);
+  const int64_t ncols = trial->nfun;
+
+  // Output blocks.  A device output is one block.  A host output is produced in blocks of
+  // columns (trial functions): the output is column-major, so each block is one contiguous
+  // range of the host matrix (when ld == nrows) and its copy one linear DMA.  Blocks are sized
+  // to the HBM budget with two device staging buffers, and a large output is cut into about
+  // 16 blocks (of at least 64 MiB) so that every copy but the last overlaps the far kernel of
+  // the next block.
+  size_t freeb = 0, totalb = 0;
+  cudaMemGetInfo(&freeb, &totalb);
+  const int64_t budget = h->cfg.hbm_budget_bytes > 0 ? h->cfg.hbm_budget_bytes : (int64_t)(0.9 * (double)freeb);
+  const int64_t per_col = (int64_t)esz * nrows;
+  int64_t cols_per_block = ncols;
+  if (host_out) {
+    cols_per_block = std::max<int64_t>(1, budget / std::max<int64_t>(1, 4 * per_col));
+    const int64_t overlap_cols = std::max<int64_t>((ncols + 15) / 16, ((int64_t)64 << 20) / std::max<int64_t>(1, per_col));
+    cols_per_block = std::min(std::min(cols_per_block, overlap_cols), ncols);
+  }
+  const int nblocks = (int)((ncols + cols_per_block - 1) / cols_per_block);
+  st.out_blocks = nblocks;
+
+  // Host tile planning depends on the spaces only: it runs on worker threads while the device
+  // uploads, classifies and integrates the singular pairs.
+  const bool pinned_cfg = h->cfg.tile_config >= 0;
+  if (pinned_cfg && h->cfg.tile_config >= kNumTileCfgs) { set_error("tile_config %d out of range", h->cfg.tile_config); return BGB_ERR_INVALID; }
+  std::vector<int> prefs;
+  if (pinned_cfg) prefs.push_back(h->cfg.tile_config);
+  else if (precision == BGB_PREC_MIXED) prefs.assign(kPrefMixed, kPrefMixed + kNumPrefMixed);
+  else prefs.assign(kPrefFp64, kPrefFp64 + kNumPrefFp64);
+  int smem_max = 0;
+  cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
+  struct Plans {
+    HostPlan test;                 // test side, all rows of the window
+    std::vector<HostPlan> trial;   // trial side per output block
+    TileCfg tc{};
+    int cfg_id = -1;
+    size_t smem = 0;
+    std::string err;
+    double ms = 0;
+  } PL;
+  const int nth = planner_threads();
+  const int target_occ = far_target_ctas_per_sm(precision);
+  auto plan_all = [&]() {
+    const auto t0 = clk::now();
+    cudaSetDevice(h->device);  // occupancy queries from this thread
+    const Supports St = build_supports(test);
+    const Supports Sb_own = same ? Supports() : build_supports(trial);
+    const Supports& Sb = same ? St : Sb_own;
+    const std::vector<int> rank_t = morton_rank(test);
+    const std::vector<int> rank_b = same ? rank_t : morton_rank(trial);
+    const std::vector<int> ord_t = order_functions(St, rank_t, (int)row0, (int)(row0 + nrows));
+    std::vector<std::vector<int>> ord_b(nblocks);
+    for (int b = 0; b < nblocks; ++b) {
+      const int64_t c0 = (int64_t)b * cols_per_block, c1 = std::min(ncols, c0 + cols_per_block);
+      ord_b[b] = order_functions(Sb, rank_b, (int)c0, (int)c1);
+    }
+    size_t smem = 0;
+    for (int id : prefs) {
+      const TileCfg tc = kTileCfgs[id];
+      PL.test = HostPlan();
+      plan_test_side_par(St, ord_t, tc.FM, row0, PL.test, nth);
+      PL.trial.assign(nblocks, HostPlan());
+      TilePlan probe{};
+      probe.FM = tc.FM; probe.FN = tc.FN; probe.SC = tc.SC; probe.MAXS = PL.test.MAXS;
+      probe.tmax = std::max(1, PL.test.tmax);
+      for (int b = 0; b < nblocks; ++b) {
+        plan_trial_side_par(Sb, ord_b[b], tc.FN, tc.SC, PL.trial[b], nth);
+        probe.gmax = std::max(probe.gmax, PL.trial[b].gmax);
+        probe.gsmax = std::max(probe.gsmax, PL.trial[b].gsmax);
+        probe.nmax = std::max(probe.nmax, std::max(1, PL.trial[b].nmax));
+      }
+      smem = far_smem_bytes(precision, K.qt, K.qb, probe);
+      // Occupancy: when the widest test tile pushes shared memory past what the kernel's
+      // CTAs per SM allow, cap the triangles per test tile at the largest count that fits.
+      int occ = 0;
+      if (smem <= (size_t)smem_max && far_persistent_occupancy(precision, K.op_kind, gen, smem, &occ) == 0 &&
+          occ >= 1 && occ < target_occ) {
+        int cap = -1;
+        for (int t = probe.tmax - 1; t >= std::max(1, PL.test.MAXS); --t) {
+          TilePlan q = probe;
+          q.tmax = t;
+          const size_t sm = far_smem_bytes(precision, K.qt, K.qb, q);
+          int o = 0;
+          if (far_persistent_occupancy(precision, K.op_kind, gen, sm, &o) == 0 && o >= target_occ) {
+            cap = t;
+            break;
+          }
+        }
+        if (cap > 0) {
+          PL.test = HostPlan();
+          plan_test_side_par(St, ord_t, tc.FM, row0, PL.test, nth, cap);
+          probe.MAXS = PL.test.MAXS;
+          probe.tmax = std::max(1, PL.test.tmax);
+          smem = far_smem_bytes(precision, K.qt, K.qb, probe);
+        }
+      }
+      occ = 0;
+      if (smem <= (size_t)smem_max && far_persistent_occupancy(precision, K.op_kind, gen, smem, &occ) == 0 && occ >= 1) {
+        PL.cfg_id = id;
+        PL.tc = tc;
+        PL.smem = smem;
+        break;
+      }
+    }
+    if (PL.cfg_id < 0) {
+      char buf[160];
+      snprintf(buf, sizeof buf, "no tile configuration fits in %d B of shared memory (last tried needs %zu B)",
+               smem_max, smem);
+      PL.err = buf;
+    }
+    PL.ms = std::chrono::duration<double, std::milli>(clk::now() - t0).count();
+  };
+  struct Joiner {
+    std::thread& t;
+    ~Joiner() {
+      if (t.joinable()) t.join();
+    }
+  };
+  std::thread planner(plan_all);
+  Joiner join_planner{planner};
+
+  // Host destination: pinned memory (cudaHostAlloc or registered) is copied into directly, and
+  // so is pageable memory when the GPU reaches it through the host page tables (a Grace host),
+  // after a host thread has faulted its pages in block by block (a DMA that faults pages runs
+  // several times slower than one into resident pages); other pageable memory goes through a
+  // pinned ring.
+  enum { DST_PINNED, DST_PAGEABLE, DST_RING } dst_kind = DST_PINNED;
+  if (host_out) {
+    cudaPointerAttributes attr{};
+    const bool pinned = cudaPointerGetAttributes(&attr, out) == cudaSuccess && attr.type == cudaMemoryTypeHost;
+    cudaGetLastError();
+    int ats = 0;
+    cudaDeviceGetAttribute(&ats, cudaDevAttrPageableMemoryAccessUsesHostPageTables, h->device);
+    dst_kind = pinned ? DST_PINNED : (ats && !(h->cfg.flags & BGB_CFG_PAGEABLE_VIA_RING) ? DST_PAGEABLE : DST_RING);
+  }
+  PrefaultProgress PF;
+  std::thread prefaulter;
+  if (dst_kind == DST_PAGEABLE) {
+    prefaulter = std::thread([&] {
+      const int nth = (int)std::min(16u, std::max(1u, std::thread::hardware_concurrency()));
+      for (int b = 0; b < nblocks && !PF.stop; ++b) {
+        const int64_t c0 = (int64_t)b * cols_per_block, nc = std::min(cols_per_block, ncols - c0);
+        char* base = (char*)out + (size_t)c0 * ld * esz;
+        if (ld == nrows) {
+          prefault_range(base, (size_t)nc * nrows * esz, nth);
+        } else {
+          for (int64_t c = 0; c < nc && !PF.stop; ++c) prefault_range(base + (size_t)c * ld * esz, (size_t)nrows * esz, 1);
+        }
+        PF.advance();
+      }
+    });
+  }
+  struct StopJoin {
+    PrefaultProgress& pf;
+    std::thread& t;
+    ~StopJoin() {
+      pf.stop = true;
+      if (t.joinable()) t.join();
+    }
+  } join_prefault{PF, prefaulter};
+
   cudaEventRecord(h->ev[0], h->stream);
   int launches = 0;
   if ((rc = upload_space(h, test, h->verts_t, h->tris_t, h->geo_t))) return rc;
   launches += test->nt > 0;
-  const bool same = same_space(test, trial);
   const Geo64* gt = h->geo_t.as<Geo64>();
   const Geo64* gb = gt;
   if (!same) {
@@ -767,12 +853,12 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
   // 2. singular / near pairs: FP64 kernel (plain path), double-float kernel (mixed path)
   if ((rc = h->sing_L.ensure(sizeof(double2) * 9 * std::max<int64_t>(1, nsing)))) return rc;
   const bool use_df = precision == BGB_PREC_MIXED && df_singular_ok(opp, max_edge(test), same ? max_edge(test) : max_edge(trial));
+  std::vector<float> df_host;  // uploaded asynchronously: lives until the end of the call
   if (use_df) {
-    std::vector<float> tab;
     DfTables M;
-    build_df_tables(qsel, R, tab, M);
-    if ((rc = h->df_tab.ensure(sizeof(float) * tab.size()))) return rc;
-    BGB_CUDA(cudaMemcpyAsync(h->df_tab.p, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice, h->stream));
+    build_df_tables(qsel, R, df_host, M);
+    if ((rc = h->df_tab.ensure(sizeof(float) * df_host.size()))) return rc;
+    BGB_CUDA(cudaMemcpyAsync(h->df_tab.p, df_host.data(), sizeof(float) * df_host.size(), cudaMemcpyHostToDevice, h->stream));
     if ((rc = h->geodf_t.ensure(sizeof(GeoDf) * std::max(1, test->nt))) ||
         (!same && (rc = h->geodf_b.ensure(sizeof(GeoDf) * std::max(1, trial->nt)))))
       return rc;
@@ -784,17 +870,13 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
                        h->ent_tau.as<int>(), h->ent_sigma.as<int>(), h->ent_cls.as<int8_t>(),
                        h->ent_mask.as<int16_t>(), nsing, h->sing_L.as<double2>(), h->abort_dev, h->num_sms, h->stream);
     launches += 1 + (same ? 0 : 1);
-    BGB_CUDA(cudaStreamSynchronize(h->stream));  // the host table buffer goes out of scope
   } else {
     launch_singular(opp, qsel, R, test->refspace, trial->refspace, gt, gb, h->ent_tau.as<int>(), h->ent_sigma.as<int>(),
                     h->ent_cls.as<int8_t>(), nsing, h->sing_L.as<double2>(), h->abort_dev, h->num_sms, h->stream);
   }
   BGB_CUDA(cudaGetLastError());
   cudaEventRecord(h->ev[2], h->stream);
-  if ((rc = check_abort(h))) return rc;
   // 3. far-pair records
-  FarConst K = make_farconst(opp, R, qsel);
-  const int gen = far_generic_q(K.qt, K.qb);
   const int rst = rec_stride(precision, K.qt, gen), rsb = rec_stride(precision, K.qb, gen);
   const size_t rsz = precision == BGB_PREC_MIXED ? sizeof(float) : sizeof(double);
   if ((rc = h->rec_t.ensure(rsz * rst * std::max(1, test->nt))) || (rc = h->rec_b.ensure(rsz * rsb * std::max(1, trial->nt))))
@@ -803,179 +885,225 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
   launch_prepare_rec(precision, 1, gen ? BGB_MAXQ : K.qb, gb, trial->nt, R, qsel.far_b, BGB_INV_4PI_D, h->rec_b.p, h->stream);
   launches += 2;
 
-  // 4. host plan
-  const bool pinned_cfg = h->cfg.tile_config >= 0;
-  if (pinned_cfg && h->cfg.tile_config >= kNumTileCfgs) { set_error("tile_config %d out of range", h->cfg.tile_config); return BGB_ERR_INVALID; }
-  std::vector<int> prefs;
-  if (pinned_cfg) prefs.push_back(h->cfg.tile_config);
-  else if (precision == BGB_PREC_MIXED) prefs.assign(std::begin(kPrefMixed), std::end(kPrefMixed));
-  else prefs.assign(std::begin(kPrefFp64), std::end(kPrefFp64));
-  int smem_max = 0;
-  cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
-  int cfg_id = -1;
-  Supports St = build_supports(test);
-  Supports Sb = same ? St : build_supports(trial);
-  std::vector<int> rank_t = morton_rank(test);
-  std::vector<int> rank_b = same ? rank_t : morton_rank(trial);
-  std::vector<int> ord_b = order_functions(Sb, rank_b, 0, trial->nfun);
-
-  // row blocks for out-of-core: bounded by the HBM budget
-  size_t freeb = 0, totalb = 0;
-  cudaMemGetInfo(&freeb, &totalb);
-  int64_t budget = h->cfg.hbm_budget_bytes > 0 ? h->cfg.hbm_budget_bytes : (int64_t)(0.9 * (double)freeb);
-  int64_t rows_per_block = nrows;
-  if (host_out) {
-    int64_t per_row = (int64_t)esz * trial->nfun;
-    rows_per_block = std::max<int64_t>(1, (budget / 2) / std::max<int64_t>(1, per_row));
-    rows_per_block = std::min(rows_per_block, nrows);
+  // 4. the host plan (joined here) and the test-side tables, uploaded once
+  planner.join();
+  st.ms_plan = PL.ms;
+  if (PL.cfg_id < 0) {
+    cudaStreamSynchronize(h->stream);
+    set_error("%s", PL.err.c_str());
+    return BGB_ERR_CAPACITY;
   }
-  st.row_blocks = (int)((nrows + rows_per_block - 1) / rows_per_block);
+  st.tile_config = PL.cfg_id;
+  const TileCfg tc = PL.tc;
+  const size_t smem = PL.smem;
+  const HostPlan& PT = PL.test;
+  std::vector<int> TI;
+  std::vector<float> TF;
+  auto cat_i = [&](std::vector<int>& dst, const std::vector<int>& v) { size_t o = dst.size(); dst.insert(dst.end(), v.begin(), v.end()); return o; };
+  const size_t o_tb_off = cat_i(TI, PT.tb_off), o_tb_tris = cat_i(TI, PT.tb_tris), o_tb_fn = cat_i(TI, PT.tb_fn_off),
+               o_fs_off = cat_i(TI, PT.fs_off), o_fs_code = cat_i(TI, PT.fs_code);
+  TF.reserve(PT.fs_coef.size());
+  for (double v : PT.fs_coef) TF.push_back((float)v);
+  if ((rc = h->tplan_i.ensure(sizeof(int) * std::max<size_t>(1, TI.size()))) ||
+      (rc = h->tplan_l.ensure(sizeof(int64_t) * std::max<size_t>(1, PT.rows.size()))) ||
+      (rc = h->tplan_d.ensure(sizeof(double) * std::max<size_t>(1, PT.fs_coef.size()))) ||
+      (rc = h->tplan_f.ensure(sizeof(float) * std::max<size_t>(1, TF.size()))))
+    return rc;
+  if ((rc = upload(h, h->tplan_i, TI, 0)) || (rc = upload(h, h->tplan_l, PT.rows, 0)) ||
+      (rc = upload(h, h->tplan_d, PT.fs_coef, 0)) || (rc = upload(h, h->tplan_f, TF, 0)))
+    return rc;
+  int per_sm = 0;
+  if ((rc = far_persistent_occupancy(precision, K.op_kind, gen, smem, &per_sm))) return rc;
+  const int ntb = (int)PT.tb_off.size() - 1;
+
   double ms_far = 0, ms_copy = 0;
   int64_t pairs_computed = 0;
-  for (int64_t r0 = row0; r0 < row0 + nrows; r0 += rows_per_block) {
-    const int64_t nr = std::min(rows_per_block, row0 + nrows - r0);
-    HostPlan P;
-    std::vector<int> ord_t = order_functions(St, rank_t, (int)r0, (int)(r0 + nr));
-    TileCfg tc{};
-    size_t smem = 0;
-    for (size_t pi_ = 0; pi_ < prefs.size(); ++pi_) {
-      if (cfg_id >= 0 && prefs[pi_] != cfg_id) continue;  // later row blocks keep the first block's choice
-      tc = kTileCfgs[prefs[pi_]];
-      P = HostPlan();
-      plan_test_side(St, ord_t, tc.FM, host_out ? r0 : row0, P);
-      plan_trial_side(Sb, ord_b, tc.FN, tc.SC, P);
-      TilePlan probe{};
-      probe.FM = tc.FM; probe.FN = tc.FN; probe.SC = tc.SC; probe.MAXS = P.MAXS;
-      probe.gmax = P.gmax; probe.gsmax = P.gsmax;
-      probe.tmax = std::max(1, P.tmax); probe.nmax = std::max(1, P.nmax);
-      smem = far_smem_bytes(precision, K.qt, K.qb, probe);
-      if (smem <= (size_t)smem_max) { cfg_id = prefs[pi_]; break; }
-    }
-    if (cfg_id < 0 || smem > (size_t)smem_max) {
-      set_error("no tile configuration fits in %d B of shared memory (last tried needs %zu B)", smem_max, smem);
-      return BGB_ERR_CAPACITY;
-    }
-    st.tile_config = cfg_id;
-    for (size_t a = 0; a + 1 < P.tb_off.size(); ++a)
-      for (size_t b = 0; b + 1 < P.bb_off.size(); ++b)
-        pairs_computed += (int64_t)(P.tb_off[a + 1] - P.tb_off[a]) * (P.bb_off[b + 1] - P.bb_off[b]);
-    // pack int arrays
+  bool pending[2] = {false, false};
+  auto harvest = [&](int slot) {  // times of the block that last used `slot` (complete)
+    if (!pending[slot]) return;
+    ms_far += event_ms(h->ev2[slot * 4 + 0], h->ev2[slot * 4 + 1]);
+    if (host_out) ms_copy += event_ms(h->ev2[slot * 4 + 2], h->ev2[slot * 4 + 3]);
+    pending[slot] = false;
+  };
+  struct SlotHost {  // host copies of a block's tables, alive until the slot is reused
     std::vector<int> I;
-    std::vector<int64_t> Lg;
-    std::vector<double> D;
-    auto put_i = [&](const std::vector<int>& v) { size_t o = I.size(); I.insert(I.end(), v.begin(), v.end()); return o; };
-    auto put_l = [&](const std::vector<int64_t>& v) { size_t o = Lg.size(); Lg.insert(Lg.end(), v.begin(), v.end()); return o; };
-    auto put_d = [&](const std::vector<double>& v) { size_t o = D.size(); D.insert(D.end(), v.begin(), v.end()); return o; };
-    size_t o_tb_off = put_i(P.tb_off), o_tb_tris = put_i(P.tb_tris), o_tb_fn = put_i(P.tb_fn_off), o_fs_off = put_i(P.fs_off),
-           o_fs_code = put_i(P.fs_code), o_bb_off = put_i(P.bb_off), o_bb_tris = put_i(P.bb_tris), o_bb_fn = put_i(P.bb_fn_off),
-           o_bb_ch = put_i(P.bb_chunk_off), o_ch_grp = put_i(P.ch_grp_off), o_grp_fn = put_i(P.grp_fn),
-           o_grp_sup = put_i(P.grp_sup_off), o_gs_code = put_i(P.gs_code);
-    size_t o_rows = put_l(P.rows), o_cols = put_l(P.cols);
-    size_t o_fs_coef = put_d(P.fs_coef), o_gs_coef = put_d(P.gs_coef);
-    std::vector<float> F32;
-    F32.reserve(P.fs_coef.size() + P.gs_coef.size());
-    for (double v : P.fs_coef) F32.push_back((float)v);
-    const size_t o_gs32 = F32.size();
-    for (double v : P.gs_coef) F32.push_back((float)v);
-    if ((rc = h->plan_i.ensure(sizeof(int) * std::max<size_t>(1, I.size()))) ||
-        (rc = h->plan_l.ensure(sizeof(int64_t) * std::max<size_t>(1, Lg.size()))) ||
-        (rc = h->plan_d.ensure(sizeof(double) * std::max<size_t>(1, D.size()))) ||
-        (rc = h->plan_f.ensure(sizeof(float) * std::max<size_t>(1, F32.size()))))
-      return rc;
-    BGB_CUDA(cudaStreamSynchronize(h->stream));  // previous block's plan arrays no longer in use
-    if ((rc = upload(h, h->plan_i, I, 0)) || (rc = upload(h, h->plan_l, Lg, 0)) || (rc = upload(h, h->plan_d, D, 0)) ||
-        (rc = upload(h, h->plan_f, F32, 0)))
-      return rc;
-    const int* pi = h->plan_i.as<int>();
-    const int64_t* pl = h->plan_l.as<int64_t>();
-    const double* pd = h->plan_d.as<double>();
-    TilePlan T{};
+    std::vector<int64_t> L;
+    std::vector<float> F;
+    std::vector<int4> items;
+    TilePlan T;
+  };
+  SlotHost slot_host[2];
+  // upload the trial-side tables of block b into its slot and launch the far kernel
+  auto enqueue_block = [&](int b) -> int {
+    const int slot = b & 1;
+    const int64_t c0 = (int64_t)b * cols_per_block;
+    const int64_t nc = std::min(cols_per_block, ncols - c0);
+    const HostPlan& PB = PL.trial[b];
+    if (pending[slot]) {  // block b-2 used this slot: its kernel and copy must be complete
+      BGB_CUDA(cudaEventSynchronize(h->ev2[slot * 4 + (host_out ? 3 : 1)]));
+      harvest(slot);
+    }
+    SlotHost& H = slot_host[slot];
+    H.I.clear();
+    H.L.clear();
+    H.F.clear();
+    H.items.clear();
+    const size_t o_bb_off = cat_i(H.I, PB.bb_off), o_bb_tris = cat_i(H.I, PB.bb_tris), o_bb_fn = cat_i(H.I, PB.bb_fn_off),
+                 o_bb_ch = cat_i(H.I, PB.bb_chunk_off), o_ch_grp = cat_i(H.I, PB.ch_grp_off),
+                 o_grp_fn = cat_i(H.I, PB.grp_fn), o_grp_sup = cat_i(H.I, PB.grp_sup_off),
+                 o_gs_code = cat_i(H.I, PB.gs_code);
+    H.L.reserve(PB.cols.size());
+    for (int64_t c : PB.cols) H.L.push_back(c - (host_out ? c0 : 0));  // staging columns start at c0
+    H.F.reserve(PB.gs_coef.size());
+    for (double v : PB.gs_coef) H.F.push_back((float)v);
+    const size_t o_gs_coef = 0;
+    pairs_computed += (int64_t)PT.tb_tris.size() * (int64_t)PB.bb_tris.size();
+    const int nbb = (int)PB.bb_off.size() - 1;
+    H.items.reserve((size_t)ntb * nbb);  // tiles, row block fastest (neighbouring rows of a column together)
+    for (int bn = 0; bn < nbb; ++bn)
+      for (int bm = 0; bm < ntb; ++bm) H.items.push_back(make_int4(0, bm, bn, 0));
+    int rc2;
+    if ((rc2 = h->plan_i[slot].ensure(sizeof(int) * std::max<size_t>(1, H.I.size()))) ||
+        (rc2 = h->plan_l[slot].ensure(sizeof(int64_t) * std::max<size_t>(1, H.L.size()))) ||
+        (rc2 = h->plan_d[slot].ensure(sizeof(double) * std::max<size_t>(1, PB.gs_coef.size()))) ||
+        (rc2 = h->plan_f[slot].ensure(sizeof(float) * std::max<size_t>(1, H.F.size()))) ||
+        (rc2 = h->far_items[slot].ensure(sizeof(int4) * std::max<size_t>(1, H.items.size()))) ||
+        (rc2 = h->far_const[slot].ensure(sizeof(FarConst) + sizeof(TilePlan) + sizeof(int) * 4)))
+      return rc2;
+    if (host_out && (rc2 = h->stage[slot].ensure(esz * (size_t)cols_per_block * nrows))) return rc2;
+    if ((rc2 = upload(h, h->plan_i[slot], H.I, 0)) || (rc2 = upload(h, h->plan_l[slot], H.L, 0)) ||
+        (rc2 = upload(h, h->plan_d[slot], PB.gs_coef, 0)) || (rc2 = upload(h, h->plan_f[slot], H.F, 0)))
+      return rc2;
+    const int* ti = h->tplan_i.as<int>();
+    const int* bi = h->plan_i[slot].as<int>();
+    TilePlan& T = H.T;
+    T = TilePlan{};
     T.rec_t = h->rec_t.p;
     T.rec_b = h->rec_b.p;
     T.bnd_t = h->bnd_t.as<float4>();
     T.bnd_b = h->bnd_b.as<float4>();
-    T.n_tblocks = (int)P.tb_off.size() - 1;
-    T.tb_off = pi + o_tb_off;
-    T.tb_tris = pi + o_tb_tris;
-    T.tb_fn_off = pi + o_tb_fn;
-    T.fs_off = pi + o_fs_off;
-    T.fs_code = pi + o_fs_code;
-    T.fs_coef = pd + o_fs_coef;
-    T.rows = pl + o_rows;
-    T.n_bblocks = (int)P.bb_off.size() - 1;
-    T.bb_off = pi + o_bb_off;
-    T.bb_tris = pi + o_bb_tris;
-    T.bb_fn_off = pi + o_bb_fn;
-    T.bb_chunk_off = pi + o_bb_ch;
-    T.ch_grp_off = pi + o_ch_grp;
-    T.grp_fn = pi + o_grp_fn;
-    T.grp_sup_off = pi + o_grp_sup;
-    T.gs_code = pi + o_gs_code;
-    T.gs_coef = pd + o_gs_coef;
-    T.fs_coef32 = h->plan_f.as<float>();
-    T.gs_coef32 = h->plan_f.as<float>() + o_gs32;
-    T.gmax = P.gmax;
-    T.gsmax = P.gsmax;
-    T.cols = pl + o_cols;
+    T.n_tblocks = ntb;
+    T.tb_off = ti + o_tb_off;
+    T.tb_tris = ti + o_tb_tris;
+    T.tb_fn_off = ti + o_tb_fn;
+    T.fs_off = ti + o_fs_off;
+    T.fs_code = ti + o_fs_code;
+    T.fs_coef = h->tplan_d.as<double>();
+    T.fs_coef32 = h->tplan_f.as<float>();
+    T.rows = h->tplan_l.as<int64_t>();
+    T.n_bblocks = nbb;
+    T.bb_off = bi + o_bb_off;
+    T.bb_tris = bi + o_bb_tris;
+    T.bb_fn_off = bi + o_bb_fn;
+    T.bb_chunk_off = bi + o_bb_ch;
+    T.ch_grp_off = bi + o_ch_grp;
+    T.grp_fn = bi + o_grp_fn;
+    T.grp_sup_off = bi + o_grp_sup;
+    T.gs_code = bi + o_gs_code;
+    T.gs_coef = h->plan_d[slot].as<double>() + o_gs_coef;
+    T.gs_coef32 = h->plan_f[slot].as<float>();
+    T.cols = h->plan_l[slot].as<int64_t>();
+    T.gmax = PB.gmax;
+    T.gsmax = PB.gsmax;
     T.sing_off = h->cls_off.as<int64_t>();
     T.sing_sigma = h->ent_sigma.as<int>();
     T.sing_L = h->sing_L.as<double2>();
     T.FM = tc.FM;
     T.FN = tc.FN;
     T.SC = tc.SC;
-    T.MAXS = P.MAXS;
-    T.tmax = std::max(1, P.tmax);
-    T.nmax = std::max(1, P.nmax);
+    T.MAXS = PT.MAXS;
+    T.tmax = std::max(1, PT.tmax);
+    T.nmax = std::max(1, PB.nmax);
     T.out_c64 = c64;
     T.abort_flag = h->abort_dev;
-    void* dst = out;
-    int64_t dld = ld;
-    if (host_out) {
-      if ((rc = h->stage[0].ensure(esz * (size_t)nr * trial->nfun))) return rc;
-      dst = h->stage[0].p;
-      dld = nr;
-    }
-    T.out = dst;
-    T.ld = dld;
-    cudaEventRecord(h->ev[3], h->stream);
-    // the single problem runs through the same persistent work-queue kernel as batches
-    // (one far kernel, so batched and single assemblies are bit-identical); tiles are
-    // queued row block fastest so concurrent CTAs write neighbouring rows of a column
-    std::vector<int4> items;
-    items.reserve((size_t)T.n_tblocks * T.n_bblocks);
-    for (int bn = 0; bn < T.n_bblocks; ++bn)
-      for (int bm = 0; bm < T.n_tblocks; ++bm) items.push_back(make_int4(0, bm, bn, 0));
-    if ((rc = h->far_items.ensure(sizeof(int4) * std::max<size_t>(1, items.size()))) ||
-        (rc = h->far_const.ensure(sizeof(FarConst) + sizeof(TilePlan) + sizeof(int) * 4)))
-      return rc;
-    FarConst* dK = (FarConst*)h->far_const.p;
-    TilePlan* dT = (TilePlan*)((char*)h->far_const.p + sizeof(FarConst));
-    int* dctr = (int*)((char*)h->far_const.p + sizeof(FarConst) + sizeof(TilePlan));
+    T.out = host_out ? h->stage[slot].p : out;
+    T.ld = host_out ? nrows : ld;
+    FarConst* dK = (FarConst*)h->far_const[slot].p;
+    TilePlan* dT = (TilePlan*)((char*)h->far_const[slot].p + sizeof(FarConst));
+    int* dctr = (int*)((char*)h->far_const[slot].p + sizeof(FarConst) + sizeof(TilePlan));
     BGB_CUDA(cudaMemcpyAsync(dK, &K, sizeof(FarConst), cudaMemcpyHostToDevice, h->stream));
     BGB_CUDA(cudaMemcpyAsync(dT, &T, sizeof(TilePlan), cudaMemcpyHostToDevice, h->stream));
-    if (!items.empty())
-      BGB_CUDA(cudaMemcpyAsync(h->far_items.p, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice, h->stream));
+    if (!H.items.empty())
+      BGB_CUDA(cudaMemcpyAsync(h->far_items[slot].p, H.items.data(), sizeof(int4) * H.items.size(),
+                               cudaMemcpyHostToDevice, h->stream));
     BGB_CUDA(cudaMemsetAsync(dctr, 0, sizeof(int), h->stream));
-    int per_sm = 0;
-    if ((rc = far_persistent_occupancy(precision, K.op_kind, gen, smem, &per_sm))) return rc;
-    const int ctas = (int)std::min<int64_t>((int64_t)items.size(), (int64_t)std::max(1, per_sm) * h->num_sms);
-    if ((rc = launch_far_persistent(precision, K.op_kind, gen, dK, dT, (const int4*)h->far_items.p, (int)items.size(),
-                                    dctr, smem, std::max(1, ctas), h->abort_dev, h->stream)))
-      return rc;
+    const int ctas = (int)std::min<int64_t>((int64_t)H.items.size(), (int64_t)std::max(1, per_sm) * h->num_sms);
+    BGB_CUDA(cudaEventRecord(h->ev2[slot * 4 + 0], h->stream));
+    if ((rc2 = launch_far_persistent(precision, K.op_kind, gen, dK, dT, (const int4*)h->far_items[slot].p,
+                                     (int)H.items.size(), dctr, smem, std::max(1, ctas), h->abort_dev, h->stream)))
+      return rc2;
     ++launches;
-    cudaEventRecord(h->ev[4], h->stream);
-    BGB_CUDA(cudaStreamSynchronize(h->stream));  // plan, items and constants are reused by the next row block
-    if (host_out) {
-      char* hdst = (char*)out + (size_t)(r0 - row0) * esz;
-      BGB_CUDA(cudaMemcpy2DAsync(hdst, (size_t)ld * esz, dst, (size_t)nr * esz, (size_t)nr * esz, (size_t)trial->nfun,
-                                 cudaMemcpyDeviceToHost, h->stream));
+    BGB_CUDA(cudaEventRecord(h->ev2[slot * 4 + 1], h->stream));
+    pending[slot] = true;
+    (void)nc;
+    return 0;
+  };
+  // copy block b to the host on the side stream; pageable destinations go through the pinned ring
+  auto copy_block = [&](int b) -> int {
+    const int slot = b & 1;
+    const int64_t c0 = (int64_t)b * cols_per_block;
+    const int64_t nc = std::min(cols_per_block, ncols - c0);
+    cudaStream_t cs = h->copy_stream;
+    if (dst_kind == DST_PAGEABLE) PF.wait_for(b + 1);  // pages of this block are resident
+    BGB_CUDA(cudaStreamWaitEvent(cs, h->ev2[slot * 4 + 1], 0));
+    BGB_CUDA(cudaEventRecord(h->ev2[slot * 4 + 2], cs));
+    char* hdst = (char*)out + (size_t)c0 * ld * esz;
+    const char* src = (const char*)h->stage[slot].p;
+    const size_t seg = (size_t)nrows * esz;  // one column of the block
+    const size_t dpitch = (size_t)ld * esz;
+    if (dst_kind != DST_RING) {
+      if (dpitch == seg)
+        BGB_CUDA(cudaMemcpyAsync(hdst, src, seg * nc, cudaMemcpyDeviceToHost, cs));
+      else
+        BGB_CUDA(cudaMemcpy2DAsync(hdst, dpitch, src, seg, seg, (size_t)nc, cudaMemcpyDeviceToHost, cs));
+    } else {
+      int rc2;
+      const size_t ring_half =
+          std::max(seg, (size_t)(h->cfg.pinned_ring_bytes > 0 ? h->cfg.pinned_ring_bytes : ((int64_t)512 << 20)));
+      if ((rc2 = ensure_ring(h, 2 * ring_half))) return rc2;
+      const int64_t cols_per_chunk = std::max<int64_t>(1, (int64_t)(ring_half / seg));
+      const int64_t nchunks = (nc + cols_per_chunk - 1) / cols_per_chunk;
+      auto host_copy = [&](int64_t k) {
+        const int64_t k0 = k * cols_per_chunk, kn = std::min(cols_per_chunk, nc - k0);
+        const char* r = (const char*)h->ring + (size_t)(k & 1) * ring_half;
+        parallel_copy_columns(hdst + (size_t)k0 * dpitch, dpitch, r, seg, seg, kn);
+      };
+      for (int64_t k = 0; k < nchunks; ++k) {
+        const int64_t k0 = k * cols_per_chunk, kn = std::min(cols_per_chunk, nc - k0);
+        BGB_CUDA(cudaMemcpyAsync((char*)h->ring + (size_t)(k & 1) * ring_half, src + (size_t)k0 * seg, seg * kn,
+                                 cudaMemcpyDeviceToHost, cs));
+        BGB_CUDA(cudaEventRecord(h->ring_ev[k & 1], cs));
+        if (k > 0) {  // copy out the previous chunk while this one is in flight
+          BGB_CUDA(cudaEventSynchronize(h->ring_ev[(k - 1) & 1]));
+          host_copy(k - 1);
+        }
+      }
+      BGB_CUDA(cudaEventSynchronize(h->ring_ev[(nchunks - 1) & 1]));
+      host_copy(nchunks - 1);
     }
-    cudaEventRecord(h->ev[5], h->stream);
-    BGB_CUDA(cudaEventSynchronize(h->ev[5]));
-    if ((rc = check_abort(h))) return rc;
-    ms_far += event_ms(h->ev[3], h->ev[4]);
-    ms_copy += event_ms(h->ev[4], h->ev[5]);
+    BGB_CUDA(cudaEventRecord(h->ev2[slot * 4 + 3], cs));
+    return 0;
+  };
+  const auto t_pipe = clk::now();
+  auto drain = [&](int code) {  // the slots' host tables must outlive uploads still in flight
+    cudaStreamSynchronize(h->stream);
+    cudaStreamSynchronize(h->copy_stream);
+    return code;
+  };
+  if ((rc = enqueue_block(0))) return drain(rc);
+  for (int b = 0; b < nblocks; ++b) {
+    if (b + 1 < nblocks && (rc = enqueue_block(b + 1))) return drain(rc);
+    if (host_out && (rc = copy_block(b))) return drain(rc);
+    if ((rc = check_abort(h))) return drain(rc);
   }
+  BGB_CUDA(cudaStreamSynchronize(h->stream));
+  BGB_CUDA(cudaStreamSynchronize(h->copy_stream));
+  harvest(0);
+  harvest(1);
+  const double ms_pipe = std::chrono::duration<double, std::milli>(clk::now() - t_pipe).count();
+  if ((rc = check_abort(h))) return rc;
+  st.ms_copy = ms_copy;
+  st.ms_pipeline = ms_pipe;
   BGB_CUDA(cudaGetLastError());
   if (!host_out && s != h->stream) {
     BGB_CUDA(cudaEventRecord(h->ev[6], h->stream));
@@ -987,7 +1115,6 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
   st.ms_classify = event_ms(h->ev[0], h->ev[1]);
   st.ms_singular = event_ms(h->ev[1], h->ev[2]);
   st.ms_far = ms_far;
-  st.ms_copy = ms_copy;
   if (stats) {
     std::vector<int8_t> cls((size_t)nsing);
     if (nsing) BGB_CUDA(cudaMemcpy(cls.data(), h->ent_cls.p, nsing, cudaMemcpyDeviceToHost));

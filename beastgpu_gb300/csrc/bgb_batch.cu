@@ -494,7 +494,7 @@ int bgb_batch_create(bgb_handle* h, int32_t n, const bgb_problem* problems, int3
   bgb_stats s{};
   s.pairs_total = pairs_total;
   s.tile_config = best_cfg;
-  s.row_blocks = best_sched;  // batches report the chosen work-queue schedule here
+  s.schedule = best_sched;
   s.ms_far = best_ms;
   s.kernel_launches = 0;
   B->stats = s;

@@ -70,6 +70,10 @@ int far_persistent_occupancy(int precision, int op_kind, int generic, size_t sme
 
 int far_generic_q(int qt, int qb) { return !(qt == 3 && qb == 4); }
 
+int far_target_ctas_per_sm(int precision) {
+  return precision == BGB_PREC_MIXED ? PMixed::kMinBlocks : PFp64::kMinBlocks;
+}
+
 int rec_stride(int precision, int q, int generic) {
   const int Q = generic ? BGB_MAXQ : q;
   return precision == BGB_PREC_MIXED ? 17 + 4 * Q : 13 + 4 * Q;

@@ -784,11 +784,24 @@ __global__ void k_far_pairs_diag(const __grid_constant__ FarConst K, const typen
   }
 }
 
+// The dynamic shared-memory limit of a kernel is set to the device maximum less its static
+// shared memory (not to one launch's size), so that concurrent callers never lower it under
+// each other's launches.
+template <class K>
+inline int max_dynamic_smem(K kern) {
+  int dev = 0, v = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  cudaFuncAttributes fa{};
+  if (cudaFuncGetAttributes(&fa, kern) != cudaSuccess) return v;
+  return v - (int)fa.sharedSizeBytes;
+}
+
 template <class P, int OP, int QT, int QB>
 int launch_persistent_t(const FarConst* Ks, const TilePlan* plans, const int4* items, int nitems, int* counter,
                         size_t smem_bytes, int ctas, const volatile int* abort_flag, cudaStream_t st) {
   auto kern = k_far_persistent<P, OP, QT, QB>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem(kern));
   if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(far persistent)");
   if (nitems <= 0) return 0;
   kern<<<ctas, kThreads, smem_bytes, st>>>(Ks, plans, items, nitems, counter, abort_flag);
@@ -799,7 +812,7 @@ int launch_persistent_t(const FarConst* Ks, const TilePlan* plans, const int4* i
 template <class P, int OP, int QT, int QB>
 int occupancy_t(size_t smem_bytes, int* per_sm) {
   cudaError_t e = cudaFuncSetAttribute(k_far_persistent<P, OP, QT, QB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem_bytes);
+                                       max_dynamic_smem(k_far_persistent<P, OP, QT, QB>));
   if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(far persistent)");
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_far_persistent<P, OP, QT, QB>, kThreads, smem_bytes);
   return e == cudaSuccess ? 0 : cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");

@@ -51,10 +51,15 @@ struct bgb_handle {
   // buffers
   bgb::DevBuf verts_t, tris_t, verts_b, tris_b, geo_t, geo_b, bnd_t, bnd_b, rec_t, rec_b;
   bgb::DevBuf cls_count, cls_off, ent_tau, ent_sigma, ent_cls, ent_mask, sing_L, err, geodf_t, geodf_b;
-  bgb::DevBuf plan_i, plan_l, plan_d, plan_f, far_items, far_const, df_tab;
+  bgb::DevBuf plan_i[2], plan_l[2], plan_d[2], plan_f[2], far_items[2], far_const[2], df_tab;
+  bgb::DevBuf tplan_i, tplan_l, tplan_d, tplan_f;  // test-side tile tables (shared by all output blocks)
   bgb::DevBuf stage[2];
   bgb::DevBuf diag_a, diag_b, diag_c, diag_d;
   cudaEvent_t ev[8] = {};
+  cudaEvent_t ev2[8] = {};   // per row-block slot: far start / end, copy start / end
+  cudaEvent_t ring_ev[2] = {};
+  void* ring = nullptr;      // pinned host staging ring
+  size_t ring_bytes = 0;
 };
 
 
@@ -93,8 +98,15 @@ FarConst make_farconst(const OpParams& op, const RuleTable& R, const QuadSel& qs
 std::vector<int> morton_rank(const bgb_space* s);
 Supports build_supports(const bgb_space* s);
 std::vector<int> order_functions(const Supports& S, const std::vector<int>& rank, int f_begin, int f_end);
-void plan_test_side(const Supports& S, const std::vector<int>& order, int FM, int64_t row0, HostPlan& P);
+// Test-side tiles: up to FM functions and at most tcap distinct triangles per tile.
+void plan_test_side(const Supports& S, const std::vector<int>& order, int FM, int64_t row0, HostPlan& P,
+                    int tcap = 1 << 30);
 void plan_trial_side(const Supports& S, const std::vector<int>& order, int FN, int SC, HostPlan& P);
+// The same plans built over ranges of blocks in up to nth threads (identical results).
+void plan_test_side_par(const Supports& S, const std::vector<int>& order, int FM, int64_t row0, HostPlan& P, int nth,
+                        int tcap = 1 << 30);
+void plan_trial_side_par(const Supports& S, const std::vector<int>& order, int FN, int SC, HostPlan& P, int nth);
+int planner_threads();
 bool same_space(const bgb_space* a, const bgb_space* b);
 // Largest triangle edge of a space (host), for the argument range of the double-float sincos.
 double max_edge(const bgb_space* s);

@@ -131,6 +131,8 @@ struct TilePlan {
 };
 
 size_t far_smem_bytes(int precision, int qt, int qb, const TilePlan& p);
+// CTAs per SM the far kernel is compiled for (__launch_bounds__ minimum blocks).
+int far_target_ctas_per_sm(int precision);
 // Persistent batched launch over a work queue of (problem, bm, bn) items (device arrays).
 int launch_far_persistent(int precision, int op_kind, int generic, const FarConst* Ks, const TilePlan* plans,
                           const int4* items, int nitems, int* counter, size_t smem_bytes, int ctas,

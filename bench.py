@@ -1,18 +1,27 @@
 """Benchmark of the dense Galerkin matrix fill on one GB300 (or N, one rank per GPU).
 
-Workload (default): Maxwell3D single layer (EFIE, alpha = -ik, beta = 1/(-ik)) on RWG over an
-icosphere of level 5 (20,480 triangles, 30,720 RWG functions), k = 2 pi * 4, default quadrature
-strategy (3 x 4-point far rule, Sauter-Schwab n = 4 for common face/edge/vertex).  Synthetic,
-seeded mesh built by the package; no dataset is involved.
+Workload (default, `--workload c2`): Maxwell3D single layer (EFIE, alpha = -ik, beta = 1/(-ik))
+on RWG over an icosphere of level 5 (20,480 triangles, 30,720 RWG functions), k = 2 pi * 4,
+default quadrature strategy (3 x 4-point far rule, Sauter-Schwab n = 4 for common
+face/edge/vertex).  Synthetic, seeded mesh built by the package; no dataset is involved.
 
-One step = one full assembly: upload of the space tables, pair classification, FP64
-singular / near-pair integrals, far-pair tiles with the gather write.  `value` is
-pair-interactions/s (nt * nb / step time) of the MIXED kernel with the output in HBM; the plain
-FP64 kernel's rate is reported beside it, and `e2e` is the same fill through the C ABI with
-the matrix copied into a pinned host buffer.  Errors of both kernels against the FP64 CPU
-oracle are measured on 1000 seeded rows.
+One step = one full assembly: upload of the space tables, pair classification, singular /
+near-pair integrals, far-pair tiles with the gather write.  `value` is pair-interactions/s
+(nt * nb / step time) of the MIXED kernel with the output in HBM; the plain FP64 kernel's rate
+is reported beside it, and `e2e` is the same fill through the public API with the matrix
+copied into a pinned host buffer (output blocks overlapped with the fill).  Errors of both
+kernels against the FP64 CPU oracle are measured on 1000 seeded rows.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+Other workloads print the same kind of line for their own configuration:
+  --workload c3   MFIE on RWG and Helmholtz single layer on Lagrange over two jittered
+                  96 x 96 coplanar plates 0.01 apart (36,864 triangles), k = 2 pi * 2
+  --workload c4   64 seeded ellipsoids (icosphere levels 1-4, axes U[0.5, 2], k U[1, 10]), EFIE,
+                  one batched persistent launch replayed from a CUDA graph vs 64 sequential
+                  plain FP64 assemblies
+  --workload c5   EFIE on an icosphere of level 6 (81,920 triangles, 122,880 RWG), k = 2 pi * 8,
+                  ComplexF32 output (121 GB) streamed to pinned host memory in output blocks
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c2|c3|c4|c5] [--impl reference]
 
 `--impl reference` times the CPU restatement of the reference algorithm (the oracle, OpenMP
 over all host cores) on a bounded row sample of the same workload.
@@ -139,10 +148,10 @@ def flush_l2(buf):
     buf.add_(1)
 
 
-def time_fill(bg, X, op, prec, steps, warmup, local, out="device", pinned=None):
+def time_fill(bg, X, op, prec, steps, warmup, local, out="device", pinned=None, cfg=None):
     """Per-step device time (CUDA events on the launching stream) of full assemblies."""
     import torch
-    cfg = bg.GPUConfiguration(precision=prec, device=local)
+    cfg = cfg or bg.GPUConfiguration(precision=prec, device=local)
     scratch = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")
     dt = np.complex64 if prec == "mixed" else np.complex128
     Zbuf = None
@@ -229,6 +238,200 @@ def run_profile_case(args):
     return 0
 
 
+def line_base(args, world, value, ms_step, dtype, config, **extra):
+    d = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+         "vs_baseline": None, "dtype": dtype, "data": "synthetic (seeded meshes built in-process)",
+         "config": config}
+    d.update(extra)
+    return d
+
+
+def oracle_rows_error(op, X, Zrows, rows, qs=None):
+    import oracle
+    import beastgpu_gb300 as bg
+    ref = oracle.assemble_rows(op, X, X, qs or bg.QuadStrat(), rows, nthreads=oracle.max_threads())
+    return rows_error(np.asarray(Zrows, dtype=np.complex128), ref)
+
+
+def run_c3(args):
+    """Near-singular stress: MFIE (RWG) and Helmholtz single layer (Lagrange) on two plates."""
+    import torch
+    import beastgpu_gb300 as bg
+    rank, world, local = dist_init(args.gpus)
+    mesh = bg.two_plates(96, jitter=0.3, seed=1, gap=0.01)
+    k = 2 * np.pi * 2
+    R, L = bg.raviartthomas(mesh), bg.lagrangec0d1(mesh)
+    cases = [("mfie_rwg", bg.Maxwell3D.doublelayer(wavenumber=k), R),
+             ("helmholtz_sl_lagrange", bg.Helmholtz3D.singlelayer(wavenumber=k), L)]
+    pairs = mesh.nt * mesh.nt
+    res = {}
+    tot_ms = {"mixed": 0.0, "fp64": 0.0}
+    launches = 0
+    with ClockSampler(local) as clocks:
+        for name, op, X in cases:
+            rows = np.sort(np.random.default_rng(3).choice(X.nfun, 200, replace=False)).astype(np.int32)
+            r = {"functions": X.nfun}
+            for prec in ("mixed", "fp64"):
+                ms, st, _, Z = time_fill(bg, X, op, prec, args.steps, args.warmup, local)
+                m = max_over_ranks(float(np.mean(ms)), world, local)
+                tot_ms[prec] += m
+                launches += sum(x["kernel_launches"] for x in st) if prec == "mixed" else 0
+                Zr = Z[:, torch.as_tensor(rows.astype(np.int64), device=Z.device)].T.cpu().numpy()
+                r[prec] = {"ms_per_step": m, "pairs_per_s": pairs / (m * 1e-3), "stats": st[-1]}
+                if rank == 0:
+                    if name.startswith("mfie"):
+                        r[prec]["max_abs_entry"] = float(np.abs(Zr).max())  # coplanar plates: exactly zero
+                    else:
+                        r[prec]["error_vs_oracle_200_rows"] = oracle_rows_error(op, X, Zr, rows)
+                del Z
+                torch.cuda.empty_cache()
+            res[name] = r
+    if rank != 0:
+        return 0
+    value = world * 2 * pairs / (tot_ms["mixed"] * 1e-3)
+    cfg = {"workload": "MFIE (RWG) + Helmholtz SL (Lagrange, interior vertices) on two jittered 96x96 plates, "
+                       "gap 0.01, k=2*pi*2", "triangles": mesh.nt, "pairs_per_step": 2 * pairs,
+           "l2": "outputs > L2; a 256 MiB buffer is written between timed steps"}
+    print(json.dumps(line_base(args, world, value, tot_ms["mixed"], "f32 far + double-float singular/near (mixed)",
+                               cfg, fp64_value=world * 2 * pairs / (tot_ms["fp64"] * 1e-3), cases=res,
+                               clocks=clocks.summary(), gpu_launches=launches)))
+    return 0
+
+
+def run_c4(args):
+    """64 uneven ellipsoids: one batched persistent launch (CUDA graph) vs 64 sequential assemblies."""
+    import torch
+    import beastgpu_gb300 as bg
+    rank, world, local = dist_init(args.gpus)
+    batch = bg.ellipsoid_batch(64, seed=2)
+    probs = []
+    for mesh, k in batch:
+        X = bg.raviartthomas(mesh)
+        probs.append((bg.Maxwell3D.singlelayer(wavenumber=k), X, X))
+    pairs = sum(m.nt * m.nt for m, _ in batch)
+    stream = torch.cuda.current_stream(local)
+    out = {}
+    with ClockSampler(local) as clocks:
+        for prec in ("mixed", "fp64"):
+            B = bg.Batch(probs, bg.GPUConfiguration(precision=prec, device=local), out="device", autotune=True)
+            for _ in range(args.warmup):
+                B.run()
+            torch.cuda.synchronize()
+            ms = [B.run()["ms_total"] for _ in range(args.steps)]
+            graph_ms = max_over_ranks(float(np.mean(ms)), world, local)
+            # 64 sequential single assemblies (one bgb_assemble each), device outputs
+            bufs = [torch.empty((X.nfun, X.nfun), dtype=torch.complex64 if prec == "mixed" else torch.complex128,
+                                device=f"cuda:{local}") for _, X, _ in probs]
+            cfg = bg.GPUConfiguration(precision=prec, device=local)
+
+            def seq():
+                for (op, X, Y), b in zip(probs, bufs):
+                    bg.assemble_gpu(op, X, Y, cfg, out="device", out_buffer=b)
+            for _ in range(args.warmup):
+                seq()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(args.steps):
+                seq()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            seq_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, world, local)
+            same = all(bool(torch.equal(a.T, b)) for a, b in zip(bufs, B.outputs))
+            errs = []
+            if rank == 0:
+                for i in (0, 21, 42, 63):
+                    op, X, _ = probs[i]
+                    rows = np.sort(np.random.default_rng(i).choice(X.nfun, min(20, X.nfun), replace=False)).astype(np.int32)
+                    Zr = B.outputs[i][torch.as_tensor(rows.astype(np.int64), device=B.outputs[i].device)].cpu().numpy()
+                    errs.append(oracle_rows_error(op, X, Zr, rows)["rel_frobenius"])
+            out[prec] = {"graph_ms_per_step": graph_ms, "graph_pairs_per_s": pairs / (graph_ms * 1e-3),
+                         "sequential_ms_per_step": seq_ms, "sequential_pairs_per_s": pairs / (seq_ms * 1e-3),
+                         "batch_bit_identical_to_sequential": same, "tile_config": B.create_stats["tile_config"],
+                         "schedule": B.create_stats["schedule"],
+                         "max_rel_frobenius_vs_oracle_sampled": max(errs) if errs else None}
+            B.close()
+            del bufs
+            torch.cuda.empty_cache()
+    if rank != 0:
+        return 0
+    value = world * pairs / (out["mixed"]["graph_ms_per_step"] * 1e-3)
+    cfg = {"workload": "64 seeded ellipsoids (icosphere levels 1-4, axes U[0.5,2], k U[1,10]), EFIE on RWG, "
+                       "one persistent CUDA-graph launch, autotuned tiles and schedule",
+           "problems": 64, "triangles": sum(m.nt for m, _ in batch), "pairs_per_step": pairs}
+    print(json.dumps(line_base(args, world, value, out["mixed"]["graph_ms_per_step"],
+                               "f32 far + double-float singular/near (mixed)", cfg,
+                               vs_sequential_fp64=out["fp64"]["sequential_ms_per_step"] / out["mixed"]["graph_ms_per_step"],
+                               results=out, clocks=clocks.summary(), gpu_launches=3 * (args.steps + args.warmup))))
+    return 0
+
+
+def run_c5(args):
+    """Out of core: level-6 icosphere EFIE, ComplexF32 output streamed to pinned host memory."""
+    import torch
+    import beastgpu_gb300 as bg
+    rank, world, local = dist_init(args.gpus)
+    mesh = bg.icosphere(6)
+    X = bg.raviartthomas(mesh)
+    op = bg.Maxwell3D.singlelayer(wavenumber=2 * np.pi * 8)
+    n = X.nfun
+    nbytes = n * n * 8
+    avail = 0
+    try:
+        for line in open("/proc/meminfo"):
+            if line.startswith("MemAvailable:"):
+                avail = int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    cfg_d = {"workload": f"EFIE on RWG, icosphere level 6 ({mesh.nt} triangles, {n} RWG), k=2*pi*8, ComplexF32 "
+                         f"output ({nbytes / 1e9:.1f} GB) in pinned host memory",
+             "triangles": mesh.nt, "functions": n, "pairs_per_step": mesh.nt * mesh.nt,
+             "hbm_budget_bytes": args.hbm_budget}
+    if avail and avail < nbytes + (24 << 30):
+        print(json.dumps({"metric": METRIC, "skipped": f"host memory {avail / 1e9:.0f} GB < output + 24 GB",
+                          "config": cfg_d}))
+        return 0
+    Z = np.empty((n, n), dtype=np.complex64, order="F")
+    cfg = bg.GPUConfiguration(precision="mixed", device=local, total_GPU_budget=args.hbm_budget)
+    # pageable destination first (the first call faults its pages in), then the same memory pinned
+    ms_pg, st_pg, _, _ = time_fill(bg, X, op, "mixed", args.steps, 1, local, out="host", pinned=Z, cfg=cfg)
+    cudart = torch.cuda.cudart()
+    t0 = time.perf_counter()
+    rc = cudart.cudaHostRegister(Z.ctypes.data, Z.nbytes, 0)
+    reg_s = time.perf_counter() - t0
+    if int(rc) != 0:
+        raise RuntimeError(f"cudaHostRegister failed ({rc})")
+    try:
+        with ClockSampler(local) as clocks:
+            ms_steps, stats, _, _ = time_fill(bg, X, op, "mixed", args.steps, args.warmup, local, out="host",
+                                              pinned=Z, cfg=cfg)
+        rows = np.sort(np.random.default_rng(5).choice(n, 100, replace=False)).astype(np.int32)
+        err = oracle_rows_error(op, X, Z[rows, :], rows) if rank == 0 else None
+    finally:
+        cudart.cudaHostUnregister(Z.ctypes.data)
+    ms = max_over_ranks(float(np.mean(ms_steps)), world, local)
+    if rank != 0:
+        return 0
+    st = stats[-1]
+    far, cp, pipe = st["ms_far"], st["ms_copy"], st["ms_pipeline"]
+    pairs = mesh.nt * mesh.nt
+    value = world * pairs / (ms * 1e-3)
+    h2d = X.mesh.vertices.nbytes + X.mesh.triangles.nbytes + X.fn_index.nbytes + X.fn_coef.nbytes
+    print(json.dumps(line_base(
+        args, world, value, ms, "f32 far + double-float singular/near (mixed)", cfg_d,
+        e2e={"value": value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(nbytes)},
+        pipeline={"out_blocks": st["out_blocks"], "ms_classify": st["ms_classify"], "ms_singular": st["ms_singular"],
+                  "ms_far": far, "ms_copy": cp, "ms_pipeline": pipe, "ms_plan": st["ms_plan"],
+                  "overlap_fraction": (far + cp - pipe) / min(far, cp) if min(far, cp) > 0 else None,
+                  "copy_gbs": nbytes / (cp * 1e-3) / 1e9 if cp > 0 else None, "host_register_s": reg_s},
+        pageable_destination={"ms_per_step": float(np.mean(ms_pg)), "pairs_per_s": pairs / (np.mean(ms_pg) * 1e-3),
+                              "ms_copy": st_pg[-1]["ms_copy"], "ms_pipeline": st_pg[-1]["ms_pipeline"]},
+        error_vs_oracle=dict(err, rows=100, seed=5), clocks=clocks.summary(),
+        gpu_launches=int(sum(x["kernel_launches"] for x in stats)))))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -239,6 +442,8 @@ def main():
     ap.add_argument("--ref-rows", type=int, default=200)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5"])
+    ap.add_argument("--hbm-budget", type=int, default=0, help="c5: HBM budget in bytes (0 = 90% of free)")
     ap.add_argument("--profile-level", type=int, default=None,
                     help="profiling case: run W + K mixed and FP64 fills of an icosphere of this level and exit")
     args = ap.parse_args()
@@ -246,6 +451,8 @@ def main():
         return run_reference(args)
     if args.profile_level is not None:
         return run_profile_case(args)
+    if args.workload != "c2":
+        return {"c3": run_c3, "c4": run_c4, "c5": run_c5}[args.workload](args)
 
     import torch
     rank, world, local = dist_init(args.gpus)

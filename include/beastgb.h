@@ -24,7 +24,12 @@
 extern "C" {
 #endif
 
-#define BGB_ABI_VERSION 1
+#define BGB_ABI_VERSION 2
+
+/* bgb_config.flags: copy pageable host outputs through the pinned ring even when the device
+ * reaches pageable memory through the host page tables (by default such outputs are written
+ * by DMA after their pages are faulted in). */
+#define BGB_CFG_PAGEABLE_VIA_RING 1
 
 typedef enum {
   BGB_OK = 0,
@@ -96,20 +101,26 @@ typedef struct {
 typedef struct {
   int32_t device;              /* CUDA device ordinal */
   int64_t hbm_budget_bytes;    /* 0 = 90% of free device memory; bounds row blocks */
-  int64_t pinned_ring_bytes;   /* 0 = 2 x 512 MiB staging ring for host output */
+  int64_t pinned_ring_bytes;   /* each half of the pinned ring that pageable host outputs are
+                                  copied through (at least one column of the output); 0 = 512 MiB */
   int32_t tile_config;         /* -1 = first tile shape that fits shared memory, else a tile id (bgb_tile_info) */
-  int32_t flags;               /* reserved, 0 */
+  int32_t flags;               /* BGB_CFG_* bits */
 } bgb_config;
 
 typedef struct {
   int64_t pairs_total;          /* nt_test * nt_trial over the assembled rows */
   int64_t pairs_class[5];       /* far, CV, CE, CF, near */
   int64_t pairs_computed;       /* triangle pairs evaluated by the far kernel (incl. halo) */
-  double ms_classify, ms_singular, ms_far, ms_copy, ms_total;
-  int32_t row_blocks;
+  double ms_classify, ms_singular; /* device time of the classification / singular stages */
+  double ms_far;                /* device time of the far kernels (sum over output blocks) */
+  double ms_copy;               /* device-to-host copy time (sum over output blocks) */
+  double ms_total;              /* wall time of the call */
+  double ms_pipeline;           /* wall time of the far kernels and copies (overlapped) */
+  double ms_plan;               /* host tile planning (runs beside the classification) */
+  int32_t out_blocks;           /* output blocks: column ranges of a host output */
   int32_t tile_config;
   int32_t kernel_launches;      /* kernels this call launched */
-  int32_t reserved;
+  int32_t schedule;             /* batches: work-queue schedule (0 problem-major, 1 largest first) */
 } bgb_stats;
 
 typedef struct bgb_handle bgb_handle;
@@ -155,7 +166,7 @@ int bgb_assemble_batch(bgb_handle* h, int32_t n, const bgb_problem* problems, in
  * work-queue schedule (flags & 1: every fitting candidate is timed on this batch), and
  * captures the whole device sequence in a CUDA graph; bgb_batch_run replays that graph
  * (re-assembling the same problems into the same outputs) and copies host outputs.
- * stats->tile_config / row_blocks report the chosen tile shape / schedule (0 problem-major,
+ * stats->tile_config / schedule report the chosen tile shape / work-queue schedule (0 problem-major,
  * 1 largest tiles first); stats->ms_total of bgb_batch_run is the graph's device time. */
 typedef struct bgb_batch bgb_batch;
 int bgb_batch_create(bgb_handle* h, int32_t n, const bgb_problem* problems, int32_t precision,

@@ -48,7 +48,7 @@ def test_no_undeclared_exports(lib):
 
 
 def test_abi_version(lib):
-    assert lib.bgb_abi_version() == 1
+    assert lib.bgb_abi_version() == _lib.ABI_VERSION == 2
     n = lib.bgb_tile_info(None, 0)
     assert n >= 4
 

@@ -139,11 +139,70 @@ def test_row_windows_and_writeback_strategies(c1):
     np.testing.assert_array_equal(part, full[100:177])
     cpuwb = bg.assemble_gpu(op, X, X, bg.GPUConfiguration(precision="fp64"), bg.GpuWriteBackFalseInstance())
     np.testing.assert_array_equal(cpuwb, full)
-    # out-of-core: a tiny HBM budget forces many row blocks; result unchanged
-    small = bg.assemble_gpu(op, X, X, bg.GPUConfiguration(precision="fp64", total_GPU_budget=2 * 60 * 480 * 16),
+    # out-of-core: a tiny HBM budget forces many output blocks; result unchanged
+    small = bg.assemble_gpu(op, X, X, bg.GPUConfiguration(precision="fp64", total_GPU_budget=4 * 30 * 480 * 16),
                             return_stats=True)
     np.testing.assert_array_equal(small[0], full)
-    assert small[1]["row_blocks"] > 1
+    assert small[1]["out_blocks"] == 16
+
+
+def test_out_of_core_pipeline_pinned_pageable_and_ring(c1):
+    """Output blocks (column ranges) double-buffered on the device, copied while the next block
+    is filled: pageable host outputs through a pinned ring (chunks of a few columns, and a ring
+    smaller than one column), pinned outputs directly; all bit-identical to the device result."""
+    import torch
+    m, X, L = c1
+    op = bg.Maxwell3D.singlelayer(wavenumber=K1)
+    n = X.nfun
+    for prec, esz, tdt in (("fp64", 16, torch.complex128), ("mixed", 8, torch.complex64)):
+        ref = bg.assemble_gpu(op, X, X, bg.GPUConfiguration(precision=prec), out="device").cpu().numpy()
+        budget = 4 * 37 * n * esz  # 37 columns per block, the last block ragged
+        cfg = bg.GPUConfiguration(precision=prec, total_GPU_budget=budget, pinned_ring_bytes=5 * n * esz)
+        Z, st = bg.assemble_gpu(op, X, X, cfg, return_stats=True)
+        assert st["out_blocks"] == (n + 36) // 37
+        np.testing.assert_array_equal(Z, ref)
+        buf = torch.empty((n, n), dtype=tdt, pin_memory=True)  # column-major n x n
+        bg.assemble_gpu(op, X, X, cfg, out_buffer=buf)
+        np.testing.assert_array_equal(buf.numpy().T, ref)
+        tiny_ring = bg.GPUConfiguration(precision=prec, total_GPU_budget=budget, pinned_ring_bytes=1,
+                                        pageable_via_ring=True)
+        W = bg.assemble_gpu(op, X, X, tiny_ring, rows=(50, 200))
+        np.testing.assert_array_equal(W, ref[50:250])
+        via_ring = bg.GPUConfiguration(precision=prec, total_GPU_budget=budget, pinned_ring_bytes=5 * n * esz,
+                                       pageable_via_ring=True)
+        np.testing.assert_array_equal(bg.assemble_gpu(op, X, X, via_ring), ref)
+
+
+def test_host_output_with_leading_dimension_keeps_other_rows(c1):
+    """Host output with ld > nrows (a window into a larger column-major array): the rows
+    outside the window are untouched, for pinned, pageable and ring destinations."""
+    import ctypes as C
+    import torch
+    from beastgpu_gb300 import _lib
+    from beastgpu_gb300.api import _Keep, c_operator, c_quadstrat, c_space, get_handle
+    m, X, L = c1
+    op = bg.Maxwell3D.singlelayer(wavenumber=K1)
+    n = X.nfun
+    ref = bg.assemble_gpu(op, X, X, bg.GPUConfiguration(precision="fp64"))
+    r0, nr, ld = 37, 101, 160
+    keep = _Keep()
+    sp = c_space(X, keep)
+    cop, cq = c_operator(op), c_quadstrat(bg.QuadStrat())
+    for flags, pinned in ((0, False), (0, True), (_lib.CFG_PAGEABLE_VIA_RING, False)):
+        h = get_handle(0, 4 * 50 * nr * 16, -1, 3 * nr * 16, flags)
+        if pinned:
+            t = torch.full((n, ld), 7.0 + 0j, dtype=torch.complex128, pin_memory=True)
+            buf, ptr = t.numpy().T, t.data_ptr()  # buf[i, j]: column-major ld x n
+        else:
+            buf = np.full((ld, n), 7.0 + 0j, dtype=np.complex128, order="F")
+            ptr = buf.ctypes.data
+        st = _lib.Stats()
+        _lib.check(_lib.load().bgb_assemble(h.ptr, C.byref(cop), C.byref(sp), C.byref(sp), C.byref(cq),
+                                            _lib.PREC_FP64, C.c_void_p(ptr), _lib.OUT_HOST_C64, ld, r0, nr, None,
+                                            C.byref(st)))
+        assert st.out_blocks > 1
+        np.testing.assert_array_equal(buf[:nr], ref[r0:r0 + nr])
+        assert np.all(buf[nr:] == 7.0)
 
 
 def test_c2_sampled_rows(qs):
