@@ -44,6 +44,10 @@ METRIC = "pair-interactions/s: mixed FP32 vs plain FP64 on GB300 at rel err <=1e
 UNIT = "pair-interactions/s"
 LEVEL, KWAVE = 5, 2 * np.pi * 4
 ERR_ROWS, ERR_SEED = 1000, 0
+# DRAM bytes (read + write) of one far-kernel launch per triangle pair, from the ncu capture of
+# the level-4 case (0.443 GB for 5120^2 pairs, profiles/kernels_efie_icosphere_l4.md); the
+# traffic is the output written once, so it scales with the pairs.
+FAR_DRAM_BYTES_PER_PAIR = 0.443e9 / (5120 * 5120)
 
 
 def workload():
@@ -526,7 +530,17 @@ def main():
     else:
         roof = {"kernel": "k_singular (FP64 Sauter-Schwab)", "bound": "fp64", "achieved": sing_tf, "peak": fp64_peak,
                 "unit": "TFLOP/s", "frac": sing_tf / fp64_peak}
-    roof.update({"traffic": None, "peak_source": "measured live by bgb_measure_issue_peaks (FMA chains)",
+    hbm_peak = None
+    try:
+        hbm_peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))).get("hbm_gbs")
+    except (OSError, ValueError):
+        pass
+    out_gb = X.nfun * X.nfun * 8 / 1e9
+    roof.update({"traffic": FAR_DRAM_BYTES_PER_PAIR * pairs if far_ms >= sing_ms else None,
+                 "traffic_source": "ncu dram__bytes of the level-4 launch scaled by pairs (x16)",
+                 "hbm_gbs_far": out_gb / (far_ms * 1e-3), "hbm_frac_far_of_measured": (out_gb / (far_ms * 1e-3)) / hbm_peak
+                 if hbm_peak else None,
+                 "peak_source": "measured live by bgb_measure_issue_peaks (FMA chains)",
                  "flop_convention": "per point pair: 15 (kernel) + 108 (EFIE 9-entry accumulation), FMA = 2",
                  "kernels_ms": {"far": far_ms, "singular": sing_ms,
                                 "classify": float(np.mean([s["ms_classify"] for s in st_mixed]))},
