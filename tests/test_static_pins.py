@@ -1,0 +1,127 @@
+"""Singular-pair integration pinned to closed-form potentials (tests/golden/static_singular.npz).
+
+The fixture holds static (k = 0) local matrices of common-face, common-edge and common-vertex
+pairs on an ellipsoid, computed by tests/golden/make_static_fixtures.py from the analytic
+potential of a flat triangle and a graded outer rule, independently of the Sauter-Schwab code.
+The oracle's (and the GPU's) Sauter-Schwab rules must converge to them exponentially in the
+order n: errors decrease with n, are below 2e-4 at the reference's n = 4 and below 1e-8 at n = 10.
+Far pairs (3 x 4 .. 13 x 13 point rules) and near pairs (3 x 4 .. 12 x 13) converge to the same
+closed forms with the orders of their rules.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import beastgpu_gb300 as bg
+import oracle
+from beastgpu_gb300.operators import Operator
+
+FIX = os.path.join(os.path.dirname(__file__), "golden", "static_singular.npz")
+ORDERS = (4, 6, 8, 10)
+TOL_N4, TOL_N10 = 2e-4, 1e-8
+
+
+NSING = 15  # pairs 0..14: 3 common face, 6 common edge, 6 common vertex; 15..18: far
+
+
+@pytest.fixture(scope="module")
+def fx():
+    d = np.load(FIX)
+    m = bg.Mesh(d["vertices"], d["triangles"])
+    pm = bg.Mesh(d["plate_vertices"], d["plate_triangles"])
+    spaces = {"hh": bg.lagrangec0d1(m), "mw_alpha": bg.raviartthomas(m), "mw_beta": bg.raviartthomas(m)}
+    plate_spaces = {"hh": bg.lagrangec0d1(pm, dirichlet=False), "mw_alpha": bg.raviartthomas(pm),
+                    "mw_beta": bg.raviartthomas(pm)}
+    ops = {"hh": Operator(0, 1.0, 0.0, 0.0),          # (kind, alpha, gamma, beta): k = 0
+           "mw_alpha": Operator(1, 1.0, 0.0, 0.0),
+           "mw_beta": Operator(1, 0.0, 0.0, 1.0)}
+    return d, spaces, plate_spaces, ops
+
+
+def _errors(L, ref):
+    return np.array([np.linalg.norm(L[k] - ref[k]) / np.linalg.norm(ref[k]) for k in range(len(ref))])
+
+
+def test_fixture_is_converged(fx):
+    d = fx[0]
+    assert d["rule_change"].max() < 1e-11      # 40 -> 60 points per dimension of the outer rule
+    assert float(d["self_term_error"]) < 1e-13  # outer rule against the closed-form self term
+    assert np.all(d["mw_beta"] > 0) and np.all(np.diagonal(d["hh"], axis1=1, axis2=2) > 0)
+
+
+SING_CLASSES = [3] * 3 + [2] * 6 + [1] * 6
+
+
+def _singular(local, fx, name, n, **kw):
+    d, spaces, _, ops = fx
+    S = spaces[name]
+    qs = bg.QuadStrat(ss_cf=n, ss_ce=n, ss_cv=n)
+    L, cls = local(ops[name], S, S, qs, d["tau"][:NSING], d["sigma"][:NSING], **kw)
+    assert cls.tolist() == SING_CLASSES
+    return L, _errors(L, d[name][:NSING]).max()
+
+
+def _far(local, fx, name, qt, qb, **kw):
+    d, spaces, _, ops = fx
+    S = spaces[name]
+    L, cls = local(ops[name], S, S, bg.QuadStrat(far_test=qt, far_trial=qb), d["tau"][NSING:], d["sigma"][NSING:],
+                   **kw)
+    assert cls.tolist() == [0] * 4
+    return L, _errors(L, d[name][NSING:]).max()
+
+
+def _near(local, fx, name, qt, qb, **kw):
+    d, _, plate_spaces, ops = fx
+    S = plate_spaces[name]
+    L, cls = local(ops[name], S, S, bg.QuadStrat(near_test=qt, near_trial=qb), d["near_tau"], d["near_sigma"], **kw)
+    assert cls.tolist() == [4] * 4
+    return L, _errors(L, d["near_" + name]).max()
+
+
+def _oracle(op, X, Y, qs, tau, sigma):
+    return oracle.local_matrices(op, X, Y, qs, tau, sigma)
+
+
+@pytest.mark.parametrize("name", ["hh", "mw_alpha", "mw_beta"])
+def test_oracle_sauter_schwab_converges_to_closed_forms(fx, name):
+    errs = [_singular(_oracle, fx, name, n)[1] for n in ORDERS]
+    assert errs[0] < TOL_N4 and errs[-1] < TOL_N10, errs
+    assert all(a > b for a, b in zip(errs, errs[1:])), errs
+
+
+@pytest.mark.parametrize("name", ["hh", "mw_alpha", "mw_beta"])
+def test_oracle_far_and_near_rules_converge_to_closed_forms(fx, name):
+    far = [_far(_oracle, fx, name, qt, qb)[1] for qt, qb in ((3, 4), (6, 7), (13, 13))]
+    assert far[0] < 5e-3 and far[-1] < 1e-5 and far[0] > far[1] > far[2], far
+    near = [_near(_oracle, fx, name, qt, qb)[1] for qt, qb in ((3, 4), (6, 7), (12, 13))]
+    assert near[-1] < 1e-3 and near[0] > near[1] > near[2], near
+
+
+def _gpu(precision):
+    def local(op, X, Y, qs, tau, sigma):
+        return bg.local_matrices(op, X, Y, tau, sigma, quadstrat=qs, precision=precision)
+    return local
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("name", ["hh", "mw_alpha", "mw_beta"])
+def test_gpu_rules_converge_to_closed_forms(fx, name, precision):
+    """Singular pairs to 1e-12 of the oracle at every order (both precisions: FP64 and
+    double-float); far pairs to 1e-12 (FP64) or 1e-6 (mixed FP32) of the oracle."""
+    local = _gpu(precision)
+    errs = []
+    for n in ORDERS:
+        L, e = _singular(local, fx, name, n)
+        ref_o, _ = _singular(_oracle, fx, name, n)
+        assert _errors(L, ref_o).max() < 1e-12
+        errs.append(e)
+    assert errs[0] < TOL_N4 and errs[-1] < TOL_N10, errs
+    assert all(a > b for a, b in zip(errs, errs[1:])), errs
+    far_tol = 1e-12 if precision == "fp64" else 1e-6
+    for qt, qb in ((3, 4), (13, 13)):
+        L, _ = _far(local, fx, name, qt, qb)
+        assert _errors(L, _far(_oracle, fx, name, qt, qb)[0]).max() < far_tol
+    L, e = _near(local, fx, name, 12, 13)
+    assert _errors(L, _near(_oracle, fx, name, 12, 13)[0]).max() < 1e-12 and e < 1e-3
