@@ -190,8 +190,12 @@ int make_opparams(const bgb_operator* op, const bgb_space* a, const bgb_space* b
   return 0;
 }
 
-FarConst make_farconst(const OpParams& op, const RuleTable& R, const QuadSel& qs) {
+FarConst make_farconst(const OpParams& op, const RuleTable& R, const QuadSel& qs, const bgb_space* test,
+                       const bgb_space* trial) {
   FarConst k{};
+  // |k delta| <= k (r_test + r_trial) < k (edge_test + edge_trial): within pi, the point-pair phase
+  // phi0 + k delta stays in [-2 pi, 2 pi] and goes to sin / cos without a second reduction
+  k.phase_direct = test && trial && std::fabs(op.gamma[1]) * (max_edge(test) + max_edge(trial)) <= 3.14159;
   k.op_kind = op.kind;
   k.qt = R.npoints[qs.far_t];
   k.qb = R.npoints[qs.far_b];
@@ -604,7 +608,7 @@ int bgb_local_matrices(bgb_handle* h, const bgb_operator* op, const bgb_space* t
                        h->ent_mask.as<int16_t>(), npairs, h->diag_c.as<double2>(), nullptr, h->num_sms, h->stream);
   }
   // far pairs through the far-kernel pair code of the requested precision
-  FarConst K = make_farconst(opp, R, qsel);
+  FarConst K = make_farconst(opp, R, qsel, test, trial);
   const int gen = far_generic_q(K.qt, K.qb);
   const int rst = rec_stride(precision, K.qt, gen), rsb = rec_stride(precision, K.qb, gen);
   const size_t esz = precision == BGB_PREC_MIXED ? sizeof(float) : sizeof(double);
@@ -670,7 +674,7 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
   }
 
   RuleTable R = make_rules();
-  const FarConst K = make_farconst(opp, R, qsel);
+  const FarConst K = make_farconst(opp, R, qsel, test, trial);
   const int gen = far_generic_q(K.qt, K.qb);
   const bool same = same_space(test, trial);
   const int64_t ncols = trial->nfun;

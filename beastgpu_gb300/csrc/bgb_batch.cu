@@ -301,7 +301,7 @@ int bgb_batch_create(bgb_handle* h, int32_t n, const bgb_problem* problems, int3
   for (int p = 0; p < n; ++p) {
     const bgb_problem& q = problems[p];
     if ((rc = make_opparams(&q.op, &q.test, &q.trial, &ops[p]))) return fail(rc);
-    Ks[p] = make_farconst(ops[p], B->rules, B->qsel);
+    Ks[p] = make_farconst(ops[p], B->rules, B->qsel, &q.test, &q.trial);
     prob_k2[p] = ops[p].k2;
     tbase[p] = (int)(tt.size() / 3);
     const int vo = (int)(vt.size() / 3);

@@ -118,6 +118,97 @@ __device__ __forceinline__ void far_pair_mixed(const FarScalars& K, const float 
 #pragma unroll
   for (int k = 0; k < 9; ++k) L[k] = make_float2(0.f, 0.f);
 
+  if constexpr (OP != BGB_OP_MAXWELL3D_DL) {
+    // Helmholtz / EFIE: q = s.(2 D_hi + s) with s = a_I - y_J, a_I = D_lo + x_I, split as
+    //   q = [c0 + a_I.(a_I + 2 D_hi)] + [y_J.(y_J - 2 D_hi)] - 2 a_I.y_J
+    // (per test point, per trial point, per point pair): 5 operations per point pair.
+    // trial points of the pair in registers when the rule is small (shared-memory loads otherwise)
+    constexpr int QY = QB <= 4 ? QB : 1;
+    float Y[QY][3], MJ[QY];
+    if constexpr (QB <= 4) {
+#pragma unroll
+      for (int J = 0; J < QB; ++J) {
+        if (J >= qb) break;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) Y[J][c] = b[OB::X + 3 * J + c];
+        MJ[J] = fmaf(Y[J][0], Y[J][0] - D2x, fmaf(Y[J][1], Y[J][1] - D2y, Y[J][2] * (Y[J][2] - D2z)));
+      }
+    }
+#pragma unroll
+    for (int I = 0; I < QT; ++I) {
+      if (I >= qt) break;
+      const float Xx = a[OA::X + 3 * I], Xy = a[OA::X + 3 * I + 1], Xz = a[OA::X + 3 * I + 2];
+      const float ax = Dl[0] + Xx, ay = Dl[1] + Xy, az = Dl[2] + Xz;
+      const float KI = fmaf(ax, ax + D2x, fmaf(ay, ay + D2y, fmaf(az, az + D2z, c0)));
+      const float wI = a[OA::W + I];
+      float2 TI = make_float2(0.f, 0.f);
+      float2 UI[3], M[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) UI[c] = M[c] = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int J = 0; J < QB; ++J) {
+        if (J >= qb) break;
+        float yx, yy, yz, mj;
+        if constexpr (QB <= 4) {
+          yx = Y[J][0], yy = Y[J][1], yz = Y[J][2], mj = MJ[J];
+        } else {
+          yx = b[OB::X + 3 * J], yy = b[OB::X + 3 * J + 1], yz = b[OB::X + 3 * J + 2];
+          mj = fmaf(yx, yx - D2x, fmaf(yy, yy - D2y, yz * (yz - D2z)));
+        }
+        const float dot = fmaf(ax, yx, fmaf(ay, yy, az * yz));
+        const float q = fmaf(-2.f, dot, KI + mj);
+        const float R2 = R0sq + q;
+        const float rs = rsqrtf(R2);
+        const float delta = __fdividef(q, fmaf(R2, rs, R0));
+        float psi = fmaf(kh, delta, phi0);
+        if (!K.phase_direct) {  // |psi| may exceed 2 pi: reduce again
+          const float nn = rintf(psi * kInv2Pi);
+          psi = fmaf(-nn, kPiA, psi);
+          psi = fmaf(-nn, kPiB, psi);
+        }
+        float sn, cs;
+        __sincosf(psi, &sn, &cs);
+        float amp = (wI * b[OB::W + J]) * rs;
+        if (K.lossy) amp *= amp0 * __expf(-K.gre * delta);
+        const float gr = amp * cs, gi = -amp * sn;
+        if (OP == BGB_OP_HELMHOLTZ3D_SL) {
+#pragma unroll
+          for (int j = 0; j < 3; ++j) {
+            const float g = shpB[J][j];
+            M[j].x = fmaf(gr, g, M[j].x);
+            M[j].y = fmaf(gi, g, M[j].y);
+          }
+        } else {
+          TI.x += gr;
+          TI.y += gi;
+          UI[0].x = fmaf(gr, yx, UI[0].x); UI[0].y = fmaf(gi, yx, UI[0].y);
+          UI[1].x = fmaf(gr, yy, UI[1].x); UI[1].y = fmaf(gi, yy, UI[1].y);
+          UI[2].x = fmaf(gr, yz, UI[2].x); UI[2].y = fmaf(gi, yz, UI[2].y);
+        }
+      }
+      if (OP == BGB_OP_HELMHOLTZ3D_SL) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          const float f = shpT[I][i];
+#pragma unroll
+          for (int j = 0; j < 3; ++j) {
+            L[i * 3 + j].x = fmaf(f, M[j].x, L[i * 3 + j].x);
+            L[i * 3 + j].y = fmaf(f, M[j].y, L[i * 3 + j].y);
+          }
+        }
+      } else {
+        S.x = fmaf(Xx, UI[0].x, fmaf(Xy, UI[1].x, fmaf(Xz, UI[2].x, S.x)));
+        S.y = fmaf(Xx, UI[0].y, fmaf(Xy, UI[1].y, fmaf(Xz, UI[2].y, S.y)));
+        Px[0].x = fmaf(Xx, TI.x, Px[0].x); Px[0].y = fmaf(Xx, TI.y, Px[0].y);
+        Px[1].x = fmaf(Xy, TI.x, Px[1].x); Px[1].y = fmaf(Xy, TI.y, Px[1].y);
+        Px[2].x = fmaf(Xz, TI.x, Px[2].x); Px[2].y = fmaf(Xz, TI.y, Px[2].y);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) { Py[c].x += UI[c].x; Py[c].y += UI[c].y; }
+        P0.x += TI.x;
+        P0.y += TI.y;
+      }
+    }
+  } else {
 #pragma unroll
   for (int I = 0; I < QT; ++I) {
     if (I >= qt) break;
@@ -213,6 +304,7 @@ __device__ __forceinline__ void far_pair_mixed(const FarScalars& K, const float 
     }
   }
 
+  }
   const float2 alpha = make_float2(K.alpha32[0], K.alpha32[1]);
   if (OP == BGB_OP_HELMHOLTZ3D_SL) {
 #pragma unroll
@@ -222,30 +314,32 @@ __device__ __forceinline__ void far_pair_mixed(const FarScalars& K, const float 
   const float inv4AA = a[OA::INV2A] * b[OB::INV2A];
   const float2 ca = make_float2(alpha.x * inv4AA, alpha.y * inv4AA);
   if (OP == BGB_OP_MAXWELL3D_SL) {
+    // L_ij = alpha/(4 A A) (S - V_i.Py - W_j.Px + (V_i.W_j) P0) + beta/(A A) P0
     const float invAA = 4.f * inv4AA;
     const float2 cb = make_float2(K.beta32[0] * invAA, K.beta32[1] * invAA);
     const float2 tb = cmulf(cb, P0);
-    float2 av[3], bv[3];
+    float V[3][3], W[3][3];
+    float2 Ai[3], Bj[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-      const float vx = a[OA::VO + 3 * i], vy = a[OA::VO + 3 * i + 1], vz = a[OA::VO + 3 * i + 2];
-      av[i].x = vx * Py[0].x + vy * Py[1].x + vz * Py[2].x;
-      av[i].y = vx * Py[0].y + vy * Py[1].y + vz * Py[2].y;
-      const float wx = b[OB::VO + 3 * i], wy = b[OB::VO + 3 * i + 1], wz = b[OB::VO + 3 * i + 2];
-      bv[i].x = wx * Px[0].x + wy * Px[1].x + wz * Px[2].x;
-      bv[i].y = wx * Px[0].y + wy * Px[1].y + wz * Px[2].y;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        V[i][c] = a[OA::VO + 3 * i + c];
+        W[i][c] = b[OB::VO + 3 * i + c];
+      }
+      Ai[i].x = S.x - fmaf(V[i][0], Py[0].x, fmaf(V[i][1], Py[1].x, V[i][2] * Py[2].x));
+      Ai[i].y = S.y - fmaf(V[i][0], Py[0].y, fmaf(V[i][1], Py[1].y, V[i][2] * Py[2].y));
+      Bj[i].x = fmaf(W[i][0], Px[0].x, fmaf(W[i][1], Px[1].x, W[i][2] * Px[2].x));
+      Bj[i].y = fmaf(W[i][0], Px[0].y, fmaf(W[i][1], Px[1].y, W[i][2] * Px[2].y));
     }
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
-        const float vw = a[OA::VO + 3 * i] * b[OB::VO + 3 * j] + a[OA::VO + 3 * i + 1] * b[OB::VO + 3 * j + 1] +
-                         a[OA::VO + 3 * i + 2] * b[OB::VO + 3 * j + 2];
-        float2 t;
-        t.x = S.x - av[i].x - bv[j].x + vw * P0.x;
-        t.y = S.y - av[i].y - bv[j].y + vw * P0.y;
-        const float2 r = cmulf(ca, t);
-        L[i * 3 + j] = make_float2(r.x + tb.x, r.y + tb.y);
+        const float vw = fmaf(V[i][0], W[j][0], fmaf(V[i][1], W[j][1], V[i][2] * W[j][2]));
+        const float tx = fmaf(vw, P0.x, Ai[i].x - Bj[j].x);
+        const float ty = fmaf(vw, P0.y, Ai[i].y - Bj[j].y);
+        L[i * 3 + j] = make_float2(fmaf(ca.x, tx, fmaf(-ca.y, ty, tb.x)), fmaf(ca.x, ty, fmaf(ca.y, tx, tb.y)));
       }
     return;
   }
@@ -449,7 +543,7 @@ __device__ __forceinline__ FarScalars far_scalars(const FarConst& K) {
   S.qt = K.qt;
   S.qb = K.qb;
   S.lossy = K.lossy;
-  S.pad = 0;
+  S.phase_direct = K.phase_direct;
   S.k_hi = K.k_hi;
   S.k_lo = K.k_lo;
   S.gre = K.gre;
@@ -544,7 +638,8 @@ __host__ __device__ inline size_t carve(unsigned char* base, int tmax, int nmax,
 
 // One output tile (test-function block bm x trial-function block bn).
 template <class P, int OP, int QT, int QB>
-__device__ __forceinline__ void tile_body(const FarConst& K, const TilePlan& p, int bm, int bn, unsigned char* smem) {
+__device__ __forceinline__ void tile_body(const FarConst& K, const TilePlan& p, int bm, int bn, unsigned char* smem,
+                                          int* s_nonfar) {
   using R = typename P::R;
   using C = typename P::C;
   constexpr int RT = P::template rec<QT>();
@@ -605,57 +700,107 @@ __device__ __forceinline__ void tile_body(const FarConst& K, const TilePlan& p, 
     s.gsCoef[i] = f32 ? (R)p.gs_coef32[sb0 + i] : (R)p.gs_coef[sb0 + i];
   }
   for (int i = tid; i < fm * fn; i += kThreads) s.Zs[i] = P::mk(0.0, 0.0);
+  if (tid == 0) *s_nonfar = 0;
   __syncthreads();
+  // Does the tile hold any non-far pair?  Most tiles do not, and skip the per-pair test.
+  for (int i = tid; i < tm; i += kThreads) {
+    const int T = s.triT[i];
+    for (int64_t e = p.sing_off[T], e1 = p.sing_off[T + 1]; e < e1; ++e) {
+      const int sg = p.sing_sigma[e];
+      int lo = 0, hi = nbk;  // triB is sorted ascending
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (s.triB[mid] < sg) lo = mid + 1;
+        else hi = mid;
+      }
+      if (lo < nbk && s.triB[lo] == sg) {
+        *s_nonfar = 1;
+        break;
+      }
+    }
+  }
+  // fixed roles of this thread: pair (ti0 + k * tstep, si) of a chunk; gather row m, groups gq + k * gstep
+  const int tstep = kThreads / SC, ti0 = tid / SC, si = tid - ti0 * SC;
+  const int FMb = p.FM, gstep = kThreads / FMb, gq = tid / FMb, m = tid - gq * FMb;
+  const bool gather_on = m < fm && gq < gstep;
+  __syncthreads();
+  const bool check = *s_nonfar != 0;
 
   const int LS = p.tmax * SC;
   for (int c = c0; c < c1; ++c) {
     const int sbase = (c - c0) * SC;
     const int scn = min(SC, nbk - sbase);
-    const int np = tm * scn;
-    for (int q = tid; q < np; q += kThreads) {
-      const int ti = q / scn, si = q - ti * scn;
+    if (si < scn) {
       const int sb = sbase + si;
-      C L[9];
-      bool done = false;
-      if (sphere_candidate(s.bndT[ti], s.bndB[sb])) {
-        const int64_t e = find_sigma(p.sing_off, p.sing_sigma, s.triT[ti], s.triB[sb]);
-        if (e >= 0) {
+      for (int ti = ti0; ti < tm; ti += tstep) {
+        C L[9];
+        bool done = false;
+        if (check && sphere_candidate(s.bndT[ti], s.bndB[sb])) {
+          const int64_t e = find_sigma(p.sing_off, p.sing_sigma, s.triT[ti], s.triB[sb]);
+          if (e >= 0) {
 #pragma unroll
-          for (int k = 0; k < 9; ++k) {
-            const double2 v = p.sing_L[e * 9 + k];
-            L[k] = P::mk(v.x, v.y);
+            for (int k = 0; k < 9; ++k) {
+              const double2 v = p.sing_L[e * 9 + k];
+              L[k] = P::mk(v.x, v.y);
+            }
+            done = true;
           }
-          done = true;
         }
-      }
-      if (!done) far_pair<P, OP, QT, QB>(S, K, s.recT + ti * RT, s.recB + sb * RB, L);
-      const int li = ti * SC + si;
+        if (!done) far_pair<P, OP, QT, QB>(S, K, s.recT + ti * RT, s.recB + sb * RB, L);
+        const int li = ti * SC + si;
 #pragma unroll
-      for (int k = 0; k < 9; ++k) s.Lbuf[k * LS + li] = L[k];
+        for (int k = 0; k < 9; ++k) s.Lbuf[k * LS + li] = L[k];
+      }
     }
     __syncthreads();
-    const int gg0 = s.chGrp[c - c0], ng = s.chGrp[c - c0 + 1] - gg0;
-    for (int it = tid; it < ng * fm; it += kThreads) {
-      const int g = it / fm, m = it - g * fm;
-      const int gi = gg0 + g;
-      const int n = s.grpFn[gi];
-      C acc = s.Zs[n * fm + m];
-      const int q0 = s.grpOff[gi], q1 = s.grpOff[gi + 1];
+    if (gather_on) {
+      const int gg0 = s.chGrp[c - c0], ng = s.chGrp[c - c0 + 1] - gg0;
+      // this row's test supports (two for RWG) in registers for the chunk
       const int cnt = s.fcnt[m];
-      for (int bsup = q0; bsup < q1; ++bsup) {
-        const int code = s.gsCode[bsup];
-        const int sl = (code >> 2) - sbase, j = code & 3;
-        const R cb = s.gsCoef[bsup];
-        for (int a = 0; a < cnt; ++a) {
-          const int fc = s.fcode[m * MAXS + a];
-          const int ta = fc >> 2, i = fc & 3;
-          const R w = s.fcoef[m * MAXS + a] * cb;
-          const C l = s.Lbuf[(i * 3 + j) * LS + ta * SC + sl];
-          acc.x = fma(w, l.x, acc.x);
-          acc.y = fma(w, l.y, acc.y);
+      int fcA = 0, fcB = 0;
+      R fwA = 0, fwB = 0;
+      if (MAXS <= 2) {
+        fcA = s.fcode[m * MAXS];
+        fwA = s.fcoef[m * MAXS];
+        if (cnt > 1) {
+          fcB = s.fcode[m * MAXS + 1];
+          fwB = s.fcoef[m * MAXS + 1];
         }
       }
-      s.Zs[n * fm + m] = acc;
+      for (int g = gq; g < ng; g += gstep) {
+        const int gi = gg0 + g;
+        const int n = s.grpFn[gi];
+        C acc = s.Zs[n * fm + m];
+        const int q0 = s.grpOff[gi], q1 = s.grpOff[gi + 1];
+        for (int bsup = q0; bsup < q1; ++bsup) {
+          const int code = s.gsCode[bsup];
+          const int sl = (code >> 2) - sbase, j = code & 3;
+          const R cb = s.gsCoef[bsup];
+          if (MAXS <= 2) {
+            {
+              const R w = fwA * cb;
+              const C l = s.Lbuf[((fcA & 3) * 3 + j) * LS + (fcA >> 2) * SC + sl];
+              acc.x = fma(w, l.x, acc.x);
+              acc.y = fma(w, l.y, acc.y);
+            }
+            if (cnt > 1) {
+              const R w = fwB * cb;
+              const C l = s.Lbuf[((fcB & 3) * 3 + j) * LS + (fcB >> 2) * SC + sl];
+              acc.x = fma(w, l.x, acc.x);
+              acc.y = fma(w, l.y, acc.y);
+            }
+          } else {
+            for (int a = 0; a < cnt; ++a) {
+              const int fc = s.fcode[m * MAXS + a];
+              const R w = s.fcoef[m * MAXS + a] * cb;
+              const C l = s.Lbuf[((fc & 3) * 3 + j) * LS + (fc >> 2) * SC + sl];
+              acc.x = fma(w, l.x, acc.x);
+              acc.y = fma(w, l.y, acc.y);
+            }
+          }
+        }
+        s.Zs[n * fm + m] = acc;
+      }
     }
     __syncthreads();
   }
@@ -680,7 +825,7 @@ __global__ void __launch_bounds__(kThreads, P::kMinBlocks) k_far_persistent(cons
                                                              int* __restrict__ counter,
                                                              const volatile int* abort_flag) {
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ int next;
+  __shared__ int next, nonfar;
   __shared__ FarConst sK;
   __shared__ TilePlan sP;
   for (;;) {
@@ -694,7 +839,7 @@ __global__ void __launch_bounds__(kThreads, P::kMinBlocks) k_far_persistent(cons
     for (int i = threadIdx.x; i < (int)(sizeof(TilePlan) / 4); i += kThreads)
       ((int*)&sP)[i] = ((const int*)&plans[it.x])[i];
     __syncthreads();
-    tile_body<P, OP, QT, QB>(sK, sP, it.y, it.z, smem);
+    tile_body<P, OP, QT, QB>(sK, sP, it.y, it.z, smem, &nonfar);
     __syncthreads();
   }
 }

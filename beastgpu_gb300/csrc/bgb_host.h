@@ -94,7 +94,10 @@ int validate_space(const bgb_space* s, const char* name);
 int make_quadsel(const bgb_quadstrat* qs, QuadSel* out);
 int make_opparams(const bgb_operator* op, const bgb_space* a, const bgb_space* b, OpParams* out);
 RuleTable make_rules();
-FarConst make_farconst(const OpParams& op, const RuleTable& R, const QuadSel& qs);
+// Far-kernel constants; with both spaces given, also decides whether the point-pair phase needs
+// no second reduction (phase_direct).
+FarConst make_farconst(const OpParams& op, const RuleTable& R, const QuadSel& qs, const bgb_space* test = nullptr,
+                       const bgb_space* trial = nullptr);
 std::vector<int> morton_rank(const bgb_space* s);
 Supports build_supports(const bgb_space* s);
 std::vector<int> order_functions(const Supports& S, const std::vector<int>& rank, int f_begin, int f_end);

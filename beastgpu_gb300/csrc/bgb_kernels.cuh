@@ -70,6 +70,7 @@ struct FarConst {
   int op_kind;
   int qt, qb;                  // rule points (runtime, <= template maxima)
   int lossy;                   // gamma has a real part
+  int phase_direct;            // k (r_test + r_trial) <= pi: the point-pair phase needs no reduction
   double alpha[2], beta[2], gamma[2];
   float alpha32[2], beta32[2];
   float k_hi, k_lo, gre;       // gamma_im as double-float, gamma_re
@@ -79,7 +80,7 @@ struct FarConst {
 
 // The scalar constants of a far launch, copied into registers per tile.
 struct FarScalars {
-  int qt, qb, lossy, pad;
+  int qt, qb, lossy, phase_direct;
   float k_hi, k_lo, gre;
   float alpha32[2], beta32[2];
   double alpha[2], beta[2], gamma[2];
