@@ -205,6 +205,17 @@ def assemble_gpu(operator: Operator, test_functions: Space, trial_functions: Spa
     return (Z, stats.as_dict()) if return_stats else Z
 
 
+def row_shard(nrows: int, rank: int, world: int):
+    """Row window (row0, nrows) of `rank` among `world` processes: contiguous, balanced to one
+    row, covering [0, nrows) exactly once (the multi-GPU split of one matrix; the reference
+    splits the same way, assamble_chunk_gpu.jl:123-130).  No data exchange is needed: each rank
+    assembles its rows against all trial functions."""
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError(f"rank {rank} outside world of {world}")
+    r0 = nrows * rank // world
+    return r0, nrows * (rank + 1) // world - r0
+
+
 def assemble(operator: Operator, test_functions: Space, trial_functions: Space, *, quadstrat: QuadStrat = None,
              precision: str = "fp64", **kw):
     """BEAST.assemble(op, X, Y; quadstrat) on the GPU (host complex matrix)."""

@@ -551,7 +551,8 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 far pairs + f64 singular/near (mixed)",
             "data": "synthetic (seeded icosphere, built in-process)",
-            "config": config_dict(mesh, X, {"parallelism": f"replicas x{world}" if world > 1 else "single GPU"}),
+            "config": config_dict(mesh, X, {"parallelism": f"{world} independent matrices, one per rank, no collective"
+                                            if world > 1 else "single GPU"}),
             "fp64_value": fp64_value, "fp64_ms_per_step": fp64_ms, "mixed_over_fp64": value / fp64_value,
             "roofline": roof, "clocks": clocks.summary(),
             "gpu_launches": int(sum(s["kernel_launches"] for s in st_mixed)),
