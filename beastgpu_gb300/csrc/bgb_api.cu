@@ -159,9 +159,10 @@ int make_quadsel(const bgb_quadstrat* qs, QuadSel* out) {
 
 int make_opparams(const bgb_operator* op, const bgb_space* a, const bgb_space* b, OpParams* out) {
   if (!op) { set_error("operator is NULL"); return BGB_ERR_INVALID; }
-  if (op->kind == BGB_OP_HELMHOLTZ3D_SL) {
+  if (op->kind == BGB_OP_HELMHOLTZ3D_SL || op->kind == BGB_OP_HELMHOLTZ3D_DL || op->kind == BGB_OP_HELMHOLTZ3D_DLT ||
+      op->kind == BGB_OP_HELMHOLTZ3D_HS) {
     if (a->refspace != BGB_REFSPACE_LAGRANGE_C0D1 || b->refspace != BGB_REFSPACE_LAGRANGE_C0D1) {
-      set_error("Helmholtz3D single layer is implemented on lagrangec0d1 spaces");
+      set_error("Helmholtz3D operators are implemented on lagrangec0d1 spaces");
       return BGB_ERR_NOT_SUPPORTED;
     }
   } else if (op->kind == BGB_OP_MAXWELL3D_SL || op->kind == BGB_OP_MAXWELL3D_DL) {
@@ -291,7 +292,9 @@ double max_edge(const bgb_space* s) {
 
 bool df_singular_ok(const OpParams& op, double edge_t, double edge_b) {
   // singular / near pairs have R <= (edge_t + edge_b) * 2 at most; df_sincos covers |k R| < 400
-  return op.gamma[0] == 0.0 && std::fabs(op.gamma[1]) * 2.0 * (edge_t + edge_b) < 350.0;
+  // the double-float kernel covers the single layers and the Maxwell double layer
+  return op.kind <= BGB_OP_MAXWELL3D_DL && op.gamma[0] == 0.0 &&
+         std::fabs(op.gamma[1]) * 2.0 * (edge_t + edge_b) < 350.0;
 }
 
 static int ensure_ring(bgb_handle* h, size_t bytes) {

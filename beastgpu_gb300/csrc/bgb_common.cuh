@@ -3,10 +3,9 @@
 // Layout of per-triangle data in HBM (built once per space by k_prepare_*):
 //   Geo64   : FP64 vertices, tangents, area -- the classification, Sauter-Schwab, near-pair
 //             and plain-FP64 far kernels read these (80 B + padding per triangle).
-//   Rec32   : FP32 far-pair record for the mixed kernel: double-float centroid, bounding
-//             radius, quadrature-point offsets from the centroid, weights, vertex offsets.
-//   Rec64   : FP64 far-pair record for the plain kernel: absolute quadrature points,
-//             weights, vertices.
+//   far records (layouts Off32 / Off64 in bgb_far_impl.cuh): FP32 record of the mixed kernel
+//             (double-float centroid, radius, 1/(2A), point offsets from the centroid,
+//             weights, vertex offsets) and FP64 record of the plain kernel.
 #pragma once
 
 #include <cstdint>
@@ -68,26 +67,6 @@ struct Geo64 {          // CompScienceMeshes simplex: tangents v_i - v_3, volume
   double pad;
 };
 
-// FP32 far-pair record (mixed kernel).  Q = points of the rule on this side.
-template <int Q>
-struct Rec32 {
-  float ch[3], cl[3];   // centroid, double-float (hi + lo)
-  float rad;            // bounding radius about the centroid (rounded up) + near threshold on the trial side
-  float inv2a;          // 1 / (2 A)   (RT shape scale)
-  float x[Q][3];        // quadrature points minus centroid
-  float w[Q];           // weights incl. Jacobian (sum = A); trial side also carries 1/(4 pi)
-  float vo[3][3];       // vertices minus centroid
-};
-
-// FP64 far-pair record (plain kernel).
-template <int Q>
-struct Rec64 {
-  double x[Q][3];       // absolute quadrature points
-  double w[Q];          // weights incl. Jacobian
-  double v[3][3];       // vertices
-  double inv2a;         // 1 / (2 A)
-};
-
 // Operator parameters as kernels see them.
 struct OpParams {
   int kind;
@@ -110,95 +89,7 @@ struct QuadSel {
   double gl_w[4][BGB_MAX_SS];
 };
 
-// ----------------------------------------------------------------------------------------
-// Shape data at a point (FP64)
-// ----------------------------------------------------------------------------------------
-struct Shp64 {
-  double x[3];
-  double val[3];
-  double vec[3][3];
-  double div;
-};
 
-// Cartesian point and shape values at chart parameters (u, v); BEAST's RTRefSpace form for
-// RT (value_i = (u t1 + v t2 - t_i) / j, divergence 2 / j with j = 2A), barycentric hats
-// for Lagrange.
-__device__ inline void shapes64(const Geo64& T, int refspace, double u, double v, Shp64& S) {
-#pragma unroll
-  for (int c = 0; c < 3; ++c) S.x[c] = __dadd_rn(__dadd_rn(T.v[2][c], __dmul_rn(T.t[0][c], u)), __dmul_rn(T.t[1][c], v));
-  S.val[0] = u;
-  S.val[1] = v;
-  S.val[2] = 1.0 - u - v;
-  if (refspace == BGB_REFSPACE_RT) {
-    double j = T.area * 2.0;
-    double inv_j = 1.0 / j;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      double utu = u * T.t[0][c], vtv = v * T.t[1][c];
-      S.vec[0][c] = ((utu - T.t[0][c]) + vtv) * inv_j;
-      S.vec[1][c] = ((utu + vtv) - T.t[1][c]) * inv_j;
-      S.vec[2][c] = (utu + vtv) * inv_j;
-    }
-    S.div = 2.0 * inv_j;
-  }
-}
-
-// exp(-R gamma) as Julia's complex exp.
-__device__ inline double2 expmg(double R, const OpParams& op) {
-  double zr = -R * op.gamma[0], zi = -R * op.gamma[1];
-  double er = (zr == 0.0) ? 1.0 : exp(zr);
-  if (zi == 0.0) return make_double2(er, zi);
-  double s, c;
-  sincos(zi, &s, &c);
-  return make_double2(er * c, er * s);
-}
-
-// Operator integrand at one point pair with weight `wgt` (quadrature weights and Jacobians),
-// accumulated into L[i][j] (test local i, trial local j).  FP64.
-__device__ inline void accumulate64(const OpParams& op, const Shp64& X, const Shp64& Y, double wgt,
-                                    double2 L[3][3]) {
-  double d0 = X.x[0] - Y.x[0], d1 = X.x[1] - Y.x[1], d2 = X.x[2] - Y.x[2];
-  double R = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
-  double2 e = expmg(R, op);
-  double g = wgt * BGB_INV_4PI_D / R;
-  double2 G = make_double2(g * e.x, g * e.y);
-  double2 alpha = make_double2(op.alpha[0], op.alpha[1]);
-  if (op.kind == BGB_OP_HELMHOLTZ3D_SL) {
-    double2 aG = cmul(alpha, G);
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int j = 0; j < 3; ++j) L[i][j] = cadd(L[i][j], cscale(aG, X.val[i] * Y.val[j]));
-  } else if (op.kind == BGB_OP_MAXWELL3D_SL) {
-    double2 a = cmul(alpha, G), b = cmul(make_double2(op.beta[0], op.beta[1]), G);
-    double dd = X.div * Y.div;
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        double fg = X.vec[i][0] * Y.vec[j][0] + X.vec[i][1] * Y.vec[j][1] + X.vec[i][2] * Y.vec[j][2];
-        L[i][j] = cadd(L[i][j], cadd(cscale(a, fg), cscale(b, dd)));
-      }
-  } else {
-    // grad_x G = -(gamma + 1/R) G r / R
-    double2 Gr = make_double2(G.x / R, G.y / R);
-    double2 H = cmul(make_double2(-op.gamma[0] - 1.0 / R, -op.gamma[1]), Gr);
-    H = cmul(alpha, H);
-    double r[3] = {d0, d1, d2};
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        const double* f = X.vec[i];
-        const double* q = Y.vec[j];
-        double c0 = r[1] * q[2] - r[2] * q[1];
-        double c1 = r[2] * q[0] - r[0] * q[2];
-        double c2 = r[0] * q[1] - r[1] * q[0];
-        double trip = f[0] * c0 + f[1] * c1 + f[2] * c2;
-        L[i][j] = cadd(L[i][j], cscale(H, trip));
-      }
-  }
-}
 
 // FP32 bounding-sphere test shared by the classifier and the far-pair kernels (identical
 // rounding in both): true if the pair may be non-far.

@@ -6,9 +6,15 @@ namespace farimpl {
 BGB_FAR_EXTERN(PMixed, 0)
 BGB_FAR_EXTERN(PMixed, 1)
 BGB_FAR_EXTERN(PMixed, 2)
+BGB_FAR_EXTERN(PMixed, 3)
+BGB_FAR_EXTERN(PMixed, 4)
+BGB_FAR_EXTERN(PMixed, 5)
 BGB_FAR_EXTERN(PFp64, 0)
 BGB_FAR_EXTERN(PFp64, 1)
 BGB_FAR_EXTERN(PFp64, 2)
+BGB_FAR_EXTERN(PFp64, 3)
+BGB_FAR_EXTERN(PFp64, 4)
+BGB_FAR_EXTERN(PFp64, 5)
 
 template <class P, int QT, int QB>
 static int dispatch_diag(const FarConst& K, const void* rt, const void* rb, const int* tau, const int* sigma,
@@ -17,6 +23,9 @@ static int dispatch_diag(const FarConst& K, const void* rt, const void* rb, cons
     case BGB_OP_HELMHOLTZ3D_SL: return launch_diag_t<P, BGB_OP_HELMHOLTZ3D_SL, QT, QB>(K, rt, rb, tau, sigma, n, out, st);
     case BGB_OP_MAXWELL3D_SL: return launch_diag_t<P, BGB_OP_MAXWELL3D_SL, QT, QB>(K, rt, rb, tau, sigma, n, out, st);
     case BGB_OP_MAXWELL3D_DL: return launch_diag_t<P, BGB_OP_MAXWELL3D_DL, QT, QB>(K, rt, rb, tau, sigma, n, out, st);
+    case BGB_OP_HELMHOLTZ3D_DL: return launch_diag_t<P, BGB_OP_HELMHOLTZ3D_DL, QT, QB>(K, rt, rb, tau, sigma, n, out, st);
+    case BGB_OP_HELMHOLTZ3D_DLT: return launch_diag_t<P, BGB_OP_HELMHOLTZ3D_DLT, QT, QB>(K, rt, rb, tau, sigma, n, out, st);
+    case BGB_OP_HELMHOLTZ3D_HS: return launch_diag_t<P, BGB_OP_HELMHOLTZ3D_HS, QT, QB>(K, rt, rb, tau, sigma, n, out, st);
   }
   set_error("unknown operator kind %d", K.op_kind);
   return BGB_ERR_INVALID;
@@ -31,6 +40,12 @@ static int dispatch_persistent(int op_kind, const FarConst* Ks, const TilePlan* 
       return launch_persistent_t<P, BGB_OP_MAXWELL3D_SL, QT, QB>(Ks, plans, items, nitems, counter, smem, ctas, ab, st);
     case BGB_OP_MAXWELL3D_DL:
       return launch_persistent_t<P, BGB_OP_MAXWELL3D_DL, QT, QB>(Ks, plans, items, nitems, counter, smem, ctas, ab, st);
+    case BGB_OP_HELMHOLTZ3D_DL:
+      return launch_persistent_t<P, BGB_OP_HELMHOLTZ3D_DL, QT, QB>(Ks, plans, items, nitems, counter, smem, ctas, ab, st);
+    case BGB_OP_HELMHOLTZ3D_DLT:
+      return launch_persistent_t<P, BGB_OP_HELMHOLTZ3D_DLT, QT, QB>(Ks, plans, items, nitems, counter, smem, ctas, ab, st);
+    case BGB_OP_HELMHOLTZ3D_HS:
+      return launch_persistent_t<P, BGB_OP_HELMHOLTZ3D_HS, QT, QB>(Ks, plans, items, nitems, counter, smem, ctas, ab, st);
   }
   set_error("unknown operator kind %d", op_kind);
   return BGB_ERR_INVALID;
@@ -42,6 +57,9 @@ static int dispatch_occupancy(int op_kind, size_t smem, int* per_sm) {
     case BGB_OP_HELMHOLTZ3D_SL: return occupancy_t<P, BGB_OP_HELMHOLTZ3D_SL, QT, QB>(smem, per_sm);
     case BGB_OP_MAXWELL3D_SL: return occupancy_t<P, BGB_OP_MAXWELL3D_SL, QT, QB>(smem, per_sm);
     case BGB_OP_MAXWELL3D_DL: return occupancy_t<P, BGB_OP_MAXWELL3D_DL, QT, QB>(smem, per_sm);
+    case BGB_OP_HELMHOLTZ3D_DL: return occupancy_t<P, BGB_OP_HELMHOLTZ3D_DL, QT, QB>(smem, per_sm);
+    case BGB_OP_HELMHOLTZ3D_DLT: return occupancy_t<P, BGB_OP_HELMHOLTZ3D_DLT, QT, QB>(smem, per_sm);
+    case BGB_OP_HELMHOLTZ3D_HS: return occupancy_t<P, BGB_OP_HELMHOLTZ3D_HS, QT, QB>(smem, per_sm);
   }
   set_error("unknown operator kind %d", op_kind);
   return BGB_ERR_INVALID;

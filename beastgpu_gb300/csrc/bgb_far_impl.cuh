@@ -39,6 +39,30 @@ constexpr float kPiC = (float)(kTwoPi - 6.28125 - (double)(float)(kTwoPi - 6.281
 constexpr float kInv2Pi = (float)(1.0 / kTwoPi);
 constexpr int kThreads = 256;
 
+// Operators on Lagrange hats: Helmholtz single layer, double layer, transposed double layer,
+// hypersingular.  They share the hat accumulation of the single layer.
+__host__ __device__ constexpr bool is_lagrange_op(int op) {
+  return op == BGB_OP_HELMHOLTZ3D_SL || op == BGB_OP_HELMHOLTZ3D_DL || op == BGB_OP_HELMHOLTZ3D_DLT ||
+         op == BGB_OP_HELMHOLTZ3D_HS;
+}
+// Unit normal (v0 - v2) x (v1 - v2) / (2A) from the centroid-relative vertices vo[3][3].
+template <class T>
+__device__ __forceinline__ void tri_normal(const T* vo, T inv2a, T n[3]) {
+  const T a0 = vo[0] - vo[6], a1 = vo[1] - vo[7], a2 = vo[2] - vo[8];
+  const T b0 = vo[3] - vo[6], b1 = vo[4] - vo[7], b2 = vo[5] - vo[8];
+  n[0] = (a1 * b2 - a2 * b1) * inv2a;
+  n[1] = (a2 * b0 - a0 * b2) * inv2a;
+  n[2] = (a0 * b1 - a1 * b0) * inv2a;
+}
+// Surface curls of the hats, n x grad(lambda_i) = (v_{i+1} - v_{i+2}) / (2A).
+template <class T>
+__device__ __forceinline__ void tri_curls(const T* vo, T inv2a, T c[3][3]) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) c[i][k] = (vo[3 * ((i + 1) % 3) + k] - vo[3 * ((i + 2) % 3) + k]) * inv2a;
+}
+
 template <int Q>
 struct Off32 {
   static constexpr int CH = 0, CL = 3, RAD = 6, INV2A = 7, X = 8, W = 8 + 3 * Q, VO = 8 + 4 * Q, SIZE = 17 + 4 * Q;
@@ -107,6 +131,10 @@ __device__ __forceinline__ void far_pair_mixed(const FarScalars& K, const float 
   const float D2x = 2.f * Dh[0], D2y = 2.f * Dh[1], D2z = 2.f * Dh[2];
   const float kh = K.k_hi;
   const float amp0 = K.lossy ? __expf(-K.gre * R0) : 1.f;
+  constexpr bool kHH = is_lagrange_op(OP);
+  float nA[3] = {0.f, 0.f, 0.f}, nB[3] = {0.f, 0.f, 0.f};
+  if (OP == BGB_OP_HELMHOLTZ3D_DLT || OP == BGB_OP_HELMHOLTZ3D_HS) tri_normal(a + OA::VO, a[OA::INV2A], nA);
+  if (OP == BGB_OP_HELMHOLTZ3D_DL || OP == BGB_OP_HELMHOLTZ3D_HS) tri_normal(b + OB::VO, b[OB::INV2A], nB);
   const int qt = QT < BGB_MAXQ ? QT : K.qt;
   const int qb = QB < BGB_MAXQ ? QB : K.qb;
 
@@ -141,6 +169,10 @@ __device__ __forceinline__ void far_pair_mixed(const FarScalars& K, const float 
       const float ax = Dl[0] + Xx, ay = Dl[1] + Xy, az = Dl[2] + Xz;
       const float KI = fmaf(ax, ax + D2x, fmaf(ay, ay + D2y, fmaf(az, az + D2z, c0)));
       const float wI = a[OA::W + I];
+      // double layer: (x - y) . n_y = (D + X_I) . n_y, constant over the trial points
+      const float cI = OP == BGB_OP_HELMHOLTZ3D_DL
+                           ? fmaf(Dh[0] + ax, nB[0], fmaf(Dh[1] + ay, nB[1], (Dh[2] + az) * nB[2]))
+                           : 1.f;
       float2 TI = make_float2(0.f, 0.f);
       float2 UI[3], M[3];
 #pragma unroll
@@ -171,12 +203,24 @@ __device__ __forceinline__ void far_pair_mixed(const FarScalars& K, const float 
         float amp = (wI * b[OB::W + J]) * rs;
         if (K.lossy) amp *= amp0 * __expf(-K.gre * delta);
         const float gr = amp * cs, gi = -amp * sn;
-        if (OP == BGB_OP_HELMHOLTZ3D_SL) {
+        if (kHH) {
+          float hr = gr, hi = gi;
+          if (OP == BGB_OP_HELMHOLTZ3D_DL || OP == BGB_OP_HELMHOLTZ3D_DLT) {
+            // (gamma + 1/R) G / R, times -(x - y) . n_x = -(D - y_J) . n_x for the transposed layer
+            const float t = (K.gre + rs) * rs, u = kh * rs;
+            hr = t * gr - u * gi;
+            hi = t * gi + u * gr;
+            if (OP == BGB_OP_HELMHOLTZ3D_DLT) {
+              const float e = -fmaf(Dh[0] + (Dl[0] - yx), nA[0], fmaf(Dh[1] + (Dl[1] - yy), nA[1], (Dh[2] + (Dl[2] - yz)) * nA[2]));
+              hr *= e;
+              hi *= e;
+            }
+          }
 #pragma unroll
           for (int j = 0; j < 3; ++j) {
             const float g = shpB[J][j];
-            M[j].x = fmaf(gr, g, M[j].x);
-            M[j].y = fmaf(gi, g, M[j].y);
+            M[j].x = fmaf(hr, g, M[j].x);
+            M[j].y = fmaf(hi, g, M[j].y);
           }
         } else {
           TI.x += gr;
@@ -186,10 +230,10 @@ __device__ __forceinline__ void far_pair_mixed(const FarScalars& K, const float 
           UI[2].x = fmaf(gr, yz, UI[2].x); UI[2].y = fmaf(gi, yz, UI[2].y);
         }
       }
-      if (OP == BGB_OP_HELMHOLTZ3D_SL) {
+      if (kHH) {
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-          const float f = shpT[I][i];
+          const float f = shpT[I][i] * cI;
 #pragma unroll
           for (int j = 0; j < 3; ++j) {
             L[i * 3 + j].x = fmaf(f, M[j].x, L[i * 3 + j].x);
@@ -306,7 +350,28 @@ __device__ __forceinline__ void far_pair_mixed(const FarScalars& K, const float 
 
   }
   const float2 alpha = make_float2(K.alpha32[0], K.alpha32[1]);
-  if (OP == BGB_OP_HELMHOLTZ3D_SL) {
+  if (OP == BGB_OP_HELMHOLTZ3D_HS) {
+    // alpha (n_x . n_y) int int f g G + beta (curl f . curl g) int int G, int int G = sum of L
+    float2 P = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) { P.x += L[k].x; P.y += L[k].y; }
+    const float nn = fmaf(nA[0], nB[0], fmaf(nA[1], nB[1], nA[2] * nB[2]));
+    const float2 an = make_float2(alpha.x * nn, alpha.y * nn);
+    const float2 bP = cmulf(make_float2(K.beta32[0], K.beta32[1]), P);
+    float cA[3][3], cB[3][3];
+    tri_curls(a + OA::VO, a[OA::INV2A], cA);
+    tri_curls(b + OB::VO, b[OB::INV2A], cB);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const float cc = fmaf(cA[i][0], cB[j][0], fmaf(cA[i][1], cB[j][1], cA[i][2] * cB[j][2]));
+        const float2 t = cmulf(an, L[i * 3 + j]);
+        L[i * 3 + j] = make_float2(fmaf(cc, bP.x, t.x), fmaf(cc, bP.y, t.y));
+      }
+    return;
+  }
+  if (kHH) {
 #pragma unroll
     for (int k = 0; k < 9; ++k) L[k] = cmulf(alpha, L[k]);
     return;
@@ -382,8 +447,12 @@ __device__ __forceinline__ void far_pair_fp64(const FarScalars& K, const double 
                                               const double* __restrict__ b, double2 L[9]) {
   using OA = Off64<QT>;
   using OB = Off64<QB>;
+  constexpr bool kHH = is_lagrange_op(OP);
   const double Dx = a[OA::C] - b[OB::C], Dy = a[OA::C + 1] - b[OB::C + 1], Dz = a[OA::C + 2] - b[OB::C + 2];
   const double gre = K.gamma[0], gim = K.gamma[1];
+  double nA[3] = {0, 0, 0}, nB[3] = {0, 0, 0};
+  if (OP == BGB_OP_HELMHOLTZ3D_DLT || OP == BGB_OP_HELMHOLTZ3D_HS) tri_normal(a + OA::VO, a[OA::INV2A], nA);
+  if (OP == BGB_OP_HELMHOLTZ3D_DL || OP == BGB_OP_HELMHOLTZ3D_HS) tri_normal(b + OB::VO, b[OB::INV2A], nB);
   const int qt = QT < BGB_MAXQ ? QT : K.qt;
   const int qb = QB < BGB_MAXQ ? QB : K.qb;
   double2 S = make_double2(0, 0), P0 = make_double2(0, 0);
@@ -398,6 +467,8 @@ __device__ __forceinline__ void far_pair_fp64(const FarScalars& K, const double 
     const double Xx = a[OA::X + 3 * I], Xy = a[OA::X + 3 * I + 1], Xz = a[OA::X + 3 * I + 2];
     const double ax = Dx + Xx, ay = Dy + Xy, az = Dz + Xz;
     const double wI = a[OA::W + I];
+    // double layer: (x - y) . n_y = (D + X_I) . n_y, constant over the trial points
+    const double cI = OP == BGB_OP_HELMHOLTZ3D_DL ? ax * nB[0] + ay * nB[1] + az * nB[2] : 1.0;
     double2 TI = make_double2(0, 0);
     double2 UI[3], EI[3], BI[3], M[3];
 #pragma unroll
@@ -415,12 +486,24 @@ __device__ __forceinline__ void far_pair_fp64(const FarScalars& K, const double 
       double amp = wI * b[OB::W + J] * rinv;
       if (gre != 0.0) amp *= exp(-gre * R);
       const double gr = amp * cs, gi = -amp * sn;
-      if (OP == BGB_OP_HELMHOLTZ3D_SL) {
+      if (kHH) {
+        double hr = gr, hi = gi;
+        if (OP == BGB_OP_HELMHOLTZ3D_DL || OP == BGB_OP_HELMHOLTZ3D_DLT) {
+          // (gamma + 1/R) G / R, times -(x - y) . n_x for the transposed double layer
+          const double t = (gre + rinv) * rinv, u = gim * rinv;
+          hr = t * gr - u * gi;
+          hi = t * gi + u * gr;
+          if (OP == BGB_OP_HELMHOLTZ3D_DLT) {
+            const double e = -(dx * nA[0] + dy * nA[1] + dz * nA[2]);
+            hr *= e;
+            hi *= e;
+          }
+        }
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
           const double g = shpB[J][j];
-          M[j].x = fma(gr, g, M[j].x);
-          M[j].y = fma(gi, g, M[j].y);
+          M[j].x = fma(hr, g, M[j].x);
+          M[j].y = fma(hi, g, M[j].y);
         }
       } else if (OP == BGB_OP_MAXWELL3D_SL) {
         TI.x += gr;
@@ -441,10 +524,10 @@ __device__ __forceinline__ void far_pair_fp64(const FarScalars& K, const double 
         BI[2].x = fma(Hx, c0z, BI[2].x); BI[2].y = fma(Hy, c0z, BI[2].y);
       }
     }
-    if (OP == BGB_OP_HELMHOLTZ3D_SL) {
+    if (kHH) {
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
-        const double f = shpT[I][i];
+        const double f = shpT[I][i] * cI;
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
           L[i * 3 + j].x = fma(f, M[j].x, L[i * 3 + j].x);
@@ -475,7 +558,28 @@ __device__ __forceinline__ void far_pair_fp64(const FarScalars& K, const double 
     }
   }
   const double2 alpha = make_double2(K.alpha[0], K.alpha[1]);
-  if (OP == BGB_OP_HELMHOLTZ3D_SL) {
+  if (OP == BGB_OP_HELMHOLTZ3D_HS) {
+    // alpha (n_x . n_y) int int f g G + beta (curl f . curl g) int int G, int int G = sum of L
+    double2 P = make_double2(0, 0);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) { P.x += L[k].x; P.y += L[k].y; }
+    const double nn = nA[0] * nB[0] + nA[1] * nB[1] + nA[2] * nB[2];
+    const double2 an = make_double2(alpha.x * nn, alpha.y * nn);
+    const double2 bP = cmul(make_double2(K.beta[0], K.beta[1]), P);
+    double cA[3][3], cB[3][3];
+    tri_curls(a + OA::VO, a[OA::INV2A], cA);
+    tri_curls(b + OB::VO, b[OB::INV2A], cB);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const double cc = cA[i][0] * cB[j][0] + cA[i][1] * cB[j][1] + cA[i][2] * cB[j][2];
+        const double2 t = cmul(an, L[i * 3 + j]);
+        L[i * 3 + j] = make_double2(fma(cc, bP.x, t.x), fma(cc, bP.y, t.y));
+      }
+    return;
+  }
+  if (kHH) {
 #pragma unroll
     for (int k = 0; k < 9; ++k) L[k] = cmul(alpha, L[k]);
     return;

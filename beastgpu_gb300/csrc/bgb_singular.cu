@@ -187,7 +187,23 @@ __global__ void k_classify_dense(const Geo64* __restrict__ tg, const Geo64* __re
 //                 grad_x G = H d, d = x - y.
 // ----------------------------------------------------------------------------------------
 template <int OP>
-struct NAcc { static constexpr int N = OP == BGB_OP_HELMHOLTZ3D_SL ? 9 : (OP == BGB_OP_MAXWELL3D_SL ? 8 : 10); };
+struct NAcc { static constexpr int N = OP == BGB_OP_MAXWELL3D_SL ? 8 : (OP == BGB_OP_MAXWELL3D_DL ? 10 : 9); };
+
+// The Helmholtz operators on Lagrange hats share the 9 hat moments.
+__host__ __device__ constexpr bool hat_op(int op) {
+  return op == BGB_OP_HELMHOLTZ3D_SL || op == BGB_OP_HELMHOLTZ3D_DL || op == BGB_OP_HELMHOLTZ3D_DLT ||
+         op == BGB_OP_HELMHOLTZ3D_HS;
+}
+// Double layers vanish on a flat common face ((x - y) . n = 0).
+__host__ __device__ constexpr bool flat_face_zero(int op) {
+  return op == BGB_OP_MAXWELL3D_DL || op == BGB_OP_HELMHOLTZ3D_DL || op == BGB_OP_HELMHOLTZ3D_DLT;
+}
+__device__ inline void unit_normal(const Geo64& T, double n[3]) {
+  const double inv = 1.0 / (2.0 * T.area);
+  n[0] = (T.t[0][1] * T.t[1][2] - T.t[0][2] * T.t[1][1]) * inv;
+  n[1] = (T.t[0][2] * T.t[1][0] - T.t[0][0] * T.t[1][2]) * inv;
+  n[2] = (T.t[0][0] * T.t[1][1] - T.t[0][1] * T.t[1][0]) * inv;
+}
 
 struct PairGeo {
   double xa[3][3];   // x = xa[0] + xa[1] u1 + xa[2] u2   (test point from SS chart params)
@@ -225,7 +241,8 @@ __device__ inline void make_pair_geo(const Geo64& A, const Geo64& B, const Chart
 template <int OP>
 __device__ __forceinline__ void add_point(const OpParams& op, const double x[3], const double y[3], double bx1,
                                           double bx2, double by1, double by2, const double cA[3],
-                                          const double cB[3], double w, double2* acc) {
+                                          const double cB[3], const double nA[3], const double nB[3], double w,
+                                          double2* acc) {
   const double d0 = x[0] - y[0], d1 = x[1] - y[1], d2 = x[2] - y[2];
   const double R2 = d0 * d0 + d1 * d1 + d2 * d2;
   const double rinv = rsqrt(R2);
@@ -235,15 +252,25 @@ __device__ __forceinline__ void add_point(const OpParams& op, const double x[3],
   double amp = w * BGB_INV_4PI_D * rinv;
   if (op.gamma[0] != 0.0) amp *= exp(-op.gamma[0] * R);
   const double gr = amp * cs, gi = -amp * sn;
-  if (OP == BGB_OP_HELMHOLTZ3D_SL) {
+  if (hat_op(OP)) {
+    double hr = gr, hi = gi;
+    if (OP == BGB_OP_HELMHOLTZ3D_DL || OP == BGB_OP_HELMHOLTZ3D_DLT) {
+      // dG/dn_y = (gamma + 1/R) G ((x - y) . n_y) / R; dG/dn_x = -(gamma + 1/R) G ((x - y) . n_x) / R
+      const double* nv = OP == BGB_OP_HELMHOLTZ3D_DL ? nB : nA;
+      double rn = (d0 * nv[0] + d1 * nv[1] + d2 * nv[2]) * rinv;
+      if (OP == BGB_OP_HELMHOLTZ3D_DLT) rn = -rn;
+      const double t = (op.gamma[0] + rinv) * rn, u = op.gamma[1] * rn;
+      hr = t * gr - u * gi;
+      hi = t * gi + u * gr;
+    }
     const double p[3] = {1.0, bx1, bx2}, q[3] = {1.0, by1, by2};
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll
       for (int b = 0; b < 3; ++b) {
         const double pq = p[a] * q[b];
-        acc[a * 3 + b].x = fma(gr, pq, acc[a * 3 + b].x);
-        acc[a * 3 + b].y = fma(gi, pq, acc[a * 3 + b].y);
+        acc[a * 3 + b].x = fma(hr, pq, acc[a * 3 + b].x);
+        acc[a * 3 + b].y = fma(hi, pq, acc[a * 3 + b].y);
       }
   } else if (OP == BGB_OP_MAXWELL3D_SL) {
     const double X0 = x[0] - cA[0], X1 = x[1] - cA[1], X2 = x[2] - cA[2];
@@ -281,19 +308,41 @@ template <int OP>
 __device__ inline void finalize(const OpParams& op, const Geo64& A, const Geo64& B, const double cA[3],
                                 const double cB[3], const double2* acc, double2 L[3][3]) {
   const double2 alpha = make_double2(op.alpha[0], op.alpha[1]);
-  if (OP == BGB_OP_HELMHOLTZ3D_SL) {
+  if (hat_op(OP)) {
     // f = T p with T = [[0,1,0],[0,0,1],[1,-1,-1]]
     const double T[3][3] = {{0, 1, 0}, {0, 0, 1}, {1, -1, -1}};
+    double2 a = alpha, bP = make_double2(0, 0);
+    double cA3[3][3], cB3[3][3];
+    if (OP == BGB_OP_HELMHOLTZ3D_HS) {
+      // alpha (n_x . n_y) int int f g G + beta (curl f . curl g) int int G, int int G = acc[0]
+      double nA[3], nB[3];
+      unit_normal(A, nA);
+      unit_normal(B, nB);
+      const double nn = nA[0] * nB[0] + nA[1] * nB[1] + nA[2] * nB[2];
+      a = make_double2(alpha.x * nn, alpha.y * nn);
+      bP = cmul(make_double2(op.beta[0], op.beta[1]), acc[0]);
+      const double ia = 1.0 / (2.0 * A.area), ib = 1.0 / (2.0 * B.area);
+      for (int i = 0; i < 3; ++i)
+        for (int c = 0; c < 3; ++c) {  // curl of hat i: (v_{i+1} - v_{i+2}) / (2A)
+          cA3[i][c] = (A.v[(i + 1) % 3][c] - A.v[(i + 2) % 3][c]) * ia;
+          cB3[i][c] = (B.v[(i + 1) % 3][c] - B.v[(i + 2) % 3][c]) * ib;
+        }
+    }
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) {
         double2 s = make_double2(0, 0);
-        for (int a = 0; a < 3; ++a)
-          for (int b = 0; b < 3; ++b) {
-            const double t = T[i][a] * T[j][b];
-            s.x += t * acc[a * 3 + b].x;
-            s.y += t * acc[a * 3 + b].y;
+        for (int p = 0; p < 3; ++p)
+          for (int q = 0; q < 3; ++q) {
+            const double t = T[i][p] * T[j][q];
+            s.x += t * acc[p * 3 + q].x;
+            s.y += t * acc[p * 3 + q].y;
           }
-        L[i][j] = cmul(alpha, s);
+        L[i][j] = cmul(a, s);
+        if (OP == BGB_OP_HELMHOLTZ3D_HS) {
+          const double cc = cA3[i][0] * cB3[j][0] + cA3[i][1] * cB3[j][1] + cA3[i][2] * cB3[j][2];
+          L[i][j].x += cc * bP.x;
+          L[i][j].y += cc * bP.y;
+        }
       }
     return;
   }
@@ -350,11 +399,13 @@ __device__ void pair_integral64(const OpParams& op, const QuadSel& qs, const Rul
   double2 acc[NA];
 #pragma unroll
   for (int k = 0; k < NA; ++k) acc[k] = make_double2(0.0, 0.0);
-  double cA[3], cB[3];
+  double cA[3], cB[3], nA[3] = {0, 0, 0}, nB[3] = {0, 0, 0};
   for (int c = 0; c < 3; ++c) {
     cA[c] = (A.v[0][c] + A.v[1][c] + A.v[2][c]) / 3.0;
     cB[c] = (B.v[0][c] + B.v[1][c] + B.v[2][c]) / 3.0;
   }
+  if (OP == BGB_OP_HELMHOLTZ3D_DLT) unit_normal(A, nA);
+  if (OP == BGB_OP_HELMHOLTZ3D_DL) unit_normal(B, nB);
   if (cls == BGB_CLASS_NEAR || cls == BGB_CLASS_FAR) {
     const int rt = cls == BGB_CLASS_NEAR ? qs.near_t : qs.far_t;
     const int rb = cls == BGB_CLASS_NEAR ? qs.near_b : qs.far_b;
@@ -369,9 +420,9 @@ __device__ void pair_integral64(const OpParams& op, const QuadSel& qs, const Rul
         y[c] = __dadd_rn(__dadd_rn(B.v[2][c], __dmul_rn(B.t[0][c], q[0])), __dmul_rn(B.t[1][c], q[1]));
       }
       const double w = ((p[2] / 2.0) * (A.area * 2.0)) * ((q[2] / 2.0) * (B.area * 2.0));
-      add_point<OP>(op, x, y, p[0], p[1], q[0], q[1], cA, cB, w, acc);
+      add_point<OP>(op, x, y, p[0], p[1], q[0], q[1], cA, cB, nA, nB, w, acc);
     }
-  } else if (!(OP == BGB_OP_MAXWELL3D_DL && cls == BGB_CLASS_CF)) {  // DL on a flat face is 0
+  } else if (!(flat_face_zero(OP) && cls == BGB_CLASS_CF)) {  // double layers on a flat face are 0
     int I[3], J[3];
     ss_permutation(cls, A, B, I, J);
     Chart chA, chB;
@@ -398,13 +449,13 @@ __device__ void pair_integral64(const OpParams& op, const QuadSel& qs, const Rul
           y[c] = P.xb[0][c] + P.xb[1][c] * v1 + P.xb[2][c] * v2;
         }
         double bx1 = 0, bx2 = 0, by1 = 0, by2 = 0;
-        if (OP == BGB_OP_HELMHOLTZ3D_SL) {
+        if (hat_op(OP)) {
           bx1 = P.ba[0][0] + P.ba[1][0] * u1 + P.ba[2][0] * u2;
           bx2 = P.ba[0][1] + P.ba[1][1] * u1 + P.ba[2][1] * u2;
           by1 = P.bb[0][0] + P.bb[1][0] * v1 + P.bb[2][0] * v2;
           by2 = P.bb[0][1] + P.bb[1][1] * v1 + P.bb[2][1] * v2;
         }
-        add_point<OP>(op, x, y, bx1, bx2, by1, by2, cA, cB, jac * mul, acc);
+        add_point<OP>(op, x, y, bx1, bx2, by1, by2, cA, cB, nA, nB, jac * mul, acc);
       }
     }
   }
@@ -615,12 +666,14 @@ void launch_singular(const OpParams& op, const QuadSel& qs, const RuleTable& rul
   if (n <= 0) return;
   int64_t blocks = (n + 7) / 8;
   if (blocks > (int64_t)num_sms * 32) blocks = (int64_t)num_sms * 32;
-  if (op.kind == BGB_OP_HELMHOLTZ3D_SL)
-    k_singular<BGB_OP_HELMHOLTZ3D_SL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, et, es, ec, n, out, abort_flag);
-  else if (op.kind == BGB_OP_MAXWELL3D_SL)
-    k_singular<BGB_OP_MAXWELL3D_SL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, et, es, ec, n, out, abort_flag);
-  else
-    k_singular<BGB_OP_MAXWELL3D_DL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, et, es, ec, n, out, abort_flag);
+  switch (op.kind) {
+    case BGB_OP_HELMHOLTZ3D_SL: k_singular<BGB_OP_HELMHOLTZ3D_SL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, et, es, ec, n, out, abort_flag); break;
+    case BGB_OP_MAXWELL3D_SL: k_singular<BGB_OP_MAXWELL3D_SL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, et, es, ec, n, out, abort_flag); break;
+    case BGB_OP_MAXWELL3D_DL: k_singular<BGB_OP_MAXWELL3D_DL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, et, es, ec, n, out, abort_flag); break;
+    case BGB_OP_HELMHOLTZ3D_DL: k_singular<BGB_OP_HELMHOLTZ3D_DL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, et, es, ec, n, out, abort_flag); break;
+    case BGB_OP_HELMHOLTZ3D_DLT: k_singular<BGB_OP_HELMHOLTZ3D_DLT><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, et, es, ec, n, out, abort_flag); break;
+    case BGB_OP_HELMHOLTZ3D_HS: k_singular<BGB_OP_HELMHOLTZ3D_HS><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, et, es, ec, n, out, abort_flag); break;
+  }
 }
 void launch_local_diag64(const OpParams& op, const QuadSel& qs, const RuleTable& rules, int rsA, int rsB,
                          const Geo64* tg, const Geo64* bg, const int* tau, const int* sigma, int64_t n, int force,
@@ -630,12 +683,14 @@ void launch_local_diag64(const OpParams& op, const QuadSel& qs, const RuleTable&
   if (n <= 0) return;
   int64_t blocks = (n + 7) / 8;
   if (blocks > (int64_t)num_sms * 32) blocks = (int64_t)num_sms * 32;
-  if (op.kind == BGB_OP_HELMHOLTZ3D_SL)
-    k_local_diag64<BGB_OP_HELMHOLTZ3D_SL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, tau, sigma, n, force, out, cls, mask, err);
-  else if (op.kind == BGB_OP_MAXWELL3D_SL)
-    k_local_diag64<BGB_OP_MAXWELL3D_SL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, tau, sigma, n, force, out, cls, mask, err);
-  else
-    k_local_diag64<BGB_OP_MAXWELL3D_DL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, tau, sigma, n, force, out, cls, mask, err);
+  switch (op.kind) {
+    case BGB_OP_HELMHOLTZ3D_SL: k_local_diag64<BGB_OP_HELMHOLTZ3D_SL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, tau, sigma, n, force, out, cls, mask, err); break;
+    case BGB_OP_MAXWELL3D_SL: k_local_diag64<BGB_OP_MAXWELL3D_SL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, tau, sigma, n, force, out, cls, mask, err); break;
+    case BGB_OP_MAXWELL3D_DL: k_local_diag64<BGB_OP_MAXWELL3D_DL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, tau, sigma, n, force, out, cls, mask, err); break;
+    case BGB_OP_HELMHOLTZ3D_DL: k_local_diag64<BGB_OP_HELMHOLTZ3D_DL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, tau, sigma, n, force, out, cls, mask, err); break;
+    case BGB_OP_HELMHOLTZ3D_DLT: k_local_diag64<BGB_OP_HELMHOLTZ3D_DLT><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, tau, sigma, n, force, out, cls, mask, err); break;
+    case BGB_OP_HELMHOLTZ3D_HS: k_local_diag64<BGB_OP_HELMHOLTZ3D_HS><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, tau, sigma, n, force, out, cls, mask, err); break;
+  }
 }
 
 void launch_prepare_bounds_batched(const Geo64* g, int nt, const int* tri_problem, const double* prob_k2, int trial_side,
@@ -663,12 +718,14 @@ void launch_singular_batched(int op_kind, const OpParams* ops, const QuadSel& qs
   if (n <= 0) return;
   int64_t blocks = (n + 7) / 8;
   if (blocks > (int64_t)num_sms * 32) blocks = (int64_t)num_sms * 32;
-  if (op_kind == BGB_OP_HELMHOLTZ3D_SL)
-    k_singular_batched<BGB_OP_HELMHOLTZ3D_SL><<<(int)blocks, 256, 0, st>>>(ops, qs, rules, tg, bg, tri_problem, et, es, ec, n, out, abort_flag);
-  else if (op_kind == BGB_OP_MAXWELL3D_SL)
-    k_singular_batched<BGB_OP_MAXWELL3D_SL><<<(int)blocks, 256, 0, st>>>(ops, qs, rules, tg, bg, tri_problem, et, es, ec, n, out, abort_flag);
-  else
-    k_singular_batched<BGB_OP_MAXWELL3D_DL><<<(int)blocks, 256, 0, st>>>(ops, qs, rules, tg, bg, tri_problem, et, es, ec, n, out, abort_flag);
+  switch (op_kind) {
+    case BGB_OP_HELMHOLTZ3D_SL: k_singular_batched<BGB_OP_HELMHOLTZ3D_SL><<<(int)blocks, 256, 0, st>>>(ops, qs, rules, tg, bg, tri_problem, et, es, ec, n, out, abort_flag); break;
+    case BGB_OP_MAXWELL3D_SL: k_singular_batched<BGB_OP_MAXWELL3D_SL><<<(int)blocks, 256, 0, st>>>(ops, qs, rules, tg, bg, tri_problem, et, es, ec, n, out, abort_flag); break;
+    case BGB_OP_MAXWELL3D_DL: k_singular_batched<BGB_OP_MAXWELL3D_DL><<<(int)blocks, 256, 0, st>>>(ops, qs, rules, tg, bg, tri_problem, et, es, ec, n, out, abort_flag); break;
+    case BGB_OP_HELMHOLTZ3D_DL: k_singular_batched<BGB_OP_HELMHOLTZ3D_DL><<<(int)blocks, 256, 0, st>>>(ops, qs, rules, tg, bg, tri_problem, et, es, ec, n, out, abort_flag); break;
+    case BGB_OP_HELMHOLTZ3D_DLT: k_singular_batched<BGB_OP_HELMHOLTZ3D_DLT><<<(int)blocks, 256, 0, st>>>(ops, qs, rules, tg, bg, tri_problem, et, es, ec, n, out, abort_flag); break;
+    case BGB_OP_HELMHOLTZ3D_HS: k_singular_batched<BGB_OP_HELMHOLTZ3D_HS><<<(int)blocks, 256, 0, st>>>(ops, qs, rules, tg, bg, tri_problem, et, es, ec, n, out, abort_flag); break;
+  }
 }
 
 }  // namespace bgb

@@ -435,9 +435,9 @@ void launch_singular_df(int op_kind, const OpDf& op, const OpDf* opdf_array, con
     BGB_LAUNCH_DF(BGB_OP_HELMHOLTZ3D_SL)
   } else if (op_kind == BGB_OP_MAXWELL3D_SL) {
     BGB_LAUNCH_DF(BGB_OP_MAXWELL3D_SL)
-  } else {
+  } else if (op_kind == BGB_OP_MAXWELL3D_DL) {
     BGB_LAUNCH_DF(BGB_OP_MAXWELL3D_DL)
-  }
+  }  // other operators take the FP64 singular kernel (df_singular_ok)
 #undef BGB_LAUNCH_DF
 }
 

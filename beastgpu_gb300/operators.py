@@ -1,6 +1,7 @@
 """Boundary integral operators and quadrature strategies, BEAST-style.
 
 Mirrors the constructors a BEAST user calls (`Helmholtz3D.singlelayer(wavenumber=k)`,
+`Helmholtz3D.doublelayer`, `.doublelayer_transposed`, `.hypersingular`,
 `Maxwell3D.singlelayer(wavenumber=k)`, `Maxwell3D.doublelayer(wavenumber=k)`) and the
 operator fields the reference reads (`biop.alpha`, `biop.gamma`,
 doubleQuadRuleMainCase.jl:168-169; SauterSchwab.jl:319-320).  The Green function is
@@ -13,9 +14,14 @@ from dataclasses import dataclass
 OP_HELMHOLTZ3D_SL = 0
 OP_MAXWELL3D_SL = 1
 OP_MAXWELL3D_DL = 2
+OP_HELMHOLTZ3D_DL = 3
+OP_HELMHOLTZ3D_DLT = 4
+OP_HELMHOLTZ3D_HS = 5
 
 _NAMES = {OP_HELMHOLTZ3D_SL: "Helmholtz3D.singlelayer", OP_MAXWELL3D_SL: "Maxwell3D.singlelayer",
-          OP_MAXWELL3D_DL: "Maxwell3D.doublelayer"}
+          OP_MAXWELL3D_DL: "Maxwell3D.doublelayer", OP_HELMHOLTZ3D_DL: "Helmholtz3D.doublelayer",
+          OP_HELMHOLTZ3D_DLT: "Helmholtz3D.doublelayer_transposed",
+          OP_HELMHOLTZ3D_HS: "Helmholtz3D.hypersingular"}
 
 
 @dataclass(frozen=True)
@@ -47,6 +53,24 @@ class Helmholtz3D:
         """alpha * int int G(x, y) f(x) g(y); alpha defaults to 1 (BEAST)."""
         g = _gamma(gamma, wavenumber)
         return Operator(OP_HELMHOLTZ3D_SL, complex(1.0 if alpha is None else alpha), g)
+
+    @staticmethod
+    def doublelayer(*, wavenumber=None, gamma=None, alpha=None) -> Operator:
+        """K: alpha * int int f(x) dG/dn_y(x, y) g(y), dG/dn_y = n_y . grad_y G; alpha defaults to 1."""
+        return Operator(OP_HELMHOLTZ3D_DL, complex(1.0 if alpha is None else alpha), _gamma(gamma, wavenumber))
+
+    @staticmethod
+    def doublelayer_transposed(*, wavenumber=None, gamma=None, alpha=None) -> Operator:
+        """K': alpha * int int f(x) dG/dn_x(x, y) g(y), dG/dn_x = n_x . grad_x G; alpha defaults to 1."""
+        return Operator(OP_HELMHOLTZ3D_DLT, complex(1.0 if alpha is None else alpha), _gamma(gamma, wavenumber))
+
+    @staticmethod
+    def hypersingular(*, wavenumber=None, gamma=None, alpha=None, beta=None) -> Operator:
+        """W in Maue's form: int int G [alpha (n_x . n_y) f g + beta curl f . curl g];
+        alpha defaults to gamma^2 and beta to 1."""
+        g = _gamma(gamma, wavenumber)
+        return Operator(OP_HELMHOLTZ3D_HS, g * g if alpha is None else complex(alpha), g,
+                        1.0 if beta is None else complex(beta))
 
 
 class Maxwell3D:

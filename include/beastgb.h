@@ -46,7 +46,11 @@ typedef enum {
 typedef enum {
   BGB_OP_HELMHOLTZ3D_SL = 0, /* alpha int int G f g */
   BGB_OP_MAXWELL3D_SL = 1,   /* int int G [alpha f.g + beta div f div g] */
-  BGB_OP_MAXWELL3D_DL = 2    /* alpha int int f(x) . (grad_x G(x,y) x g(y)) */
+  BGB_OP_MAXWELL3D_DL = 2,   /* alpha int int f(x) . (grad_x G(x,y) x g(y)) */
+  BGB_OP_HELMHOLTZ3D_DL = 3,  /* alpha int int f(x) dG/dn_y g(y), dG/dn_y = n_y . grad_y G (Lagrange) */
+  BGB_OP_HELMHOLTZ3D_DLT = 4, /* alpha int int f(x) dG/dn_x g(y), the transposed double layer (Lagrange) */
+  BGB_OP_HELMHOLTZ3D_HS = 5   /* int int G [alpha (n_x.n_y) f g + beta curl f . curl g] (hypersingular,
+                                 Maue's form; BEAST: alpha = gamma^2, beta = 1) */
 } bgb_op_kind;
 
 /* Local shape-function families (BEAST reference spaces). */

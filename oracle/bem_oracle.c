@@ -171,6 +171,8 @@ typedef struct {
   double val[3];   /* Lagrange: barycentric hats (Integrand_gpu.jl:51-55) */
   double vec[3][3];/* RT: vector values (x - v_i) / (2A) (BEAST RTRefSpace) */
   double div;      /* RT divergence 1 / A */
+  double n[3];     /* unit normal (t1 x t2) / (2A) */
+  double curl[3][3]; /* Lagrange: surface curl n x grad(val_i) = (v_{i+1} - v_{i+2}) / (2A) */
 } shp_t;
 
 static void eval_shapes(const tri_t* T, int32_t refspace, double u, double v, shp_t* S) {
@@ -178,6 +180,14 @@ static void eval_shapes(const tri_t* T, int32_t refspace, double u, double v, sh
   S->val[0] = u;
   S->val[1] = v;
   S->val[2] = 1.0 - u - v;
+  {
+    const double inv_j = 1.0 / (T->area * 2.0);
+    S->n[0] = (T->t[0][1] * T->t[1][2] - T->t[0][2] * T->t[1][1]) * inv_j;
+    S->n[1] = (T->t[0][2] * T->t[1][0] - T->t[0][0] * T->t[1][2]) * inv_j;
+    S->n[2] = (T->t[0][0] * T->t[1][1] - T->t[0][1] * T->t[1][0]) * inv_j;
+    for (int i = 0; i < 3; ++i)
+      for (int c = 0; c < 3; ++c) S->curl[i][c] = (T->v[(i + 1) % 3][c] - T->v[(i + 2) % 3][c]) * inv_j;
+  }
   if (refspace == ORC_REFSPACE_RT) {
     double j = T->area * 2.0;
     double inv_j = 1.0 / j;
@@ -210,6 +220,32 @@ static void accumulate_far(const orc_operator* op, const shp_t* X, const shp_t* 
     return;
   }
   cpx G = cmul(mk(wx * wy * inv4pi() / R, 0.0), expmg(R, op->gamma));
+  if (op->kind == ORC_OP_HELMHOLTZ3D_DL || op->kind == ORC_OP_HELMHOLTZ3D_DLT) {
+    /* dG/dn_y = (gamma + 1/R) G ((x - y) . n_y) / R;  dG/dn_x = -(gamma + 1/R) G ((x - y) . n_x) / R
+     * (BEAST's HH3DDoubleLayerFDBIO / HH3DDoubleLayerTransposedFDBIO, written from the kernel) */
+    const double* nv = op->kind == ORC_OP_HELMHOLTZ3D_DL ? Y->n : X->n;
+    double rn = (d0 * nv[0] + d1 * nv[1]) + d2 * nv[2];
+    if (op->kind == ORC_OP_HELMHOLTZ3D_DLT) rn = -rn;
+    cpx H = cmul(mk(op->gamma[0] + 1.0 / R, op->gamma[1]), cmulr(G, rn / R));
+    H = cmul(alpha, H);
+    for (int i = 0; i < 3; ++i) {
+      cpx t = cmulr(H, X->val[i]);
+      for (int j = 0; j < 3; ++j) L[i][j] = cadd(L[i][j], cmulr(t, Y->val[j]));
+    }
+    return;
+  }
+  if (op->kind == ORC_OP_HELMHOLTZ3D_HS) {
+    /* Maue's form of the hypersingular operator (BEAST's HH3DHyperSingularFDBIO):
+     * alpha (n_x . n_y) f g G + beta (curl f . curl g) G */
+    const double nn = (X->n[0] * Y->n[0] + X->n[1] * Y->n[1]) + X->n[2] * Y->n[2];
+    cpx a = cmulr(cmul(alpha, G), nn), b = cmul(mk(op->beta[0], op->beta[1]), G);
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        const double cc = (X->curl[i][0] * Y->curl[j][0] + X->curl[i][1] * Y->curl[j][1]) + X->curl[i][2] * Y->curl[j][2];
+        L[i][j] = cadd(L[i][j], cadd(cmulr(a, X->val[i] * Y->val[j]), cmulr(b, cc)));
+      }
+    return;
+  }
   if (op->kind == ORC_OP_MAXWELL3D_SL) {
     cpx beta = mk(op->beta[0], op->beta[1]);
     cpx a = cmul(alpha, G), b = cmul(beta, G);
@@ -384,7 +420,9 @@ static void ss_point(const ss_ctx* c, double u1, double u2, double v1, double v2
  * xi) with the region maps of SauterSchwab.jl:265-297 (CV 2 regions, CE 5, CF 6). */
 static int sauter_schwab(const orc_operator* op, int cls, const tri_t* A, int32_t rsA, const tri_t* B,
                          int32_t rsB, int n, cpx L[3][3]) {
-  if (op->kind == ORC_OP_MAXWELL3D_DL && cls == ORC_CLASS_CF) return 0; /* exactly zero on a flat face */
+  if ((op->kind == ORC_OP_MAXWELL3D_DL || op->kind == ORC_OP_HELMHOLTZ3D_DL || op->kind == ORC_OP_HELMHOLTZ3D_DLT) &&
+      cls == ORC_CLASS_CF)
+    return 0; /* exactly zero on a flat face */
   double q[64], w[64];
   if (orc_gauss_legendre01(n, q, w)) return -1;
   int I[3], J[3];
@@ -448,7 +486,8 @@ static double op_k2(const orc_operator* op) {
 
 static int valid_op_space(const orc_operator* op, const orc_space* a, const orc_space* b) {
   if (!op || !a || !b) return 0;
-  if (op->kind == ORC_OP_HELMHOLTZ3D_SL)
+  if (op->kind == ORC_OP_HELMHOLTZ3D_SL || op->kind == ORC_OP_HELMHOLTZ3D_DL || op->kind == ORC_OP_HELMHOLTZ3D_DLT ||
+      op->kind == ORC_OP_HELMHOLTZ3D_HS)
     return a->refspace == ORC_REFSPACE_LAGRANGE_C0D1 && b->refspace == ORC_REFSPACE_LAGRANGE_C0D1;
   if (op->kind == ORC_OP_MAXWELL3D_SL || op->kind == ORC_OP_MAXWELL3D_DL)
     return a->refspace == ORC_REFSPACE_RT && b->refspace == ORC_REFSPACE_RT;

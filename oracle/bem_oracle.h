@@ -27,7 +27,14 @@
 extern "C" {
 #endif
 
-enum { ORC_OP_HELMHOLTZ3D_SL = 0, ORC_OP_MAXWELL3D_SL = 1, ORC_OP_MAXWELL3D_DL = 2 };
+enum {
+  ORC_OP_HELMHOLTZ3D_SL = 0,
+  ORC_OP_MAXWELL3D_SL = 1,
+  ORC_OP_MAXWELL3D_DL = 2,
+  ORC_OP_HELMHOLTZ3D_DL = 3,  /* alpha int int f(x) dG/dn_y g(y) */
+  ORC_OP_HELMHOLTZ3D_DLT = 4, /* alpha int int f(x) dG/dn_x g(y) */
+  ORC_OP_HELMHOLTZ3D_HS = 5   /* int int G [alpha (n_x.n_y) f g + beta curl f . curl g] */
+};
 enum { ORC_REFSPACE_LAGRANGE_C0D1 = 0, ORC_REFSPACE_RT = 1 };
 enum { ORC_CLASS_FAR = 0, ORC_CLASS_CV = 1, ORC_CLASS_CE = 2, ORC_CLASS_CF = 3, ORC_CLASS_NEAR = 4 };
 

@@ -6,6 +6,8 @@ For a test triangle tau and trial triangle sigma the local matrices are
   HH   L_ij = 1/(4 pi) int_tau int_sigma lambda_i(x) lambda_j(y) / |x - y|        (Lagrange hats)
   MWa  L_ij = 1/(4 pi) int_tau int_sigma psi_i(x) . psi_j(y) / |x - y|            (RWG vector part)
   MWb  L_ij = 1/(4 pi) int_tau int_sigma div psi_i div psi_j / |x - y|           (RWG divergence part)
+  DL   L_ij = 1/(4 pi) int_tau int_sigma lambda_i(x) lambda_j(y) (x - y).n_sigma / |x - y|^3
+  DLT  L_ij = DL of the swapped pair, transposed (the kernel of the transposed double layer)
 
 with lambda_i the barycentric coordinate of chart vertex i, psi_i(x) = (x - v_i) / (2 A) and
 div psi_i = 1 / A (BEAST's RT reference shapes).  The inner integrals over sigma are the closed
@@ -16,7 +18,8 @@ IEEE TAP 32(3), 1984; Graglia, IEEE TAP 41(10), 1993):
                                                                    - atan(P0 l- / (R0^2 + |d| R-))) ]
   int_T (y - rho)/R = 1/2 sum_edges u_hat [ R0^2 ln((R+ + l+)/(R- + l-)) + l+ R+ - l- R- ]
 
-and the outer integral over tau is a tensor Gauss-Legendre rule in collapsed coordinates on the
+with the double-layer potential from the signed solid angle (Van Oosterom & Strackee 1983) and the
+surface gradient theorem, and the outer integral over tau is a tensor Gauss-Legendre rule in collapsed coordinates on the
 three centroid subtriangles of tau, graded toward tau's edges and vertices (where the outer
 integrand loses smoothness).  Checked against the closed-form self term of a triangle
 (Eibert & Hansen, IEEE TAP 43(12), 1995) to 1e-14.
@@ -65,6 +68,53 @@ def tri_potentials(V, r):
         P1 += 0.5 * uhat[None, :] * (R02 * lg + lp * Rp - lm * Rm)[:, None]
     P1 += (rho - r) * P0[:, None]
     return P0, P1
+
+
+def dl_potentials(V, r):
+    """W0 = int_T d / |r - y|^3 dy (the signed solid angle, d = (r - y) . n) and
+    W1 = int_T (y - rho) / |r - y|^3 dy = -sum_edges u_hat ln((R+ + l+)/(R- + l-)) (surface
+    gradient theorem), for the double-layer potential of a flat triangle."""
+    v1, v2, v3 = V
+    n = np.cross(v2 - v1, v3 - v1)
+    n /= np.linalg.norm(n)
+    d = (r - v1) @ n
+    rho = r - d[:, None] * n[None, :]
+    q = V[None, :, :] - r[:, None, :]
+    nq = np.linalg.norm(q, axis=2)
+    trip = np.einsum("ij,ij->i", q[:, 0], np.cross(q[:, 1], q[:, 2]))
+    den = (nq[:, 0] * nq[:, 1] * nq[:, 2] + np.einsum("ij,ij->i", q[:, 0], q[:, 1]) * nq[:, 2] +
+           np.einsum("ij,ij->i", q[:, 0], q[:, 2]) * nq[:, 1] + np.einsum("ij,ij->i", q[:, 1], q[:, 2]) * nq[:, 0])
+    W0 = -2 * np.arctan2(trip, den)  # Van Oosterom & Strackee, IEEE TBME 30(2), 1983
+    W1 = np.zeros((len(r), 3))
+    for a, b in ((v1, v2), (v2, v3), (v3, v1)):
+        lhat = (b - a) / np.linalg.norm(b - a)
+        uhat = np.cross(lhat, n)
+        lm, lp = (a - rho) @ lhat, (b - rho) @ lhat
+        P = (a - rho) @ uhat
+        Rm, Rp = np.linalg.norm(r - a, axis=1), np.linalg.norm(r - b, axis=1)
+        R02 = P * P + d * d
+        with np.errstate(divide="ignore", invalid="ignore"):
+            num = np.where(lp >= 0, Rp + lp, R02 / (Rp - lp))
+            den2 = np.where(lm >= 0, Rm + lm, R02 / (Rm - lm))
+            lg = np.log(num / den2)
+        lg = np.where(R02 <= 0, 0.0, lg)
+        W1 -= uhat[None, :] * lg[:, None]
+    return W0, W1, d
+
+
+def local_static_dl(Vt, Vs, n=40, p=3):
+    """DL_ij = 1/(4 pi) int_tau lambda_i(x) int_sigma lambda_j(y) (x - y) . n_sigma / |x - y|^3."""
+    x, w = graded_rule(Vt, n, p)
+    W0, W1, d = dl_potentials(Vs, x)
+    lam_t = barycentric(Vt, x)
+    lam_s = barycentric(Vs, x)
+    gs = grad_barycentric(Vs)
+    dl = np.zeros((3, 3))
+    for i in range(3):
+        for j in range(3):
+            inner = lam_s[:, j] * W0 + d * (W1 @ gs[j])
+            dl[i, j] = np.sum(w * lam_t[:, i] * inner) / (4 * np.pi)
+    return dl
 
 
 def graded_rule(V, n=40, p=3):
@@ -149,13 +199,21 @@ def pick_pairs(tris):
 
 
 def tables(V, T, pairs):
-    hh, mwa, mwb, err = [], [], [], []
+    hh, mwa, mwb, dl, dlt, err = [], [], [], [], [], []
     for a, b in pairs:
-        r40 = local_static(V[T[a]], V[T[b]], 40)
-        r60 = local_static(V[T[a]], V[T[b]], 60)
+        A, B = V[T[a]], V[T[b]]
+        r40 = local_static(A, B, 40)
+        r60 = local_static(A, B, 60)
         hh.append(r60[0]), mwa.append(r60[1]), mwb.append(r60[2])
         err.append(max(np.abs(x - y).max() / np.abs(y).max() for x, y in zip(r40, r60)))
-    return np.array(hh), np.array(mwa), np.array(mwb), np.array(err)
+        if a == b:  # the double layers vanish on a flat common face
+            dl.append(np.zeros((3, 3))), dlt.append(np.zeros((3, 3)))
+            continue
+        d40, d60 = local_static_dl(A, B, 40), local_static_dl(A, B, 60)
+        t60 = local_static_dl(B, A, 60).T  # transposed double layer: DL with the roles swapped
+        dl.append(d60), dlt.append(t60)
+        err.append(np.abs(d40 - d60).max() / max(np.abs(d60).max(), 1e-300))
+    return np.array(hh), np.array(mwa), np.array(mwb), np.array(dl), np.array(dlt), np.array(err)
 
 
 def main():
@@ -166,12 +224,12 @@ def main():
     assert len(pairs) == 15, len(pairs)
     # far pairs: the three closest non-touching pairs and the farthest one
     pairs += [(67, 69), (40, 55), (3, 12), (19, 59)]
-    hh, mwa, mwb, err = tables(V, T, pairs)
+    hh, mwa, mwb, dl, dlt, err = tables(V, T, pairs)
     # near pairs (class 4 at k = 0) of two jittered coplanar 4 x 4 plates 0.01 apart
     p = bg.two_plates(4, jitter=0.3, seed=1, gap=0.01)
     PV, PT = p.vertices.astype(np.float64), p.triangles.astype(np.int32)
     near = [(24, 32), (25, 34), (26, 37), (24, 35)]
-    nhh, nmwa, nmwb, nerr = tables(PV, PT, near)
+    nhh, nmwa, nmwb, ndl, ndlt, nerr = tables(PV, PT, near)
     # the CF self term of the outer rule against its closed form
     Vt = V[T[0]]
     x, w = graded_rule(Vt, 60)
@@ -179,10 +237,10 @@ def main():
     self_err = abs(np.sum(w * P0) - closed_form_self(Vt)) / closed_form_self(Vt)
     out = os.path.join(HERE, "static_singular.npz")
     np.savez(out, vertices=V, triangles=T, tau=np.array([q[0] for q in pairs], dtype=np.int32),
-             sigma=np.array([q[1] for q in pairs], dtype=np.int32), hh=hh, mw_alpha=mwa, mw_beta=mwb,
+             sigma=np.array([q[1] for q in pairs], dtype=np.int32), hh=hh, mw_alpha=mwa, mw_beta=mwb, dl=dl, dlt=dlt,
              plate_vertices=PV, plate_triangles=PT, near_tau=np.array([q[0] for q in near], dtype=np.int32),
              near_sigma=np.array([q[1] for q in near], dtype=np.int32), near_hh=nhh, near_mw_alpha=nmwa,
-             near_mw_beta=nmwb, rule_change=np.concatenate([err, nerr]), self_term_error=np.array(self_err))
+             near_mw_beta=nmwb, near_dl=ndl, near_dlt=ndlt, rule_change=np.concatenate([err, nerr]), self_term_error=np.array(self_err))
     print(f"wrote {out}: {len(pairs)} + {len(near)} pairs, max change 40 -> 60 points per dimension "
           f"{max(err.max(), nerr.max()):.2e}, self-term error {self_err:.2e}")
 
