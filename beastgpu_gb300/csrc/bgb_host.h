@@ -89,6 +89,8 @@ extern const int kPrefMixed[];
 extern const int kNumPrefMixed;
 extern const int kPrefFp64[];
 extern const int kNumPrefFp64;
+extern const int kPrefLagrange[];
+extern const int kNumPrefLagrange;
 
 int validate_space(const bgb_space* s, const char* name);
 int make_quadsel(const bgb_quadstrat* qs, QuadSel* out);
