@@ -45,9 +45,9 @@ UNIT = "pair-interactions/s"
 LEVEL, KWAVE = 5, 2 * np.pi * 4
 ERR_ROWS, ERR_SEED = 1000, 0
 # DRAM bytes (read + write) of one far-kernel launch per triangle pair, from the ncu capture of
-# the level-4 case (0.443 GB for 5120^2 pairs, profiles/kernels_efie_icosphere_l4.md); the
+# the level-4 case (0.440 GB for 5120^2 pairs, profiles/kernels_efie_icosphere_l4.md); the
 # traffic is the output written once, so it scales with the pairs.
-FAR_DRAM_BYTES_PER_PAIR = 0.443e9 / (5120 * 5120)
+FAR_DRAM_BYTES_PER_PAIR = 0.440e9 / (5120 * 5120)
 
 
 def workload():
