@@ -405,14 +405,17 @@ static int classify_all(bgb_handle* h, const bgb_space* test, const bgb_space* t
   const int nt = test->nt, nb = trial->nt;
   if ((rc = h->bnd_t.ensure(sizeof(float4) * std::max(1, nt)))) return rc;
   if ((rc = h->bnd_b.ensure(sizeof(float4) * std::max(1, nb)))) return rc;
+  if ((rc = h->bnd_c.ensure(sizeof(float4) * std::max(1, (nb + 31) / 32)))) return rc;
   if ((rc = h->cls_count.ensure(sizeof(int) * (size_t)(nt + 1)))) return rc;
   if ((rc = h->cls_off.ensure(sizeof(int64_t) * (size_t)(nt + 1)))) return rc;
   if ((rc = h->err.ensure(sizeof(int) * 4))) return rc;
   BGB_CUDA(cudaMemsetAsync(h->err.p, 0, sizeof(int) * 4, h->stream));
   launch_prepare_bounds(gt, nt, k2, 0, h->bnd_t.as<float4>(), h->stream);
   launch_prepare_bounds(gb, nb, k2, 1, h->bnd_b.as<float4>(), h->stream);
+  launch_chunk_bounds(h->bnd_b.as<float4>(), nb, h->bnd_c.as<float4>(), h->stream);
   launch_classify(false, h->bnd_t.as<float4>(), h->bnd_b.as<float4>(), gt, gb, nt, nb, k2, h->cls_count.as<int>(),
-                  nullptr, nullptr, nullptr, nullptr, h->err.as<int>(), h->num_sms, h->stream);
+                  nullptr, nullptr, nullptr, nullptr, h->err.as<int>(), h->num_sms, h->stream, nullptr,
+                  h->bnd_c.as<float4>());
   launch_scan(h->cls_count.as<int>(), nt, h->cls_off.as<int64_t>(), h->stream);
   int64_t tot = 0;
   int herr = 0;
@@ -429,7 +432,7 @@ static int classify_all(bgb_handle* h, const bgb_space* test, const bgb_space* t
   if ((rc = h->ent_mask.ensure(sizeof(int16_t) * (size_t)std::max<int64_t>(1, tot)))) return rc;
   launch_classify(true, h->bnd_t.as<float4>(), h->bnd_b.as<float4>(), gt, gb, nt, nb, k2, h->cls_count.as<int>(),
                   h->cls_off.as<int64_t>(), h->ent_tau.as<int>(), h->ent_sigma.as<int>(), h->ent_cls.as<int8_t>(),
-                  h->err.as<int>(), h->num_sms, h->stream, h->ent_mask.as<int16_t>());
+                  h->err.as<int>(), h->num_sms, h->stream, h->ent_mask.as<int16_t>(), h->bnd_c.as<float4>());
   BGB_CUDA(cudaGetLastError());
   *total = tot;
   return 0;
@@ -503,7 +506,7 @@ int bgb_destroy(bgb_handle* h) {
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
-  DevBuf* bufs[] = {&h->verts_t, &h->tris_t, &h->verts_b, &h->tris_b, &h->geo_t, &h->geo_b, &h->bnd_t, &h->bnd_b,
+  DevBuf* bufs[] = {&h->verts_t, &h->tris_t, &h->verts_b, &h->tris_b, &h->geo_t, &h->geo_b, &h->bnd_t, &h->bnd_b, &h->bnd_c,
                     &h->rec_t, &h->rec_b, &h->cls_count, &h->cls_off, &h->ent_tau, &h->ent_sigma, &h->ent_cls, &h->ent_mask, &h->geodf_t, &h->geodf_b,
                     &h->sing_L, &h->err, &h->plan_i[0], &h->plan_l[0], &h->plan_d[0], &h->plan_f[0], &h->far_items[0], &h->far_const[0], &h->plan_i[1], &h->plan_l[1], &h->plan_d[1], &h->plan_f[1], &h->far_items[1], &h->far_const[1], &h->df_tab, &h->stage[0], &h->stage[1], &h->tplan_i, &h->tplan_l, &h->tplan_d, &h->tplan_f,
                     &h->diag_a, &h->diag_b, &h->diag_c, &h->diag_d};

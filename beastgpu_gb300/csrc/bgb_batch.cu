@@ -22,7 +22,7 @@ struct bgb_batch {
   size_t smem = 0;
   bool host_out = false, c64 = false;
   // device buffers
-  bgb::DevBuf verts_t, tris_t, verts_b, tris_b, geo_t, geo_b, bnd_t, bnd_b, rec_t, rec_b;
+  bgb::DevBuf verts_t, tris_t, verts_b, tris_b, geo_t, geo_b, bnd_t, bnd_b, bnd_c, rec_t, rec_b;
   bgb::DevBuf tri_problem, prob_trial, prob_k2, ops, Ks, plans, items, counter;
   bgb::DevBuf cls_count, cls_off, ent_tau, ent_sigma, ent_cls, ent_mask, sing_L, err, geodf_t, geodf_b, opdf;
   bgb::DevBuf plan_i, plan_l, plan_d, plan_f, stage, df_tab;
@@ -45,7 +45,7 @@ struct bgb_batch {
     if (graph) cudaGraphDestroy(graph);
     for (auto e : ev)
       if (e) cudaEventDestroy(e);
-    bgb::DevBuf* bufs[] = {&verts_t, &verts_b, &tris_t, &tris_b, &geo_t, &geo_b, &bnd_t, &bnd_b, &rec_t, &rec_b,
+    bgb::DevBuf* bufs[] = {&verts_t, &verts_b, &tris_t, &tris_b, &geo_t, &geo_b, &bnd_t, &bnd_b, &bnd_c, &rec_t, &rec_b,
                            &tri_problem, &prob_trial, &prob_k2, &ops, &Ks, &plans, &items, &counter, &cls_count,
                            &cls_off, &ent_tau, &ent_sigma, &ent_cls, &ent_mask, &sing_L, &err, &geodf_t, &geodf_b, &opdf, &plan_i, &plan_l, &plan_d,
                            &plan_f, &stage, &df_tab};
@@ -86,14 +86,16 @@ int enqueue_device_work(bgb_batch* B, cudaStream_t st, bool far_only) {
     const int* tp_b = B->tri_problem.as<int>() + B->nt_t;
     launch_prepare_bounds_batched(gt, B->nt_t, tp_t, B->prob_k2.as<double>(), 0, B->bnd_t.as<float4>(), st);
     launch_prepare_bounds_batched(gb, B->nt_b, tp_b, B->prob_k2.as<double>(), 1, B->bnd_b.as<float4>(), st);
+    launch_chunk_bounds(B->bnd_b.as<float4>(), B->nt_b, B->bnd_c.as<float4>(), st);
     launch_classify_batched(false, B->bnd_t.as<float4>(), B->bnd_b.as<float4>(), gt, gb, B->nt_t, tp_t,
                             B->prob_trial.as<int2>(), B->prob_k2.as<double>(), B->cls_count.as<int>(), nullptr,
-                            nullptr, nullptr, nullptr, B->err.as<int>(), h->num_sms, st);
+                            nullptr, nullptr, nullptr, B->err.as<int>(), h->num_sms, st, nullptr, B->bnd_c.as<float4>());
     launch_scan(B->cls_count.as<int>(), B->nt_t, B->cls_off.as<int64_t>(), st);
     launch_classify_batched(true, B->bnd_t.as<float4>(), B->bnd_b.as<float4>(), gt, gb, B->nt_t, tp_t,
                             B->prob_trial.as<int2>(), B->prob_k2.as<double>(), B->cls_count.as<int>(),
                             B->cls_off.as<int64_t>(), B->ent_tau.as<int>(), B->ent_sigma.as<int>(),
-                            B->ent_cls.as<int8_t>(), B->err.as<int>(), h->num_sms, st, B->ent_mask.as<int16_t>());
+                            B->ent_cls.as<int8_t>(), B->err.as<int>(), h->num_sms, st, B->ent_mask.as<int16_t>(),
+                            B->bnd_c.as<float4>());
     if (B->use_df) {
       launch_prepare_geodf(gt, B->nt_t, B->geodf_t.as<GeoDf>(), st);
       if (!B->shared_trial) launch_prepare_geodf(gb, B->nt_b, B->geodf_b.as<GeoDf>(), st);
@@ -355,6 +357,7 @@ int bgb_batch_create(bgb_handle* h, int32_t n, const bgb_problem* problems, int3
   if ((rc = B->geo_t.ensure(sizeof(Geo64) * std::max(1, B->nt_t))) ||
       (!B->shared_trial && (rc = B->geo_b.ensure(sizeof(Geo64) * std::max(1, B->nt_b)))) ||
       (rc = B->bnd_t.ensure(sizeof(float4) * std::max(1, B->nt_t))) || (rc = B->bnd_b.ensure(sizeof(float4) * std::max(1, B->nt_b))) ||
+      (rc = B->bnd_c.ensure(sizeof(float4) * std::max(1, (B->nt_b + 31) / 32))) ||
       (rc = B->cls_count.ensure(sizeof(int) * (B->nt_t + 1))) || (rc = B->cls_off.ensure(sizeof(int64_t) * (B->nt_t + 1))) ||
       (rc = B->err.ensure(sizeof(int) * 4)) || (rc = B->counter.ensure(sizeof(int) * 4)) ||
       (rc = B->rec_t.ensure(rsz * rec_stride(precision, qt, B->generic) * std::max(1, B->nt_t))) ||
@@ -373,9 +376,10 @@ int bgb_batch_create(bgb_handle* h, int32_t n, const bgb_problem* problems, int3
   launch_prepare_bounds_batched(gt, B->nt_t, B->tri_problem.as<int>(), B->prob_k2.as<double>(), 0, B->bnd_t.as<float4>(), st);
   launch_prepare_bounds_batched(gb, B->nt_b, B->tri_problem.as<int>() + B->nt_t, B->prob_k2.as<double>(), 1,
                                 B->bnd_b.as<float4>(), st);
+  launch_chunk_bounds(B->bnd_b.as<float4>(), B->nt_b, B->bnd_c.as<float4>(), st);
   launch_classify_batched(false, B->bnd_t.as<float4>(), B->bnd_b.as<float4>(), gt, gb, B->nt_t, B->tri_problem.as<int>(),
                           B->prob_trial.as<int2>(), B->prob_k2.as<double>(), B->cls_count.as<int>(), nullptr, nullptr,
-                          nullptr, nullptr, B->err.as<int>(), h->num_sms, st);
+                          nullptr, nullptr, B->err.as<int>(), h->num_sms, st, nullptr, B->bnd_c.as<float4>());
   launch_scan(B->cls_count.as<int>(), B->nt_t, B->cls_off.as<int64_t>(), st);
   int herr = 0;
   int64_t tot = 0;

@@ -49,7 +49,7 @@ struct bgb_handle {
   int* abort_dev = nullptr;
   std::mutex mu;
   // buffers
-  bgb::DevBuf verts_t, tris_t, verts_b, tris_b, geo_t, geo_b, bnd_t, bnd_b, rec_t, rec_b;
+  bgb::DevBuf verts_t, tris_t, verts_b, tris_b, geo_t, geo_b, bnd_t, bnd_b, bnd_c, rec_t, rec_b;
   bgb::DevBuf cls_count, cls_off, ent_tau, ent_sigma, ent_cls, ent_mask, sing_L, err, geodf_t, geodf_b;
   bgb::DevBuf plan_i[2], plan_l[2], plan_d[2], plan_f[2], far_items[2], far_const[2], df_tab;
   bgb::DevBuf tplan_i, tplan_l, tplan_d, tplan_f;  // test-side tile tables (shared by all output blocks)

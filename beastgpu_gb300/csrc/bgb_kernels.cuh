@@ -11,9 +11,12 @@ namespace bgb {
 // ---- bgb_singular.cu -------------------------------------------------------------------
 void launch_prepare_geo64(const double* verts, const int32_t* tris, int nt, Geo64* out, cudaStream_t st);
 void launch_prepare_bounds(const Geo64* g, int nt, double k2, int trial_side, float4* out, cudaStream_t st);
+// Bounding spheres of chunks of 32 consecutive trial triangles (out: (nb + 31) / 32 entries).
+void launch_chunk_bounds(const float4* b, int nb, float4* out, cudaStream_t st);
+// cb (optional): the trial chunk spheres; whole chunks are skipped by one test.
 void launch_classify(bool fill, const float4* tb, const float4* bb, const Geo64* tg, const Geo64* bg, int nt, int nb,
                      double k2, int* count, const int64_t* offset, int* out_tau, int* out_sigma, int8_t* out_cls,
-                     int* err, int num_sms, cudaStream_t st, int16_t* out_mask = nullptr);
+                     int* err, int num_sms, cudaStream_t st, int16_t* out_mask = nullptr, const float4* cb = nullptr);
 void launch_scan(const int* counts, int n, int64_t* offsets, cudaStream_t st);
 void launch_classify_dense(const Geo64* tg, const Geo64* bg, int t0, int t1, int s0, int s1, double k2, int8_t* out,
                            int* err, cudaStream_t st);
@@ -29,7 +32,7 @@ void launch_prepare_bounds_batched(const Geo64* g, int nt, const int* tri_proble
 void launch_classify_batched(bool fill, const float4* tb, const float4* bb, const Geo64* tg, const Geo64* bg, int nt,
                              const int* tri_problem, const int2* prob_trial, const double* prob_k2, int* count,
                              const int64_t* offset, int* out_tau, int* out_sigma, int8_t* out_cls, int* err,
-                             int num_sms, cudaStream_t st, int16_t* out_mask = nullptr);
+                             int num_sms, cudaStream_t st, int16_t* out_mask = nullptr, const float4* cb = nullptr);
 void launch_singular_batched(int op_kind, const OpParams* ops, const QuadSel& qs, const RuleTable& rules,
                              const Geo64* tg, const Geo64* bg, const int* tri_problem, const int* et, const int* es,
                              const int8_t* ec, int64_t n, double2* out, const volatile int* abort_flag, int num_sms,

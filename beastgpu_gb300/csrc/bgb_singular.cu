@@ -67,6 +67,32 @@ __global__ void k_prepare_bounds(const Geo64* __restrict__ g, int nt, double k2,
   out[t] = make_float4((float)c[0], (float)c[1], (float)c[2], (float)r);
 }
 
+// One sphere around the spheres of 32 consecutive trial triangles (chunk c = [32 c, 32 c + 32)),
+// inflated so that the FP32 sphere test against it is true whenever it is true for a member:
+// the classifier skips a whole chunk with one test.  Tight when consecutive triangles are
+// spatially close (structured and hierarchical meshes); still correct when they are not.
+__global__ void k_chunk_bounds(const float4* __restrict__ b, int nb, float4* __restrict__ out) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s0 = 32 * c, s1 = min(nb, s0 + 32);
+  if (s0 >= nb) return;
+  double m[3] = {0.0, 0.0, 0.0};
+  for (int s = s0; s < s1; ++s) {
+    m[0] += b[s].x;
+    m[1] += b[s].y;
+    m[2] += b[s].z;
+  }
+  for (int k = 0; k < 3; ++k) m[k] /= (double)(s1 - s0);
+  const float cx = (float)m[0], cy = (float)m[1], cz = (float)m[2];
+  double R = 0.0;
+  for (int s = s0; s < s1; ++s) {
+    const double d0 = (double)b[s].x - cx, d1 = (double)b[s].y - cy, d2 = (double)b[s].z - cz;
+    R = fmax(R, sqrt(d0 * d0 + d1 * d1 + d2 * d2) + (double)b[s].w);
+  }
+  const double cn = sqrt((double)cx * cx + (double)cy * cy + (double)cz * cz);
+  R = R * (1.0 + 1e-5) + 1e-6 * (cn + R) + 1e-30;
+  out[c] = make_float4(cx, cy, cz, __double2float_ru(R));
+}
+
 // ----------------------------------------------------------------------------------------
 // Exact FP64 predicate (doubleQuadRuleMainCase.jl:324-339; codes quadrule_determine.jl:76).
 // Rounded like the Julia code: no contraction, IEEE sqrt and division.  *mask (optional)
@@ -98,42 +124,81 @@ __device__ int classify_exact(const Geo64& a, const Geo64& b, double k2, int* ma
   return (mx >= xtol2) ? BGB_CLASS_FAR : BGB_CLASS_NEAR;
 }
 
+// One warp classifies test triangle tau against trial triangles [s_begin, s_end).  The FP32
+// sphere test sweeps 32 trial triangles per step; its candidates are queued (ascending) in a
+// per-warp shared-memory list, and the exact FP64 predicate runs on 32 queued candidates at a
+// time, one per lane, instead of on whichever lanes happen to hold a candidate (a divergent
+// FP64 warp pays the full warp cost for one lane).  The output order stays trial-ascending.
+template <bool FILL>
+__device__ __forceinline__ void classify_sweep(int tau, float4 a, const Geo64& A, int s_begin, int s_end,
+                                               const float4* __restrict__ bb, const float4* __restrict__ cb,
+                                               const Geo64* __restrict__ bg,
+                                               double k2, int* __restrict__ queue, int* __restrict__ count,
+                                               const int64_t* __restrict__ offset, int* __restrict__ out_tau,
+                                               int* __restrict__ out_sigma, int8_t* __restrict__ out_cls,
+                                               int16_t* __restrict__ out_mask, int* __restrict__ err) {
+  const int lane = threadIdx.x & 31;
+  const int64_t base = FILL ? offset[tau] : 0;
+  int n = 0, queued = 0;
+  auto drain = [&](int k) {  // classify queue[0..k) (k <= 32), one candidate per lane
+    int cls = 0, mask = 0, s = 0;
+    if (lane < k) {
+      s = queue[lane];
+      cls = classify_exact(A, bg[s], k2, &mask);
+      if (cls < 0) {
+        atomicOr(err, 1);
+        cls = 0;
+      }
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, cls != 0);
+    if (FILL && cls != 0) {
+      const int64_t pos = base + n + __popc(bal & ((1u << lane) - 1u));
+      out_tau[pos] = tau;
+      out_sigma[pos] = s;
+      out_cls[pos] = (int8_t)cls;
+      if (out_mask) out_mask[pos] = (int16_t)mask;
+    }
+    n += __popc(bal);
+  };
+  for (int c = s_begin >> 5; 32 * c < s_end; ++c) {
+    if (cb && !sphere_candidate(a, cb[c])) continue;  // no member of the chunk can be near (warp-uniform)
+    const int s = 32 * c + lane;
+    const bool cand = s >= s_begin && s < s_end && sphere_candidate(a, bb[s]);
+    const unsigned bal = __ballot_sync(0xffffffffu, cand);
+    if (cand) queue[queued + __popc(bal & ((1u << lane) - 1u))] = s;  // queued < 32: room for 32 more
+    queued += __popc(bal);
+    __syncwarp();
+    if (queued >= 32) {
+      drain(32);
+      __syncwarp();
+      const int rest = queued - 32;
+      const int moved = lane < rest ? queue[32 + lane] : 0;
+      __syncwarp();
+      if (lane < rest) queue[lane] = moved;
+      __syncwarp();
+      queued = rest;
+    }
+  }
+  if (queued > 0) drain(queued);
+  __syncwarp();
+  if (!FILL && lane == 0) count[tau] = n;
+}
+
 template <bool FILL>
 __global__ void __launch_bounds__(256) k_classify(const float4* __restrict__ tb, const float4* __restrict__ bb,
+                                                  const float4* __restrict__ cb,
                                                   const Geo64* __restrict__ tg, const Geo64* __restrict__ bg,
                                                   int nt, int nb, double k2, int* __restrict__ count,
                                                   const int64_t* __restrict__ offset, int* __restrict__ out_tau,
                                                   int* __restrict__ out_sigma, int8_t* __restrict__ out_cls,
                                                   int16_t* __restrict__ out_mask, int* __restrict__ err) {
-  const int lane = threadIdx.x & 31;
+  __shared__ int queues[8][64];
+  int* queue = queues[threadIdx.x >> 5];
   const int warps = (gridDim.x * blockDim.x) >> 5;
   for (int tau = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; tau < nt; tau += warps) {
-    float4 a = tb[tau];
-    int64_t base = FILL ? offset[tau] : 0;
-    int n = 0;
-    for (int s0 = 0; s0 < nb; s0 += 32) {
-      int s = s0 + lane;
-      int cls = 0, mask = 0;
-      if (s < nb) {
-        if (sphere_candidate(a, bb[s])) {
-          cls = classify_exact(tg[tau], bg[s], k2, &mask);
-          if (cls < 0) {
-            atomicOr(err, 1);
-            cls = 0;
-          }
-        }
-      }
-      unsigned bal = __ballot_sync(0xffffffffu, cls != 0);
-      if (FILL && cls != 0) {
-        int64_t pos = base + n + __popc(bal & ((1u << lane) - 1u));
-        out_tau[pos] = tau;
-        out_sigma[pos] = s;
-        out_cls[pos] = (int8_t)cls;
-        if (out_mask) out_mask[pos] = (int16_t)mask;
-      }
-      n += __popc(bal);
-    }
-    if (!FILL && lane == 0) count[tau] = n;
+    const Geo64 A = tg[tau];
+    classify_sweep<FILL>(tau, tb[tau], A, 0, nb, bb, cb, bg, k2, queue, count, offset, out_tau, out_sigma, out_cls,
+                         out_mask, err);
   }
 }
 
@@ -556,6 +621,7 @@ __global__ void k_prepare_bounds_batched(const Geo64* __restrict__ g, int nt, co
 
 template <bool FILL>
 __global__ void __launch_bounds__(256) k_classify_batched(const float4* __restrict__ tb, const float4* __restrict__ bb,
+                                                          const float4* __restrict__ cb,
                                                           const Geo64* __restrict__ tg, const Geo64* __restrict__ bg,
                                                           int nt, const int* __restrict__ tri_problem,
                                                           const int2* __restrict__ prob_trial,
@@ -563,36 +629,15 @@ __global__ void __launch_bounds__(256) k_classify_batched(const float4* __restri
                                                           const int64_t* __restrict__ offset, int* __restrict__ out_tau,
                                                           int* __restrict__ out_sigma, int8_t* __restrict__ out_cls,
                                                           int16_t* __restrict__ out_mask, int* __restrict__ err) {
-  const int lane = threadIdx.x & 31;
+  __shared__ int queues[8][64];
+  int* queue = queues[threadIdx.x >> 5];
   const int warps = (gridDim.x * blockDim.x) >> 5;
   for (int tau = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; tau < nt; tau += warps) {
-    const float4 a = tb[tau];
     const int pr = tri_problem[tau];
     const int2 rg = prob_trial[pr];
-    const double k2 = prob_k2[pr];
-    int64_t base = FILL ? offset[tau] : 0;
-    int n = 0;
-    for (int s0 = rg.x; s0 < rg.y; s0 += 32) {
-      const int s = s0 + lane;
-      int cls = 0, mask = 0;
-      if (s < rg.y && sphere_candidate(a, bb[s])) {
-        cls = classify_exact(tg[tau], bg[s], k2, &mask);
-        if (cls < 0) {
-          atomicOr(err, 1);
-          cls = 0;
-        }
-      }
-      const unsigned bal = __ballot_sync(0xffffffffu, cls != 0);
-      if (FILL && cls != 0) {
-        const int64_t pos = base + n + __popc(bal & ((1u << lane) - 1u));
-        out_tau[pos] = tau;
-        out_sigma[pos] = s;
-        out_cls[pos] = (int8_t)cls;
-        if (out_mask) out_mask[pos] = (int16_t)mask;
-      }
-      n += __popc(bal);
-    }
-    if (!FILL && lane == 0) count[tau] = n;
+    const Geo64 A = tg[tau];
+    classify_sweep<FILL>(tau, tb[tau], A, rg.x, rg.y, bb, cb, bg, prob_k2[pr], queue, count, offset, out_tau,
+                         out_sigma, out_cls, out_mask, err);
   }
 }
 
@@ -634,18 +679,22 @@ void launch_prepare_geo64(const double* verts, const int32_t* tris, int nt, Geo6
 void launch_prepare_bounds(const Geo64* g, int nt, double k2, int trial_side, float4* out, cudaStream_t st) {
   if (nt > 0) k_prepare_bounds<<<(nt + 255) / 256, 256, 0, st>>>(g, nt, k2, trial_side, out);
 }
+void launch_chunk_bounds(const float4* b, int nb, float4* out, cudaStream_t st) {
+  const int nc = (nb + 31) / 32;
+  if (nc > 0) k_chunk_bounds<<<(nc + 127) / 128, 128, 0, st>>>(b, nb, out);
+}
 void launch_classify(bool fill, const float4* tb, const float4* bb, const Geo64* tg, const Geo64* bg, int nt, int nb,
                      double k2, int* count, const int64_t* offset, int* out_tau, int* out_sigma, int8_t* out_cls,
-                     int* err, int num_sms, cudaStream_t st, int16_t* out_mask) {
+                     int* err, int num_sms, cudaStream_t st, int16_t* out_mask, const float4* cb) {
   if (nt <= 0) return;
   int blocks = (nt + 7) / 8;
   blocks = blocks < num_sms * 16 ? blocks : num_sms * 16;
   if (fill)
-    k_classify<true><<<blocks, 256, 0, st>>>(tb, bb, tg, bg, nt, nb, k2, count, offset, out_tau, out_sigma, out_cls,
-                                              out_mask, err);
+    k_classify<true><<<blocks, 256, 0, st>>>(tb, bb, cb, tg, bg, nt, nb, k2, count, offset, out_tau, out_sigma,
+                                              out_cls, out_mask, err);
   else
-    k_classify<false><<<blocks, 256, 0, st>>>(tb, bb, tg, bg, nt, nb, k2, count, offset, out_tau, out_sigma, out_cls,
-                                               nullptr, err);
+    k_classify<false><<<blocks, 256, 0, st>>>(tb, bb, cb, tg, bg, nt, nb, k2, count, offset, out_tau, out_sigma,
+                                               out_cls, nullptr, err);
 }
 void launch_scan(const int* counts, int n, int64_t* offsets, cudaStream_t st) {
   k_scan_counts<<<1, 1024, 0, st>>>(counts, n, offsets);
@@ -700,15 +749,15 @@ void launch_prepare_bounds_batched(const Geo64* g, int nt, const int* tri_proble
 void launch_classify_batched(bool fill, const float4* tb, const float4* bb, const Geo64* tg, const Geo64* bg, int nt,
                              const int* tri_problem, const int2* prob_trial, const double* prob_k2, int* count,
                              const int64_t* offset, int* out_tau, int* out_sigma, int8_t* out_cls, int* err,
-                             int num_sms, cudaStream_t st, int16_t* out_mask) {
+                             int num_sms, cudaStream_t st, int16_t* out_mask, const float4* cb) {
   if (nt <= 0) return;
   int blocks = (nt + 7) / 8;
   blocks = blocks < num_sms * 16 ? blocks : num_sms * 16;
   if (fill)
-    k_classify_batched<true><<<blocks, 256, 0, st>>>(tb, bb, tg, bg, nt, tri_problem, prob_trial, prob_k2, count, offset,
+    k_classify_batched<true><<<blocks, 256, 0, st>>>(tb, bb, cb, tg, bg, nt, tri_problem, prob_trial, prob_k2, count, offset,
                                                      out_tau, out_sigma, out_cls, out_mask, err);
   else
-    k_classify_batched<false><<<blocks, 256, 0, st>>>(tb, bb, tg, bg, nt, tri_problem, prob_trial, prob_k2, count,
+    k_classify_batched<false><<<blocks, 256, 0, st>>>(tb, bb, cb, tg, bg, nt, tri_problem, prob_trial, prob_k2, count,
                                                       offset, out_tau, out_sigma, out_cls, nullptr, err);
 }
 void launch_singular_batched(int op_kind, const OpParams* ops, const QuadSel& qs, const RuleTable& rules,
