@@ -59,6 +59,23 @@ def test_classification_bit_exact_plates_with_near_pairs(plates):
     assert (got == 4).sum() > 0, "the jittered plates should produce near pairs"
 
 
+@pytest.mark.parametrize("n", [7, 13])
+def test_classification_and_assembly_ragged_sizes(n):
+    """Triangle counts that are not multiples of the 32-triangle chunks of the classifier
+    (98 and 338 triangles), shuffled triangle order (loose chunk spheres): classes bit-exact, the
+    assembled matrix equal to the oracle's."""
+    p = bg.plate(n, jitter=0.3, seed=3)
+    perm = np.random.default_rng(n).permutation(p.nt)
+    m = bg.Mesh(p.vertices, p.triangles[perm])
+    X = bg.raviartthomas(m)
+    k = 6 * np.pi
+    np.testing.assert_array_equal(bg.classify(X, X, k * k), oracle.classify_block(X, X, k * k))
+    op = bg.Maxwell3D.singlelayer(wavenumber=k)
+    ref = oracle.assemble(op, X, X, bg.QuadStrat())
+    assert rel(bg.assemble_gpu(op, X, X, bg.GPUConfiguration(precision="fp64")), ref) < FP64_TOL
+    assert rel(bg.assemble_gpu(op, X, X, bg.GPUConfiguration(precision="mixed")).astype(np.complex128), ref) < MIXED_TOL
+
+
 @pytest.mark.parametrize("name", list(OPS))
 @pytest.mark.parametrize("cls", [0, 1, 2, 3])
 def test_local_matrices_per_class(c1, qs, name, cls):
@@ -264,3 +281,39 @@ def test_batch_bit_identical_to_single_assemblies(qs):
     outs = bg.assemble_batch(probs[:2], bg.GPUConfiguration(precision="fp64"), out="host")
     for (op, X, Y), z in zip(probs[:2], outs):
         assert rel(z, oracle.assemble(op, X, Y, qs)) < FP64_TOL
+
+
+def test_abort_interrupts_a_running_assembly_and_the_handle_recovers():
+    """bgb_abort from another thread makes a running bgb_assemble return BGB_ERR_ABORTED (the
+    kernels poll a host-mapped flag between tiles and pairs; nothing traps); the next call on the
+    same handle assembles normally."""
+    import threading
+    import time
+    from beastgpu_gb300 import _lib
+    from beastgpu_gb300.api import get_handle
+    m = bg.icosphere(5)
+    X = bg.raviartthomas(m)
+    op = bg.Maxwell3D.singlelayer(wavenumber=8 * np.pi)
+    cfg = bg.GPUConfiguration(precision="fp64")  # long enough (about a second) to be interrupted
+    h = get_handle(0)
+    result = {}
+
+    def run():
+        try:
+            bg.assemble_gpu(op, X, X, cfg, out="device")
+            result["rc"] = 0
+        except _lib.BGBError as e:
+            result["rc"] = e.code
+
+    t = threading.Thread(target=run)
+    t.start()
+    while t.is_alive():
+        _lib.load().bgb_abort(h.ptr)
+        time.sleep(0.005)
+    t.join()
+    assert result["rc"] == -5  # BGB_ERR_ABORTED
+    small = bg.icosphere(2)
+    Y = bg.raviartthomas(small)
+    ref = oracle.assemble(bg.Maxwell3D.singlelayer(wavenumber=K1), Y, Y, bg.QuadStrat())
+    z = bg.assemble_gpu(bg.Maxwell3D.singlelayer(wavenumber=K1), Y, Y, bg.GPUConfiguration(precision="fp64"))
+    assert rel(z, ref) < FP64_TOL
