@@ -317,3 +317,31 @@ def test_abort_interrupts_a_running_assembly_and_the_handle_recovers():
     ref = oracle.assemble(bg.Maxwell3D.singlelayer(wavenumber=K1), Y, Y, bg.QuadStrat())
     z = bg.assemble_gpu(bg.Maxwell3D.singlelayer(wavenumber=K1), Y, Y, bg.GPUConfiguration(precision="fp64"))
     assert rel(z, ref) < FP64_TOL
+
+
+@pytest.mark.parametrize("name", ["efie", "hh", "hs"])
+def test_distinct_test_and_trial_spaces(name):
+    """Test and trial spaces on different meshes (a sphere against a nearby plate, in both orders):
+    separate geometry, bounds and tile plans per side; rectangular matrices equal to the oracle's."""
+    sphere = bg.icosphere(2)
+    p = bg.plate(9, jitter=0.2, seed=5)
+    v = p.vertices.copy()
+    c = v[np.argmin(np.linalg.norm(v[:, :2] - 0.5, axis=1))].copy()
+    v[:, :2] -= c[:2]  # a plate vertex 0.01 above the sphere's north pole: near pairs across the meshes
+    v[:, 2] += 1.01
+    plate = bg.Mesh(v, p.triangles)
+    make = {"efie": lambda k: bg.Maxwell3D.singlelayer(wavenumber=k),
+            "hh": lambda k: bg.Helmholtz3D.singlelayer(wavenumber=k),
+            "hs": lambda k: bg.Helmholtz3D.hypersingular(wavenumber=k)}[name]
+    space = bg.raviartthomas if name == "efie" else bg.lagrangec0d1
+    op = make(2 * np.pi)
+    for X, Y in ((space(sphere), space(plate)), (space(plate), space(sphere))):
+        assert (oracle.classify_block(X, Y, op.wavenumber ** 2) == 4).any()
+        ref = oracle.assemble(op, X, Y, bg.QuadStrat())
+        assert ref.shape == (X.nfun, Y.nfun)
+        z64 = bg.assemble_gpu(op, X, Y, bg.GPUConfiguration(precision="fp64"))
+        zmx = bg.assemble_gpu(op, X, Y, bg.GPUConfiguration(precision="mixed"))
+        assert rel(z64, ref) < FP64_TOL
+        assert rel(zmx.astype(np.complex128), ref) < MIXED_TOL
+        part = bg.assemble_gpu(op, X, Y, bg.GPUConfiguration(precision="fp64"), rows=(3, X.nfun - 5))
+        np.testing.assert_array_equal(part, z64[3:X.nfun - 2])
