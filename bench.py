@@ -104,9 +104,10 @@ class ClockSampler:
     """nvidia-smi clock / throttle samples during the timed region."""
 
     def __init__(self, index):
+        import tempfile
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        self.path = os.path.join(tempfile.gettempdir(), f"bgb_clocks_{os.getpid()}.csv")
 
     def __enter__(self):
         try:
@@ -297,7 +298,7 @@ def run_c3(args):
     cfg = {"workload": "MFIE (RWG) + Helmholtz SL (Lagrange, interior vertices) on two jittered 96x96 plates, "
                        "gap 0.01, k=2*pi*2", "triangles": mesh.nt, "pairs_per_step": 2 * pairs,
            "l2": "outputs > L2; a 256 MiB buffer is written between timed steps"}
-    print(json.dumps(line_base(args, world, value, tot_ms["mixed"], "f32 far + double-float singular/near (mixed)",
+    print(json.dumps(line_base(args, world, value, tot_ms["mixed"], "f32 far pairs + double-float (f32 pairs) singular/near (mixed)",
                                cfg, fp64_value=world * 2 * pairs / (tot_ms["fp64"] * 1e-3), cases=res,
                                clocks=clocks.summary(), gpu_launches=launches)))
     return 0
@@ -365,7 +366,7 @@ def run_c4(args):
                        "one persistent CUDA-graph launch, autotuned tiles and schedule",
            "problems": 64, "triangles": sum(m.nt for m, _ in batch), "pairs_per_step": pairs}
     print(json.dumps(line_base(args, world, value, out["mixed"]["graph_ms_per_step"],
-                               "f32 far + double-float singular/near (mixed)", cfg,
+                               "f32 far pairs + double-float (f32 pairs) singular/near (mixed)", cfg,
                                vs_sequential_fp64=out["fp64"]["sequential_ms_per_step"] / out["mixed"]["graph_ms_per_step"],
                                results=out, clocks=clocks.summary(), gpu_launches=3 * (args.steps + args.warmup))))
     return 0
@@ -423,7 +424,7 @@ def run_c5(args):
     value = world * pairs / (ms * 1e-3)
     h2d = X.mesh.vertices.nbytes + X.mesh.triangles.nbytes + X.fn_index.nbytes + X.fn_coef.nbytes
     print(json.dumps(line_base(
-        args, world, value, ms, "f32 far + double-float singular/near (mixed)", cfg_d,
+        args, world, value, ms, "f32 far pairs + double-float (f32 pairs) singular/near (mixed)", cfg_d,
         e2e={"value": value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(nbytes)},
         pipeline={"out_blocks": st["out_blocks"], "ms_classify": st["ms_classify"], "ms_singular": st["ms_singular"],
                   "ms_far": far, "ms_copy": cp, "ms_pipeline": pipe, "ms_plan": st["ms_plan"],
@@ -549,7 +550,7 @@ def main():
                  "halo_redundancy": st_mixed[0]["pairs_computed"] / pairs})
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32 far pairs + f64 singular/near (mixed)",
+            "vs_baseline": None, "dtype": "f32 far pairs + double-float (f32 pairs) singular/near (mixed)",
             "data": "synthetic (seeded icosphere, built in-process)",
             "config": config_dict(mesh, X, {"parallelism": f"{world} independent matrices, one per rank, no collective"
                                             if world > 1 else "single GPU"}),
