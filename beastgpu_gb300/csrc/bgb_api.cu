@@ -264,6 +264,13 @@ const int kNumTileCfgs = sizeof(kTileCfgs) / sizeof(kTileCfgs[0]);
 // Upload helpers
 // ----------------------------------------------------------------------------------------
 template <class T>
+static int upload_on(cudaStream_t st, DevBuf& buf, const std::vector<T>& v) {
+  if (v.empty()) return 0;
+  BGB_CUDA(cudaMemcpyAsync(buf.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+  return 0;
+}
+
+template <class T>
 static int upload(bgb_handle* h, DevBuf& buf, const std::vector<T>& v, size_t offset_bytes) {
   if (v.empty()) return 0;
   BGB_CUDA(cudaMemcpyAsync((char*)buf.p + offset_bytes, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice,
@@ -476,12 +483,14 @@ int bgb_create(bgb_handle** out, const bgb_config* cfg) {
   cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, c.device);
   int rc = 0;
   if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess ||
-      (e = cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking)) != cudaSuccess) {
+      (e = cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking)) != cudaSuccess) {
     rc = cuda_fail(e, "cudaStreamCreate");
   }
   for (int i = 0; i < 8 && !rc; ++i)
-    if ((e = cudaEventCreate(&h->ev[i])) != cudaSuccess || (e = cudaEventCreate(&h->ev2[i])) != cudaSuccess)
-      rc = cuda_fail(e, "cudaEventCreate");
+    if ((e = cudaEventCreate(&h->ev[i])) != cudaSuccess) rc = cuda_fail(e, "cudaEventCreate");
+  for (int i = 0; i < 4 * bgb_handle::kSlots && !rc; ++i)
+    if ((e = cudaEventCreate(&h->ev2[i])) != cudaSuccess) rc = cuda_fail(e, "cudaEventCreate");
   for (int i = 0; i < 2 && !rc; ++i)
     if ((e = cudaEventCreateWithFlags(&h->ring_ev[i], cudaEventDisableTiming)) != cudaSuccess) rc = cuda_fail(e, "cudaEventCreate");
   if (!rc) {
@@ -506,20 +515,27 @@ int bgb_destroy(bgb_handle* h) {
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
+  if (h->stream2) cudaStreamSynchronize(h->stream2);
   DevBuf* bufs[] = {&h->verts_t, &h->tris_t, &h->verts_b, &h->tris_b, &h->geo_t, &h->geo_b, &h->bnd_t, &h->bnd_b, &h->bnd_c,
                     &h->rec_t, &h->rec_b, &h->cls_count, &h->cls_off, &h->ent_tau, &h->ent_sigma, &h->ent_cls, &h->ent_mask, &h->geodf_t, &h->geodf_b,
-                    &h->sing_L, &h->err, &h->plan_i[0], &h->plan_l[0], &h->plan_d[0], &h->plan_f[0], &h->far_items[0], &h->far_const[0], &h->plan_i[1], &h->plan_l[1], &h->plan_d[1], &h->plan_f[1], &h->far_items[1], &h->far_const[1], &h->df_tab, &h->stage[0], &h->stage[1], &h->tplan_i, &h->tplan_l, &h->tplan_d, &h->tplan_f,
+                    &h->sing_L, &h->err, &h->df_tab, &h->tplan_i, &h->tplan_l, &h->tplan_d, &h->tplan_f,
                     &h->diag_a, &h->diag_b, &h->diag_c, &h->diag_d};
   for (DevBuf* b : bufs) b->release();
-  for (int i = 0; i < 8; ++i) {
-    if (h->ev[i]) cudaEventDestroy(h->ev[i]);
-    if (h->ev2[i]) cudaEventDestroy(h->ev2[i]);
+  for (int k = 0; k < bgb_handle::kSlots; ++k) {
+    DevBuf* slot_bufs[] = {&h->plan_i[k], &h->plan_l[k], &h->plan_d[k], &h->plan_f[k], &h->far_items[k], &h->far_const[k],
+                           &h->stage[k]};
+    for (DevBuf* b : slot_bufs) b->release();
   }
+  for (int i = 0; i < 8; ++i)
+    if (h->ev[i]) cudaEventDestroy(h->ev[i]);
+  for (int i = 0; i < 4 * bgb_handle::kSlots; ++i)
+    if (h->ev2[i]) cudaEventDestroy(h->ev2[i]);
   for (int i = 0; i < 2; ++i)
     if (h->ring_ev[i]) cudaEventDestroy(h->ring_ev[i]);
   if (h->ring) cudaFreeHost(h->ring);
   if (h->stream) cudaStreamDestroy(h->stream);
   if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
+  if (h->stream2) cudaStreamDestroy(h->stream2);
   if (h->abort_host) cudaFreeHost((void*)h->abort_host);
   delete h;
   return 0;
@@ -709,7 +725,20 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
     const int64_t overlap_cols = std::max<int64_t>((ncols + 15) / 16, ((int64_t)64 << 20) / std::max<int64_t>(1, per_col));
     cols_per_block = std::min(std::min(cols_per_block, overlap_cols), ncols);
   }
-  const int nblocks = (int)((ncols + cols_per_block - 1) / cols_per_block);
+  // Block b covers columns [col_start[b], col_start[b + 1]).  With several blocks the first and the
+  // last are cut to about a quarter: the copies, which bound the pipeline when they are as fast as
+  // the fill, start sooner, and the last copy (the only one not hidden behind a far kernel) is short.
+  std::vector<int64_t> col_start;
+  for (int64_t c = 0; c < ncols; c += cols_per_block) col_start.push_back(c);
+  if (host_out && col_start.size() >= 4) {
+    const int64_t quarter = std::max<int64_t>(1, (cols_per_block + 3) / 4);
+    col_start.push_back(std::min(quarter, ncols - 1));
+    col_start.push_back(std::max<int64_t>(1, ncols - quarter));
+    std::sort(col_start.begin(), col_start.end());
+    col_start.erase(std::unique(col_start.begin(), col_start.end()), col_start.end());
+  }
+  col_start.push_back(ncols);
+  const int nblocks = (int)col_start.size() - 1;
   st.out_blocks = nblocks;
 
   // Host tile planning depends on the spaces only: it runs on worker threads while the device
@@ -744,10 +773,21 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
     const std::vector<int> rank_b = same ? rank_t : morton_rank(trial);
     const std::vector<int> ord_t = order_functions(St, rank_t, (int)row0, (int)(row0 + nrows));
     std::vector<std::vector<int>> ord_b(nblocks);
-    for (int b = 0; b < nblocks; ++b) {
-      const int64_t c0 = (int64_t)b * cols_per_block, c1 = std::min(ncols, c0 + cols_per_block);
-      ord_b[b] = order_functions(Sb, rank_b, (int)c0, (int)c1);
-    }
+    // per output block: function order and trial-side plan, blocks spread over the planner's threads
+    auto over_blocks = [&](auto fn) {
+      if (nblocks == 1) {
+        fn(0, nth);
+        return;
+      }
+      std::vector<std::thread> th;
+      const int nt = std::min(nth, nblocks);
+      for (int t = 0; t < nt; ++t)
+        th.emplace_back([&, t] {
+          for (int b = t; b < nblocks; b += nt) fn(b, 1);
+        });
+      for (auto& x : th) x.join();
+    };
+    over_blocks([&](int b, int) { ord_b[b] = order_functions(Sb, rank_b, (int)col_start[b], (int)col_start[b + 1]); });
     size_t smem = 0;
     for (int id : prefs) {
       const TileCfg tc = kTileCfgs[id];
@@ -757,8 +797,8 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
       TilePlan probe{};
       probe.FM = tc.FM; probe.FN = tc.FN; probe.SC = tc.SC; probe.MAXS = PL.test.MAXS;
       probe.tmax = std::max(1, PL.test.tmax);
+      over_blocks([&](int b, int threads) { plan_trial_side_par(Sb, ord_b[b], tc.FN, tc.SC, PL.trial[b], threads); });
       for (int b = 0; b < nblocks; ++b) {
-        plan_trial_side_par(Sb, ord_b[b], tc.FN, tc.SC, PL.trial[b], nth);
         probe.gmax = std::max(probe.gmax, PL.trial[b].gmax);
         probe.gsmax = std::max(probe.gsmax, PL.trial[b].gsmax);
         probe.nmax = std::max(probe.nmax, std::max(1, PL.trial[b].nmax));
@@ -833,7 +873,7 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
     prefaulter = std::thread([&] {
       const int nth = (int)std::min(16u, std::max(1u, std::thread::hardware_concurrency()));
       for (int b = 0; b < nblocks && !PF.stop; ++b) {
-        const int64_t c0 = (int64_t)b * cols_per_block, nc = std::min(cols_per_block, ncols - c0);
+        const int64_t c0 = col_start[b], nc = col_start[b + 1] - c0;
         char* base = (char*)out + (size_t)c0 * ld * esz;
         if (ld == nrows) {
           prefault_range(base, (size_t)nc * nrows * esz, nth);
@@ -937,7 +977,8 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
 
   double ms_far = 0, ms_copy = 0;
   int64_t pairs_computed = 0;
-  bool pending[2] = {false, false};
+  constexpr int NS = bgb_handle::kSlots;
+  bool pending[NS] = {};
   auto harvest = [&](int slot) {  // times of the block that last used `slot` (complete)
     if (!pending[slot]) return;
     ms_far += event_ms(h->ev2[slot * 4 + 0], h->ev2[slot * 4 + 1]);
@@ -951,14 +992,15 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
     std::vector<int4> items;
     TilePlan T;
   };
-  SlotHost slot_host[2];
+  SlotHost slot_host[NS];
   // upload the trial-side tables of block b into its slot and launch the far kernel
   auto enqueue_block = [&](int b) -> int {
-    const int slot = b & 1;
-    const int64_t c0 = (int64_t)b * cols_per_block;
-    const int64_t nc = std::min(cols_per_block, ncols - c0);
+    const int slot = b % NS;
+    cudaStream_t cst = (b & 1) ? h->stream2 : h->stream;  // consecutive blocks alternate compute streams
+    const int64_t c0 = col_start[b];
+    const int64_t nc = col_start[b + 1] - c0;
     const HostPlan& PB = PL.trial[b];
-    if (pending[slot]) {  // block b-2 used this slot: its kernel and copy must be complete
+    if (pending[slot]) {  // block b - NS used this slot: its kernel and copy must be complete
       BGB_CUDA(cudaEventSynchronize(h->ev2[slot * 4 + (host_out ? 3 : 1)]));
       harvest(slot);
     }
@@ -990,8 +1032,8 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
         (rc2 = h->far_const[slot].ensure(sizeof(FarConst) + sizeof(TilePlan) + sizeof(int) * 4)))
       return rc2;
     if (host_out && (rc2 = h->stage[slot].ensure(esz * (size_t)cols_per_block * nrows))) return rc2;
-    if ((rc2 = upload(h, h->plan_i[slot], H.I, 0)) || (rc2 = upload(h, h->plan_l[slot], H.L, 0)) ||
-        (rc2 = upload(h, h->plan_d[slot], PB.gs_coef, 0)) || (rc2 = upload(h, h->plan_f[slot], H.F, 0)))
+    if ((rc2 = upload_on(cst, h->plan_i[slot], H.I)) || (rc2 = upload_on(cst, h->plan_l[slot], H.L)) ||
+        (rc2 = upload_on(cst, h->plan_d[slot], PB.gs_coef)) || (rc2 = upload_on(cst, h->plan_f[slot], H.F)))
       return rc2;
     const int* ti = h->tplan_i.as<int>();
     const int* bi = h->plan_i[slot].as<int>();
@@ -1040,28 +1082,28 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
     FarConst* dK = (FarConst*)h->far_const[slot].p;
     TilePlan* dT = (TilePlan*)((char*)h->far_const[slot].p + sizeof(FarConst));
     int* dctr = (int*)((char*)h->far_const[slot].p + sizeof(FarConst) + sizeof(TilePlan));
-    BGB_CUDA(cudaMemcpyAsync(dK, &K, sizeof(FarConst), cudaMemcpyHostToDevice, h->stream));
-    BGB_CUDA(cudaMemcpyAsync(dT, &T, sizeof(TilePlan), cudaMemcpyHostToDevice, h->stream));
+    BGB_CUDA(cudaMemcpyAsync(dK, &K, sizeof(FarConst), cudaMemcpyHostToDevice, cst));
+    BGB_CUDA(cudaMemcpyAsync(dT, &T, sizeof(TilePlan), cudaMemcpyHostToDevice, cst));
     if (!H.items.empty())
       BGB_CUDA(cudaMemcpyAsync(h->far_items[slot].p, H.items.data(), sizeof(int4) * H.items.size(),
-                               cudaMemcpyHostToDevice, h->stream));
-    BGB_CUDA(cudaMemsetAsync(dctr, 0, sizeof(int), h->stream));
+                               cudaMemcpyHostToDevice, cst));
+    BGB_CUDA(cudaMemsetAsync(dctr, 0, sizeof(int), cst));
     const int ctas = (int)std::min<int64_t>((int64_t)H.items.size(), (int64_t)std::max(1, per_sm) * h->num_sms);
-    BGB_CUDA(cudaEventRecord(h->ev2[slot * 4 + 0], h->stream));
+    BGB_CUDA(cudaEventRecord(h->ev2[slot * 4 + 0], cst));
     if ((rc2 = launch_far_persistent(precision, K.op_kind, gen, dK, dT, (const int4*)h->far_items[slot].p,
-                                     (int)H.items.size(), dctr, smem, std::max(1, ctas), h->abort_dev, h->stream)))
+                                     (int)H.items.size(), dctr, smem, std::max(1, ctas), h->abort_dev, cst)))
       return rc2;
     ++launches;
-    BGB_CUDA(cudaEventRecord(h->ev2[slot * 4 + 1], h->stream));
+    BGB_CUDA(cudaEventRecord(h->ev2[slot * 4 + 1], cst));
     pending[slot] = true;
     (void)nc;
     return 0;
   };
   // copy block b to the host on the side stream; pageable destinations go through the pinned ring
   auto copy_block = [&](int b) -> int {
-    const int slot = b & 1;
-    const int64_t c0 = (int64_t)b * cols_per_block;
-    const int64_t nc = std::min(cols_per_block, ncols - c0);
+    const int slot = b % NS;
+    const int64_t c0 = col_start[b];
+    const int64_t nc = col_start[b + 1] - c0;
     cudaStream_t cs = h->copy_stream;
     if (dst_kind == DST_PAGEABLE) PF.wait_for(b + 1);  // pages of this block are resident
     BGB_CUDA(cudaStreamWaitEvent(cs, h->ev2[slot * 4 + 1], 0));
@@ -1104,8 +1146,13 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
     return 0;
   };
   const auto t_pipe = clk::now();
+  // the second compute stream starts after everything enqueued so far (classification, singular
+  // pairs, records, test-side tables)
+  BGB_CUDA(cudaEventRecord(h->ev[3], h->stream));
+  BGB_CUDA(cudaStreamWaitEvent(h->stream2, h->ev[3], 0));
   auto drain = [&](int code) {  // the slots' host tables must outlive uploads still in flight
     cudaStreamSynchronize(h->stream);
+    cudaStreamSynchronize(h->stream2);
     cudaStreamSynchronize(h->copy_stream);
     return code;
   };
@@ -1116,9 +1163,9 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
     if ((rc = check_abort(h))) return drain(rc);
   }
   BGB_CUDA(cudaStreamSynchronize(h->stream));
+  BGB_CUDA(cudaStreamSynchronize(h->stream2));
   BGB_CUDA(cudaStreamSynchronize(h->copy_stream));
-  harvest(0);
-  harvest(1);
+  for (int k = 0; k < NS; ++k) harvest(k);
   const double ms_pipe = std::chrono::duration<double, std::milli>(clk::now() - t_pipe).count();
   if ((rc = check_abort(h))) return rc;
   st.ms_copy = ms_copy;

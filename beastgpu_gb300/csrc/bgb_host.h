@@ -44,6 +44,8 @@ struct bgb_handle {
   int num_sms = 0;
   cudaStream_t stream = nullptr;
   cudaStream_t copy_stream = nullptr;
+  cudaStream_t stream2 = nullptr;  // second compute stream: consecutive output blocks alternate, so one
+                                   // block's far kernel starts while the previous one drains
   bgb_config cfg{};
   volatile int* abort_host = nullptr;
   int* abort_dev = nullptr;
@@ -51,12 +53,13 @@ struct bgb_handle {
   // buffers
   bgb::DevBuf verts_t, tris_t, verts_b, tris_b, geo_t, geo_b, bnd_t, bnd_b, bnd_c, rec_t, rec_b;
   bgb::DevBuf cls_count, cls_off, ent_tau, ent_sigma, ent_cls, ent_mask, sing_L, err, geodf_t, geodf_b;
-  bgb::DevBuf plan_i[2], plan_l[2], plan_d[2], plan_f[2], far_items[2], far_const[2], df_tab;
+  static constexpr int kSlots = 3;  // output-block slots in flight (staging, plan tables, events)
+  bgb::DevBuf plan_i[kSlots], plan_l[kSlots], plan_d[kSlots], plan_f[kSlots], far_items[kSlots], far_const[kSlots], df_tab;
   bgb::DevBuf tplan_i, tplan_l, tplan_d, tplan_f;  // test-side tile tables (shared by all output blocks)
-  bgb::DevBuf stage[2];
+  bgb::DevBuf stage[kSlots];
   bgb::DevBuf diag_a, diag_b, diag_c, diag_d;
   cudaEvent_t ev[8] = {};
-  cudaEvent_t ev2[8] = {};   // per row-block slot: far start / end, copy start / end
+  cudaEvent_t ev2[4 * kSlots] = {};  // per output-block slot: far start / end, copy start / end
   cudaEvent_t ring_ev[2] = {};
   void* ring = nullptr;      // pinned host staging ring
   size_t ring_bytes = 0;
