@@ -479,8 +479,8 @@ __device__ __forceinline__ void far_pair_fp64(const FarScalars& K, const double 
       const double Yx = b[OB::X + 3 * J], Yy = b[OB::X + 3 * J + 1], Yz = b[OB::X + 3 * J + 2];
       const double dx = ax - Yx, dy = ay - Yy, dz = az - Yz;
       const double R2 = dx * dx + dy * dy + dz * dz;
-      const double R = sqrt(R2);
-      const double rinv = 1.0 / R;
+      const double rinv = rsqrt(R2);
+      const double R = R2 * rinv;
       double sn = 0.0, cs = 1.0;
       if (gim != 0.0) sincos(gim * R, &sn, &cs);
       double amp = wI * b[OB::W + J] * rinv;
