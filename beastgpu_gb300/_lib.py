@@ -17,7 +17,7 @@ STATUS = {0: "OK", -1: "INVALID", -2: "OOM", -3: "CUDA", -4: "TIMEOUT", -5: "ABO
 PREC_FP64, PREC_MIXED = 0, 1
 OUT_HOST_C64, OUT_HOST_C32, OUT_DEVICE_C64, OUT_DEVICE_C32 = 0, 1, 2, 3
 CFG_PAGEABLE_VIA_RING = 1
-ABI_VERSION = 2  # BGB_ABI_VERSION of include/beastgb.h
+ABI_VERSION = 3  # BGB_ABI_VERSION of include/beastgb.h
 
 
 class BGBError(RuntimeError):
@@ -67,6 +67,20 @@ class Problem(C.Structure):
                 ("ld", C.c_int64)]
 
 
+class Operator2D(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("wavenumber", C.c_double), ("alpha", C.c_double * 2), ("beta", C.c_double * 2)]
+
+
+class CurveSpace(C.Structure):
+    _fields_ = [("refspace", C.c_int32), ("nv", C.c_int32), ("ns", C.c_int32), ("nfun", C.c_int32),
+                ("vertices", C.c_void_p), ("segments", C.c_void_p), ("fn_index", C.c_void_p),
+                ("fn_coef", C.c_void_p)]
+
+
+class QuadStrat2D(C.Structure):
+    _fields_ = [("far_test", C.c_int32), ("far_trial", C.c_int32), ("near", C.c_int32), ("singular", C.c_int32)]
+
+
 # every exported symbol of include/beastgb.h with its ctypes signature
 SIGNATURES = {
     "bgb_abi_version": ([], C.c_int),
@@ -94,6 +108,12 @@ SIGNATURES = {
     "bgb_classify_csr_noalloc": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
                                   C.c_int32, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
                                   C.POINTER(C.c_int64), C.c_void_p], C.c_int),
+    "bgb_assemble_curve": ([C.c_void_p, C.POINTER(Operator2D), C.POINTER(CurveSpace), C.POINTER(CurveSpace),
+                            C.POINTER(QuadStrat2D), C.c_void_p, C.c_int32, C.c_int64, C.c_int64, C.c_int64, C.c_void_p,
+                            C.POINTER(Stats)], C.c_int),
+    "bgb_local_matrices_curve": ([C.c_void_p, C.POINTER(Operator2D), C.POINTER(CurveSpace), C.POINTER(CurveSpace),
+                                  C.POINTER(QuadStrat2D), C.c_int64, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p,
+                                  C.c_void_p], C.c_int),
 }
 
 _lib = None

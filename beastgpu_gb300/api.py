@@ -20,6 +20,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _lib
+from .curves import CurveSpace, Operator2D, QuadStrat2D, defaultquadstrat2d
 from .operators import Operator, QuadStrat, defaultquadstrat
 from .spaces import Space
 
@@ -138,6 +139,23 @@ def c_operator(op: Operator) -> _lib.Operator:
                          (C.c_double * 2)(g.real, g.imag))
 
 
+def c_curve_space(space: CurveSpace, keep: _Keep) -> _lib.CurveSpace:
+    m = space.mesh
+    return _lib.CurveSpace(space.refspace, m.nv, m.ns, space.nfun, keep.ptr(m.vertices, np.float64),
+                           keep.ptr(m.segments, np.int32), keep.ptr(space.fn_index, np.int32),
+                           keep.ptr(space.fn_coef, np.float64))
+
+
+def c_operator2d(op: Operator2D) -> _lib.Operator2D:
+    a, b = complex(op.alpha), complex(op.beta)
+    return _lib.Operator2D(op.kind, float(op.wavenumber), (C.c_double * 2)(a.real, a.imag),
+                           (C.c_double * 2)(b.real, b.imag))
+
+
+def c_quadstrat2d(qs: QuadStrat2D) -> _lib.QuadStrat2D:
+    return _lib.QuadStrat2D(qs.far_test, qs.far_trial, qs.near, qs.singular)
+
+
 def c_quadstrat(qs: QuadStrat) -> _lib.QuadStrat:
     return _lib.QuadStrat(qs.far_test, qs.far_trial, qs.near_test, qs.near_trial, qs.ss_cf, qs.ss_ce, qs.ss_cv)
 
@@ -160,6 +178,9 @@ def assemble_gpu(operator: Operator, test_functions: Space, trial_functions: Spa
     buffer of the right shape/dtype to write into.
     """
     config = config or GPUConfiguration()
+    if isinstance(test_functions, CurveSpace):
+        return _assemble_curve(operator, test_functions, trial_functions, config, quadstrat, out, dtype, rows,
+                               out_buffer, stream, return_stats)
     quadstrat = quadstrat or defaultquadstrat(operator, test_functions, trial_functions)
     prec = _precision(config.precision)
     if dtype is None:
@@ -203,6 +224,61 @@ def assemble_gpu(operator: Operator, test_functions: Space, trial_functions: Spa
     else:
         raise ValueError("out must be 'host' or 'device'")
     return (Z, stats.as_dict()) if return_stats else Z
+
+
+def _assemble_curve(operator, X, Y, config, quadstrat, out, dtype, rows, out_buffer, stream, return_stats):
+    """The curve (2-D) path: FP64 arithmetic; dtype complex128 (default) or complex64 output."""
+    if not isinstance(Y, CurveSpace) or not isinstance(operator, Operator2D):
+        raise TypeError("curve spaces need a Helmholtz2D operator and a curve trial space")
+    quadstrat = quadstrat or defaultquadstrat2d(operator, X, Y)
+    dtype = np.dtype(np.complex128 if dtype is None else dtype)
+    if dtype not in (np.complex128, np.complex64):
+        raise ValueError("dtype must be complex128 or complex64")
+    c64 = dtype == np.complex128
+    row0, nrows = (0, X.nfun) if rows is None else (int(rows[0]), int(rows[1]))
+    ncols = Y.nfun
+    h = get_handle(config.device, config.total_GPU_budget, config.tile_config, config.pinned_ring_bytes, 0)
+    keep = _Keep()
+    cop, ct, cb, cq = c_operator2d(operator), c_curve_space(X, keep), c_curve_space(Y, keep), c_quadstrat2d(quadstrat)
+    stats = _lib.Stats()
+    lib = _lib.load()
+    if out == "host":
+        Z = np.empty((nrows, ncols), dtype=dtype, order="F") if out_buffer is None else out_buffer
+        ptr = Z.data_ptr() if hasattr(Z, "data_ptr") else Z.ctypes.data
+        kind = _lib.OUT_HOST_C64 if c64 else _lib.OUT_HOST_C32
+        _lib.check(lib.bgb_assemble_curve(h.ptr, C.byref(cop), C.byref(ct), C.byref(cb), C.byref(cq), C.c_void_p(ptr),
+                                          kind, max(1, nrows), row0, nrows, None, C.byref(stats)))
+    elif out == "device":
+        import torch
+        tdt = torch.complex128 if c64 else torch.complex64
+        Zt = torch.empty((ncols, max(1, nrows)), dtype=tdt, device=f"cuda:{config.device}") if out_buffer is None \
+            else out_buffer
+        st = stream if stream is not None else torch.cuda.current_stream(config.device).cuda_stream
+        kind = _lib.OUT_DEVICE_C64 if c64 else _lib.OUT_DEVICE_C32
+        _lib.check(lib.bgb_assemble_curve(h.ptr, C.byref(cop), C.byref(ct), C.byref(cb), C.byref(cq),
+                                          C.c_void_p(Zt.data_ptr()), kind, max(1, nrows), row0, nrows, C.c_void_p(st),
+                                          C.byref(stats)))
+        Z = Zt.T
+    else:
+        raise ValueError("out must be 'host' or 'device'")
+    return (Z, stats.as_dict()) if return_stats else Z
+
+
+def local_matrices_curve(operator: Operator2D, test_functions: CurveSpace, trial_functions: CurveSpace, tau, sigma, *,
+                         quadstrat: QuadStrat2D = None, force_class: int = -1, device: int = 0):
+    """2x2 local matrices L[p, i, j] of explicit segment pairs and their classes (curve path)."""
+    quadstrat = quadstrat or defaultquadstrat2d()
+    tau = np.ascontiguousarray(tau, dtype=np.int32)
+    sigma = np.ascontiguousarray(sigma, dtype=np.int32)
+    h = get_handle(device)
+    keep = _Keep()
+    out = np.empty((tau.size, 2, 2, 2), dtype=np.float64)
+    cls = np.empty(tau.size, dtype=np.int8)
+    _lib.check(_lib.load().bgb_local_matrices_curve(
+        h.ptr, C.byref(c_operator2d(operator)), C.byref(c_curve_space(test_functions, keep)),
+        C.byref(c_curve_space(trial_functions, keep)), C.byref(c_quadstrat2d(quadstrat)), tau.size, tau.ctypes.data,
+        sigma.ctypes.data, int(force_class), out.ctypes.data, cls.ctypes.data))
+    return out[..., 0] + 1j * out[..., 1], cls
 
 
 def row_shard(nrows: int, rank: int, world: int):

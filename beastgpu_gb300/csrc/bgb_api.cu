@@ -104,7 +104,7 @@ RuleTable make_rules() {
 }
 
 // Gauss-Legendre on [0, 1], ascending (Newton on the Legendre recurrence).
-static void gauss_legendre01(int n, double* x, double* w) {
+void gauss_legendre01(int n, double* x, double* w) {
   for (int i = 0; i < n; ++i) {
     double t = -std::cos(M_PI * (i + 0.75) / (n + 0.5)), dp = 1.0;
     for (int it = 0; it < 100; ++it) {
@@ -521,6 +521,7 @@ int bgb_destroy(bgb_handle* h) {
                     &h->sing_L, &h->err, &h->df_tab, &h->tplan_i, &h->tplan_l, &h->tplan_d, &h->tplan_f,
                     &h->diag_a, &h->diag_b, &h->diag_c, &h->diag_d};
   for (DevBuf* b : bufs) b->release();
+  h->curve.release();
   for (int k = 0; k < bgb_handle::kSlots; ++k) {
     DevBuf* slot_bufs[] = {&h->plan_i[k], &h->plan_l[k], &h->plan_d[k], &h->plan_f[k], &h->far_items[k], &h->far_const[k],
                            &h->stage[k]};

@@ -1,0 +1,904 @@
+// Curve (2-D) path of libbeastgb: BEAST Helmholtz2D operators on polygonal curves, in FP64.
+//
+//   upload curves -> k_curve_geo -> per block of output columns:
+//     k_curve_classify (non-far pairs into a list) -> k_curve_far (one thread per far pair,
+//     Gauss-Legendre product rule) -> k_curve_special (one warp per coincident, common-vertex
+//     or near pair) -> k_curve_gather (one thread per matrix entry, supports in a fixed order)
+//
+// The reference's 2-D prototype (old_code/doubleQuadRule_2d_gpu.jl:129-210, :265-465) integrates
+// one segment pair per host call, with one GPU thread per point pair and a reduction into the
+// 2x2 result.  Here one launch integrates every pair of a block of columns (a thread per far
+// pair, a warp per singular or near pair), and the matrix is gathered without atomics.  The
+// Hankel functions are CUDA's double-precision Bessel functions (the prototype's truncated series
+// at :31-64 hold only for small kR).
+#include "bgb_host.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+namespace bgb {
+namespace curve {
+
+struct SegGeo {
+  double x0, y0, x1, y1;  // vertices v0, v1
+  double dx, dy;          // v1 - v0
+  double len, nx, ny;     // length and unit normal (dy, -dx) / len
+};
+
+constexpr int kMaxGL = 32;
+constexpr int kMaxSing = 16;
+constexpr int kMaxGraded = (3 * kMaxSing + 1) * kMaxSing;
+constexpr int kMaxDepth = 16;  // bisections of a near pair
+constexpr double kInv2Pi = 0.15915494309189535;
+
+// Point rules of one call (copied to shared memory by the kernels that use them).
+struct Rules {
+  int nft, nfb, nnear, nsing, ngraded, pad;
+  double ft_x[kMaxGL], ft_w[kMaxGL], fb_x[kMaxGL], fb_w[kMaxGL], nr_x[kMaxGL], nr_w[kMaxGL];
+  double sg_x[kMaxSing], sg_w[kMaxSing];  // Gauss-Legendre, smooth direction of the singular rules
+  double gz[kMaxGraded], gwz[kMaxGraded];  // graded rule towards 0
+};
+
+struct Op {
+  int kind, nsA, nsB, LS;  // LS = nsA * nsB entries per local matrix
+  double k, k2;
+  double ar, ai, br, bi;
+};
+
+// A non-far pair: its local matrix goes to L[slot .. slot + LS).
+struct Special {
+  int64_t slot;
+  int tau, sigma;
+  int cls, match;  // match = 2 * (local vertex of tau) + (local vertex of sigma) of the first shared vertex
+};
+
+struct Acc {
+  double pr[4], pi[4];  // sum of kernel x weight x f_i g_j, index 2 i + j
+  double mr, mi;        // hypersingular: sum of G x weight
+};
+
+// ----------------------------------------------------------------------------------------
+// Device functions
+// ----------------------------------------------------------------------------------------
+__global__ void k_curve_geo(const double* __restrict__ v, const int* __restrict__ seg, int ns, SegGeo* __restrict__ out) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ns) return;
+  const int a = seg[2 * e], b = seg[2 * e + 1];
+  SegGeo g;
+  g.x0 = v[2 * a];
+  g.y0 = v[2 * a + 1];
+  g.x1 = v[2 * b];
+  g.y1 = v[2 * b + 1];
+  g.dx = __dsub_rn(g.x1, g.x0);
+  g.dy = __dsub_rn(g.y1, g.y0);
+  g.len = __dsqrt_rn(__dadd_rn(__dmul_rn(g.dx, g.dx), __dmul_rn(g.dy, g.dy)));
+  g.nx = __ddiv_rn(g.dy, g.len);
+  g.ny = __ddiv_rn(-g.dx, g.len);
+  out[e] = g;
+}
+
+// Pair class with BEAST's predicate over the segments' vertices (doubleQuadRuleMainCase.jl:187-200,
+// quadrule_determine.jl:1-3), the trial length standing for the chart volume; every operation
+// rounded as written (no contraction), as the oracle is compiled.  -1: degenerate pair.
+__device__ __forceinline__ int classify(const SegGeo& a, const SegGeo& b, double k2, int* match) {
+  const double dtol = 2.220446049250313e-16 * 1.0e3;
+  const double xtol2 = 0.2 * 0.2;
+  const double ax[2] = {a.x0, a.x1}, ay[2] = {a.y0, a.y1};
+  const double bx[2] = {b.x0, b.x1}, by[2] = {b.y0, b.y1};
+  int hits = 0;
+  double dmin2 = 1.7976931348623157e308;
+  *match = -1;
+#pragma unroll
+  for (int u1 = 0; u1 < 2; ++u1)
+#pragma unroll
+    for (int u2 = 0; u2 < 2; ++u2) {
+      const double dx = __dsub_rn(ax[u1], bx[u2]), dy = __dsub_rn(ay[u1], by[u2]);
+      const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+      if (__dsqrt_rn(d2) < dtol) {
+        if (hits == 0) *match = 2 * u1 + u2;
+        ++hits;
+      }
+      dmin2 = fmin(dmin2, d2);
+    }
+  if (hits > 2) return -1;
+  if (hits == 2) return 3;
+  if (hits == 1) return 1;
+  const double m = fmax(__dmul_rn(dmin2, k2), __ddiv_rn(dmin2, __dmul_rn(16.0, b.len)));
+  return m >= xtol2 ? 0 : 4;
+}
+
+// One point pair: chart parameters s (test) and t (trial), separation r = x - y, rule weight w.
+template <int OP>
+__device__ __forceinline__ void add_point(const Op& op, const SegGeo& A, const SegGeo& B, double s, double t,
+                                          double rx, double ry, double w, Acc& c) {
+  const double R = sqrt(rx * rx + ry * ry);
+  double Kr, Ki;
+  if (OP == BGB_OP2D_SL || OP == BGB_OP2D_HS) {
+    if (op.k == 0.0) {
+      Kr = -log(R) * kInv2Pi;
+      Ki = 0.0;
+    } else {
+      const double z = op.k * R;
+      Kr = -0.25 * y0(z);
+      Ki = -0.25 * j0(z);
+    }
+  } else {
+    double gr, gi;
+    if (op.k == 0.0) {
+      gr = -kInv2Pi / (R * R);
+      gi = 0.0;
+    } else {
+      const double z = op.k * R, f = op.k / (4.0 * R);
+      gr = f * y1(z);
+      gi = f * j1(z);
+    }
+    const double proj = OP == BGB_OP2D_DL ? -(rx * B.nx + ry * B.ny) : rx * A.nx + ry * A.ny;
+    Kr = gr * proj;
+    Ki = gi * proj;
+  }
+  const double ww = w * A.len * B.len;
+  Kr *= ww;
+  Ki *= ww;
+  const double f[2] = {op.nsA == 1 ? 1.0 : 1.0 - s, s};
+  const double g[2] = {op.nsB == 1 ? 1.0 : 1.0 - t, t};
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const double fg = f[i] * g[j];
+      c.pr[2 * i + j] += Kr * fg;
+      c.pi[2 * i + j] += Ki * fg;
+    }
+  if (OP == BGB_OP2D_HS) {
+    c.mr += Kr;
+    c.mi += Ki;
+  }
+}
+
+template <int OP>
+__device__ __forceinline__ void finalize(const Op& op, const SegGeo& A, const SegGeo& B, const Acc& c,
+                                         double2* __restrict__ out) {
+  const double nn = A.nx * B.nx + A.ny * B.ny;
+  const double dA[2] = {op.nsA == 2 ? -1.0 / A.len : 0.0, op.nsA == 2 ? 1.0 / A.len : 0.0};
+  const double dB[2] = {op.nsB == 2 ? -1.0 / B.len : 0.0, op.nsB == 2 ? 1.0 / B.len : 0.0};
+  const double bmr = op.br * c.mr - op.bi * c.mi, bmi = op.br * c.mi + op.bi * c.mr;
+  for (int i = 0; i < op.nsA; ++i)
+    for (int j = 0; j < op.nsB; ++j) {
+      const double pr = c.pr[2 * i + j], pi = c.pi[2 * i + j];
+      double lr = op.ar * pr - op.ai * pi, li = op.ar * pi + op.ai * pr;
+      if (OP == BGB_OP2D_HS) {
+        const double d = dA[i] * dB[j];
+        lr = lr * nn + bmr * d;
+        li = li * nn + bmi * d;
+      }
+      out[i * op.nsB + j] = make_double2(lr, li);
+    }
+}
+
+__device__ __forceinline__ void acc_zero(Acc& c) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) c.pr[k] = c.pi[k] = 0.0;
+  c.mr = c.mi = 0.0;
+}
+
+// Far pair: Gauss-Legendre product rule, one thread (doubleQuadRule_2d_gpu.jl:142-181).
+template <int OP>
+__device__ __forceinline__ void far_pair(const Op& op, const double* fx, const double* fw, int nft, const double* bx,
+                                         const double* bw, int nfb, const SegGeo& A, const SegGeo& B, Acc& c) {
+  for (int p = 0; p < nft; ++p) {
+    const double s = fx[p];
+    const double x0 = A.x0 + s * A.dx, x1 = A.y0 + s * A.dy;
+    for (int q = 0; q < nfb; ++q) {
+      const double t = bx[q];
+      const double y0v = B.x0 + t * B.dx, y1v = B.y0 + t * B.dy;
+      add_point<OP>(op, A, B, s, t, x0 - y0v, x1 - y1v, fw[p] * bw[q], c);
+    }
+  }
+}
+
+__device__ __forceinline__ double point_seg_dist2(double px, double py, double ax, double ay, double bx, double by) {
+  const double dx = __dsub_rn(bx, ax), dy = __dsub_rn(by, ay);
+  const double L2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+  double t = L2 > 0.0 ? __ddiv_rn(__dadd_rn(__dmul_rn(__dsub_rn(px, ax), dx), __dmul_rn(__dsub_rn(py, ay), dy)), L2) : 0.0;
+  t = t < 0.0 ? 0.0 : (t > 1.0 ? 1.0 : t);
+  const double ex = __dsub_rn(__dadd_rn(ax, __dmul_rn(t, dx)), px), ey = __dsub_rn(__dadd_rn(ay, __dmul_rn(t, dy)), py);
+  return __dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey));
+}
+
+// Warp-cooperative rules: every lane runs the same control flow and integrates the points
+// k = lane, lane + 32, ... of each rule; the partial sums are reduced by the caller.
+template <int OP>
+__device__ void near_rule_warp(const Op& op, const Rules& R, const SegGeo& A, const SegGeo& B, int lane, Acc& c) {
+  struct Box {
+    double s0, s1, t0, t1;
+    int depth;
+  };
+  Box stack[2 * kMaxDepth + 4];
+  int top = 0;
+  stack[top++] = Box{0.0, 1.0, 0.0, 1.0, 0};
+  const int n = R.nnear;
+  while (top > 0) {
+    const Box b = stack[--top];
+    const double p0x = __dadd_rn(A.x0, __dmul_rn(b.s0, A.dx)), p0y = __dadd_rn(A.y0, __dmul_rn(b.s0, A.dy));
+    const double p1x = __dadd_rn(A.x0, __dmul_rn(b.s1, A.dx)), p1y = __dadd_rn(A.y0, __dmul_rn(b.s1, A.dy));
+    const double q0x = __dadd_rn(B.x0, __dmul_rn(b.t0, B.dx)), q0y = __dadd_rn(B.y0, __dmul_rn(b.t0, B.dy));
+    const double q1x = __dadd_rn(B.x0, __dmul_rn(b.t1, B.dx)), q1y = __dadd_rn(B.y0, __dmul_rn(b.t1, B.dy));
+    const double la = __dmul_rn(__dsub_rn(b.s1, b.s0), A.len), lb = __dmul_rn(__dsub_rn(b.t1, b.t0), B.len);
+    double d2 = point_seg_dist2(p0x, p0y, q0x, q0y, q1x, q1y);
+    d2 = fmin(d2, point_seg_dist2(p1x, p1y, q0x, q0y, q1x, q1y));
+    d2 = fmin(d2, point_seg_dist2(q0x, q0y, p0x, p0y, p1x, p1y));
+    d2 = fmin(d2, point_seg_dist2(q1x, q1y, p0x, p0y, p1x, p1y));
+    if (b.depth < kMaxDepth && __dsqrt_rn(d2) < fmax(la, lb)) {
+      if (la >= lb) {
+        const double sm = 0.5 * (b.s0 + b.s1);
+        stack[top++] = Box{sm, b.s1, b.t0, b.t1, b.depth + 1};
+        stack[top++] = Box{b.s0, sm, b.t0, b.t1, b.depth + 1};
+      } else {
+        const double tm = 0.5 * (b.t0 + b.t1);
+        stack[top++] = Box{b.s0, b.s1, tm, b.t1, b.depth + 1};
+        stack[top++] = Box{b.s0, b.s1, b.t0, tm, b.depth + 1};
+      }
+      continue;
+    }
+    const double hs = b.s1 - b.s0, ht = b.t1 - b.t0;
+    for (int k = lane; k < n * n; k += 32) {
+      const int p = k / n, q = k - p * n;
+      const double s = b.s0 + hs * R.nr_x[p], t = b.t0 + ht * R.nr_x[q];
+      const double rx = (A.x0 + s * A.dx) - (B.x0 + t * B.dx), ry = (A.y0 + s * A.dy) - (B.y0 + t * B.dy);
+      add_point<OP>(op, A, B, s, t, rx, ry, (hs * R.nr_w[p]) * (ht * R.nr_w[q]), c);
+    }
+  }
+}
+
+// Coincident (match 0: same orientation, 1: reversed) and common-vertex rules: the chart square
+// split along its diagonal, graded coordinate z towards the singularity, Gauss coordinate w.
+template <int OP>
+__device__ void singular_rule_warp(const Op& op, const Rules& R, const SegGeo& A, const SegGeo& B, int cls,
+                                   int match, int lane, Acc& c) {
+  const int n = R.nsing, nz = R.ngraded, per_half = nz * n;
+  if (cls == 3) {
+    if (OP == BGB_OP2D_DL || OP == BGB_OP2D_DLT) return;  // r lies along the segment
+    const bool same = match == 0;
+    for (int k = lane; k < 2 * per_half; k += 32) {
+      const int half = k >= per_half;
+      const int rem = k - half * per_half, a = rem / n, b = rem - a * n;
+      const double z = R.gz[a], w = R.sg_x[b];
+      double u, v, uv;
+      if (!half) { u = z + (1.0 - z) * w; v = (1.0 - z) * w; uv = z; }
+      else { u = (1.0 - z) * w; v = z + (1.0 - z) * w; uv = -z; }
+      const double wt = R.gwz[a] * R.sg_w[b] * (1.0 - z);
+      add_point<OP>(op, A, B, u, same ? v : 1.0 - v, uv * A.dx, uv * A.dy, wt, c);
+    }
+    return;
+  }
+  const int ma = match >> 1, mb = match & 1;
+  const double ax = ma == 0 ? A.dx : -A.dx, ay = ma == 0 ? A.dy : -A.dy;
+  const double bx = mb == 0 ? B.dx : -B.dx, by = mb == 0 ? B.dy : -B.dy;
+  for (int k = lane; k < 2 * per_half; k += 32) {
+    const int half = k >= per_half;
+    const int rem = k - half * per_half, a = rem / n, b = rem - a * n;
+    const double z = R.gz[a], w = R.sg_x[b];
+    double xi, eta;
+    if (!half) { xi = z; eta = z * w; }
+    else { xi = z * w; eta = z; }
+    const double wt = R.gwz[a] * R.sg_w[b] * z;
+    add_point<OP>(op, A, B, ma == 0 ? xi : 1.0 - xi, mb == 0 ? eta : 1.0 - eta, xi * ax - eta * bx,
+                  xi * ay - eta * by, wt, c);
+  }
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  return v;
+}
+
+// ----------------------------------------------------------------------------------------
+// Kernels
+// ----------------------------------------------------------------------------------------
+// counts[0]: list length, [1]: degenerate-pair flag, [2 + class]: non-far pairs of owned columns.
+__global__ void __launch_bounds__(256) k_curve_classify(const SegGeo* __restrict__ gT, const SegGeo* __restrict__ gB,
+                                                        const int* __restrict__ T, int nT, const int* __restrict__ S,
+                                                        int nS, const unsigned char* __restrict__ own, double k2,
+                                                        int LS, Special* __restrict__ list, int cap,
+                                                        int* __restrict__ counts) {
+  const int tl = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tl >= nT) return;
+  const SegGeo A = gT[T[tl]];
+  for (int sl = blockIdx.y; sl < nS; sl += gridDim.y) {
+    const SegGeo B = gB[S[sl]];
+    int match;
+    const int cls = classify(A, B, k2, &match);
+    if (cls == 0) continue;
+    if (cls < 0) {
+      atomicOr(&counts[1], 1);
+      continue;
+    }
+    const int idx = atomicAdd(&counts[0], 1);
+    if (idx < cap) {
+      Special sp;
+      sp.slot = ((int64_t)sl * nT + tl) * LS;
+      sp.tau = T[tl];
+      sp.sigma = S[sl];
+      sp.cls = cls;
+      sp.match = match;
+      list[idx] = sp;
+    }
+    if (own[sl]) atomicAdd(&counts[2 + cls], 1);
+  }
+}
+
+template <int OP>
+__global__ void __launch_bounds__(128) k_curve_far(Op op, const Rules* __restrict__ rules, const SegGeo* __restrict__ gT,
+                                                   const SegGeo* __restrict__ gB, const int* __restrict__ T, int nT,
+                                                   const int* __restrict__ S, int nS, double2* __restrict__ L) {
+  __shared__ double fx[kMaxGL], fw[kMaxGL], bx[kMaxGL], bw[kMaxGL];
+  const int nft = rules->nft, nfb = rules->nfb;
+  for (int i = threadIdx.x; i < kMaxGL; i += blockDim.x) {
+    fx[i] = rules->ft_x[i];
+    fw[i] = rules->ft_w[i];
+    bx[i] = rules->fb_x[i];
+    bw[i] = rules->fb_w[i];
+  }
+  __syncthreads();
+  const int tl = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tl >= nT) return;
+  const SegGeo A = gT[T[tl]];
+  for (int sl = blockIdx.y; sl < nS; sl += gridDim.y) {
+    const SegGeo B = gB[S[sl]];
+    int match;
+    if (classify(A, B, op.k2, &match) != 0) continue;
+    Acc c;
+    acc_zero(c);
+    far_pair<OP>(op, fx, fw, nft, bx, bw, nfb, A, B, c);
+    finalize<OP>(op, A, B, c, L + ((int64_t)sl * nT + tl) * op.LS);
+  }
+}
+
+template <int OP>
+__global__ void __launch_bounds__(256) k_curve_special(Op op, const Rules* __restrict__ rules,
+                                                       const SegGeo* __restrict__ gT, const SegGeo* __restrict__ gB,
+                                                       const Special* __restrict__ list, int n,
+                                                       double2* __restrict__ L) {
+  __shared__ Rules sR;
+  {
+    const int* src = (const int*)rules;
+    int* dst = (int*)&sR;
+    for (int i = threadIdx.x; i < (int)(sizeof(Rules) / sizeof(int)); i += blockDim.x) dst[i] = src[i];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int nwarps = gridDim.x * (blockDim.x >> 5);
+  for (int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < n; e += nwarps) {
+    const Special sp = list[e];
+    const SegGeo A = gT[sp.tau], B = gB[sp.sigma];
+    Acc c;
+    acc_zero(c);
+    if (sp.cls == 4) near_rule_warp<OP>(op, sR, A, B, lane, c);
+    else singular_rule_warp<OP>(op, sR, A, B, sp.cls, sp.match, lane, c);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      c.pr[k] = warp_sum(c.pr[k]);
+      c.pi[k] = warp_sum(c.pi[k]);
+    }
+    c.mr = warp_sum(c.mr);
+    c.mi = warp_sum(c.mi);
+    if (lane == 0) finalize<OP>(op, A, B, c, L + sp.slot);
+  }
+}
+
+// Explicit pairs (bgb_local_matrices_curve): far pairs by the far-kernel code, the others listed
+// for k_curve_special.  err[0]: list length, err[1]: invalid pair / rule.
+template <int OP>
+__global__ void __launch_bounds__(128) k_curve_pairs(Op op, const Rules* __restrict__ rules, const SegGeo* __restrict__ gT,
+                                                     const SegGeo* __restrict__ gB, const int2* __restrict__ pairs,
+                                                     int64_t npairs, int force, double2* __restrict__ L,
+                                                     signed char* __restrict__ cls_out, Special* __restrict__ list,
+                                                     int* __restrict__ err) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npairs) return;
+  const SegGeo A = gT[pairs[p].x], B = gB[pairs[p].y];
+  int match;
+  const int cls = classify(A, B, op.k2, &match);
+  cls_out[p] = (signed char)cls;
+  const int rule = force >= 0 ? force : cls;
+  if (cls < 0 || ((rule == 1 || rule == 3) && rule != cls)) {
+    atomicOr(&err[1], 1);
+    return;
+  }
+  if (rule == 0) {
+    Acc c;
+    acc_zero(c);
+    far_pair<OP>(op, rules->ft_x, rules->ft_w, rules->nft, rules->fb_x, rules->fb_w, rules->nfb, A, B, c);
+    finalize<OP>(op, A, B, c, L + p * 4);
+    return;
+  }
+  const int idx = atomicAdd(&err[0], 1);
+  Special sp;
+  sp.slot = p * 4;
+  sp.tau = pairs[p].x;
+  sp.sigma = pairs[p].y;
+  sp.cls = rule;
+  sp.match = match;
+  list[idx] = sp;
+}
+
+// Z[m, n] = sum over supports (test outer, trial inner, both by segment) of c_m c_n L.
+template <typename OutT>
+__global__ void __launch_bounds__(256) k_curve_gather(const double2* __restrict__ L, int nT, int LS, int nsB,
+                                                      int nrows, int ncols, const int64_t* __restrict__ toff,
+                                                      const int* __restrict__ tcode, const double* __restrict__ tcoef,
+                                                      const int64_t* __restrict__ boff, const int* __restrict__ bcode,
+                                                      const double* __restrict__ bcoef, OutT* __restrict__ out,
+                                                      int64_t ld) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= nrows) return;
+  const int64_t a0 = toff[m], a1 = toff[m + 1];
+  for (int n = blockIdx.y; n < ncols; n += gridDim.y) {
+    double zr = 0.0, zi = 0.0;
+    const int64_t b0 = boff[n], b1 = boff[n + 1];
+    for (int64_t a = a0; a < a1; ++a) {
+      const int ta = tcode[a];
+      const double ca = tcoef[a];
+      for (int64_t b = b0; b < b1; ++b) {
+        const int tb = bcode[b];
+        const double2 v = L[((int64_t)(tb >> 1) * nT + (ta >> 1)) * LS + (ta & 1) * nsB + (tb & 1)];
+        const double cb = bcoef[b];
+        zr += (v.x * ca) * cb;
+        zi += (v.y * ca) * cb;
+      }
+    }
+    OutT o;
+    o.x = zr;
+    o.y = zi;
+    out[m + (int64_t)n * ld] = o;
+  }
+}
+
+// ----------------------------------------------------------------------------------------
+// Host side
+// ----------------------------------------------------------------------------------------
+static int validate_curve(const bgb_curve_space* s, const char* name) {
+  if (!s) { set_error("%s curve space is NULL", name); return BGB_ERR_INVALID; }
+  if (s->refspace != BGB_REFSPACE2D_LAGRANGE_C0D1 && s->refspace != BGB_REFSPACE2D_LAGRANGE_CXD0) {
+    set_error("%s curve space: unknown refspace %d", name, s->refspace);
+    return BGB_ERR_INVALID;
+  }
+  if (s->nv < 0 || s->ns < 0 || s->nfun < 0) { set_error("%s curve space: negative sizes", name); return BGB_ERR_INVALID; }
+  if (s->ns > 0 && (!s->vertices || !s->segments || !s->fn_index || !s->fn_coef)) {
+    set_error("%s curve space: NULL table", name);
+    return BGB_ERR_INVALID;
+  }
+  for (int64_t i = 0; i < 2 * (int64_t)s->nv; ++i)
+    if (!std::isfinite(s->vertices[i])) { set_error("%s curve space: non-finite vertex coordinate at %lld", name, (long long)i); return BGB_ERR_INVALID; }
+  const int nsh = s->refspace == BGB_REFSPACE2D_LAGRANGE_CXD0 ? 1 : 2;
+  for (int64_t e = 0; e < s->ns; ++e) {
+    const int a = s->segments[2 * e], b = s->segments[2 * e + 1];
+    if (a < 0 || a >= s->nv || b < 0 || b >= s->nv) { set_error("%s curve space: segment %lld has a vertex index out of range", name, (long long)e); return BGB_ERR_INVALID; }
+    const double dx = s->vertices[2 * b] - s->vertices[2 * a], dy = s->vertices[2 * b + 1] - s->vertices[2 * a + 1];
+    if (a == b || !(dx * dx + dy * dy > 0.0)) { set_error("%s curve space: segment %lld is degenerate", name, (long long)e); return BGB_ERR_INVALID; }
+    for (int i = 0; i < nsh; ++i) {
+      const int f = s->fn_index[2 * e + i];
+      if (f < -1 || f >= s->nfun) { set_error("%s curve space: segment %lld local %d has function index %d out of range", name, (long long)e, i, f); return BGB_ERR_INVALID; }
+      if (f >= 0 && !std::isfinite(s->fn_coef[2 * e + i])) { set_error("%s curve space: non-finite coefficient", name); return BGB_ERR_INVALID; }
+    }
+    if (nsh == 2 && s->fn_index[2 * e] >= 0 && s->fn_index[2 * e] == s->fn_index[2 * e + 1]) {
+      set_error("%s curve space: segment %lld maps both local shapes to one function", name, (long long)e);
+      return BGB_ERR_INVALID;
+    }
+  }
+  return 0;
+}
+
+static int make_op(const bgb_operator2d* op, const bgb_curve_space* a, const bgb_curve_space* b, Op* out) {
+  if (!op) { set_error("operator is NULL"); return BGB_ERR_INVALID; }
+  if (op->kind < BGB_OP2D_SL || op->kind > BGB_OP2D_HS) { set_error("unknown 2-D operator kind %d", op->kind); return BGB_ERR_INVALID; }
+  if (!std::isfinite(op->wavenumber) || op->wavenumber < 0.0) { set_error("wave number must be finite and >= 0"); return BGB_ERR_INVALID; }
+  for (int c = 0; c < 2; ++c)
+    if (!std::isfinite(op->alpha[c]) || !std::isfinite(op->beta[c])) { set_error("operator has non-finite parameters"); return BGB_ERR_INVALID; }
+  Op o{};
+  o.kind = op->kind;
+  o.nsA = a->refspace == BGB_REFSPACE2D_LAGRANGE_CXD0 ? 1 : 2;
+  o.nsB = b->refspace == BGB_REFSPACE2D_LAGRANGE_CXD0 ? 1 : 2;
+  o.LS = o.nsA * o.nsB;
+  o.k = op->wavenumber;
+  o.k2 = op->wavenumber * op->wavenumber;
+  o.ar = op->alpha[0];
+  o.ai = op->alpha[1];
+  o.br = op->beta[0];
+  o.bi = op->beta[1];
+  *out = o;
+  return 0;
+}
+
+static int make_rules(const bgb_quadstrat2d* qs, Rules* R) {
+  if (!qs) { set_error("quadstrat is NULL"); return BGB_ERR_INVALID; }
+  if (qs->far_test < 1 || qs->far_test > kMaxGL || qs->far_trial < 1 || qs->far_trial > kMaxGL || qs->near < 1 ||
+      qs->near > kMaxGL || qs->singular < 1 || qs->singular > kMaxSing) {
+    set_error("curve quadstrat: Gauss points must be 1..%d and the singular order 1..%d (got %d %d %d %d)", kMaxGL,
+              kMaxSing, qs->far_test, qs->far_trial, qs->near, qs->singular);
+    return BGB_ERR_INVALID;
+  }
+  std::memset(R, 0, sizeof(Rules));
+  R->nft = qs->far_test;
+  R->nfb = qs->far_trial;
+  R->nnear = qs->near;
+  R->nsing = qs->singular;
+  gauss_legendre01(R->nft, R->ft_x, R->ft_w);
+  gauss_legendre01(R->nfb, R->fb_x, R->fb_w);
+  gauss_legendre01(R->nnear, R->nr_x, R->nr_w);
+  const int n = R->nsing;
+  gauss_legendre01(n, R->sg_x, R->sg_w);
+  // graded rule: [0, q^(3n)] then [q^(lev+1), q^lev] for lev = 3n - 1 .. 0, n Gauss points each
+  const double q = 0.35;
+  int k = 0;
+  for (int lev = 3 * n; lev >= 0; --lev) {
+    const double a = lev == 3 * n ? 0.0 : std::pow(q, lev + 1), b = std::pow(q, lev);
+    for (int i = 0; i < n; ++i) {
+      R->gz[k] = a + (b - a) * R->sg_x[i];
+      R->gwz[k] = (b - a) * R->sg_w[i];
+      ++k;
+    }
+  }
+  R->ngraded = k;
+  return 0;
+}
+
+static int upload_curve(cudaStream_t st, const bgb_curve_space* s, DevBuf& verts, DevBuf& segs, DevBuf& geo) {
+  int rc;
+  if ((rc = verts.ensure(sizeof(double) * 2 * (size_t)std::max(1, s->nv))) ||
+      (rc = segs.ensure(sizeof(int) * 2 * (size_t)std::max(1, s->ns))) ||
+      (rc = geo.ensure(sizeof(SegGeo) * (size_t)std::max(1, s->ns))))
+    return rc;
+  if (s->nv) BGB_CUDA(cudaMemcpyAsync(verts.p, s->vertices, sizeof(double) * 2 * (size_t)s->nv, cudaMemcpyHostToDevice, st));
+  if (s->ns) {
+    BGB_CUDA(cudaMemcpyAsync(segs.p, s->segments, sizeof(int) * 2 * (size_t)s->ns, cudaMemcpyHostToDevice, st));
+    k_curve_geo<<<(s->ns + 255) / 256, 256, 0, st>>>(verts.as<double>(), segs.as<int>(), s->ns, geo.as<SegGeo>());
+    BGB_CUDA(cudaGetLastError());
+  }
+  return 0;
+}
+
+template <class T>
+static int put(cudaStream_t st, DevBuf& buf, const std::vector<T>& v) {
+  int rc;
+  if ((rc = buf.ensure(sizeof(T) * std::max<size_t>(1, v.size())))) return rc;
+  if (!v.empty()) BGB_CUDA(cudaMemcpyAsync(buf.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, st));
+  return 0;
+}
+
+template <int OP>
+static void launch_far(const Op& op, const Rules* rules, const SegGeo* gT, const SegGeo* gB, const int* T, int nT,
+                       const int* S, int nS, double2* L, cudaStream_t st) {
+  dim3 grid((nT + 127) / 128, std::min(nS, 65535));
+  k_curve_far<OP><<<grid, 128, 0, st>>>(op, rules, gT, gB, T, nT, S, nS, L);
+}
+
+template <int OP>
+static void launch_special(const Op& op, const Rules* rules, const SegGeo* gT, const SegGeo* gB, const Special* list,
+                           int n, double2* L, int num_sms, cudaStream_t st) {
+  if (n <= 0) return;
+  const int blocks = std::max(1, std::min((n + 7) / 8, num_sms * 8));
+  k_curve_special<OP><<<blocks, 256, 0, st>>>(op, rules, gT, gB, list, n, L);
+}
+
+template <int OP>
+static void launch_pairs(const Op& op, const Rules* rules, const SegGeo* gT, const SegGeo* gB, const int2* pairs,
+                         int64_t np, int force, double2* L, signed char* cls, Special* list, int* err, cudaStream_t st) {
+  k_curve_pairs<OP><<<(unsigned)((np + 127) / 128), 128, 0, st>>>(op, rules, gT, gB, pairs, np, force, L, cls, list, err);
+}
+
+#define BGB_CURVE_DISPATCH(kind, fn, ...)                              \
+  switch (kind) {                                                      \
+    case BGB_OP2D_SL: fn<BGB_OP2D_SL>(__VA_ARGS__); break;             \
+    case BGB_OP2D_DL: fn<BGB_OP2D_DL>(__VA_ARGS__); break;             \
+    case BGB_OP2D_DLT: fn<BGB_OP2D_DLT>(__VA_ARGS__); break;           \
+    default: fn<BGB_OP2D_HS>(__VA_ARGS__); break;                      \
+  }
+
+// Supports of functions [f0, f1) as (segment, local, coef), sorted by function then segment.
+struct CurveSupports {
+  std::vector<int64_t> off;
+  std::vector<int> seg, loc;
+  std::vector<double> coef;
+};
+
+static CurveSupports curve_supports(const bgb_curve_space* s, int64_t f0, int64_t f1) {
+  const int nsh = s->refspace == BGB_REFSPACE2D_LAGRANGE_CXD0 ? 1 : 2;
+  CurveSupports C;
+  C.off.assign((size_t)(f1 - f0) + 1, 0);
+  for (int64_t e = 0; e < s->ns; ++e)
+    for (int i = 0; i < nsh; ++i) {
+      const int f = s->fn_index[2 * e + i];
+      if (f >= f0 && f < f1) C.off[(size_t)(f - f0) + 1]++;
+    }
+  for (size_t k = 1; k < C.off.size(); ++k) C.off[k] += C.off[k - 1];
+  const size_t tot = (size_t)C.off.back();
+  C.seg.resize(tot);
+  C.loc.resize(tot);
+  C.coef.resize(tot);
+  std::vector<int64_t> fill(C.off.begin(), C.off.end() - 1);
+  for (int64_t e = 0; e < s->ns; ++e)  // ascending segments: each function's list comes out sorted
+    for (int i = 0; i < nsh; ++i) {
+      const int f = s->fn_index[2 * e + i];
+      if (f >= f0 && f < f1) {
+        const int64_t k = fill[(size_t)(f - f0)]++;
+        C.seg[(size_t)k] = (int)e;
+        C.loc[(size_t)k] = i;
+        C.coef[(size_t)k] = s->fn_coef[2 * e + i];
+      }
+    }
+  return C;
+}
+
+// Local segment indices: sorted distinct segments of the supports; code = 2 * local + shape.
+static void localise(const CurveSupports& C, std::vector<int>& segs, std::vector<int>& code, std::vector<int>& map_scratch) {
+  segs.assign(C.seg.begin(), C.seg.end());
+  std::sort(segs.begin(), segs.end());
+  segs.erase(std::unique(segs.begin(), segs.end()), segs.end());
+  for (size_t k = 0; k < segs.size(); ++k) map_scratch[(size_t)segs[k]] = (int)k;
+  code.resize(C.seg.size());
+  for (size_t k = 0; k < C.seg.size(); ++k) code[k] = 2 * map_scratch[(size_t)C.seg[k]] + C.loc[k];
+}
+
+}  // namespace curve
+}  // namespace bgb
+
+using namespace bgb;
+using namespace bgb::curve;
+
+extern "C" {
+
+int bgb_assemble_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_curve_space* test,
+                       const bgb_curve_space* trial, const bgb_quadstrat2d* qs, void* out, int32_t out_kind,
+                       int64_t ld, int64_t row0, int64_t nrows, void* stream, bgb_stats* stats) {
+  const auto t_start = std::chrono::steady_clock::now();
+  if (!h) { set_error("handle is NULL"); return BGB_ERR_INVALID; }
+  std::lock_guard<std::mutex> lk(h->mu);
+  int rc;
+  if ((rc = validate_curve(test, "test")) || (rc = validate_curve(trial, "trial"))) return rc;
+  Op o;
+  Rules R;
+  if ((rc = make_op(op, test, trial, &o)) || (rc = make_rules(qs, &R))) return rc;
+  if (out_kind < BGB_OUT_HOST_C64 || out_kind > BGB_OUT_DEVICE_C32) { set_error("bad out_kind %d", out_kind); return BGB_ERR_INVALID; }
+  if (nrows < 0) nrows = (int64_t)test->nfun - row0;
+  if (row0 < 0 || row0 + nrows > test->nfun) { set_error("row window [%lld, %lld) outside [0, %d)", (long long)row0, (long long)(row0 + nrows), test->nfun); return BGB_ERR_INVALID; }
+  if (ld < std::max<int64_t>(1, nrows)) { set_error("ld %lld < nrows %lld", (long long)ld, (long long)nrows); return BGB_ERR_INVALID; }
+  if (!out && nrows > 0 && trial->nfun > 0) { set_error("out is NULL"); return BGB_ERR_INVALID; }
+  *h->abort_host = 0;
+  bgb_stats st{};
+  if (nrows == 0 || trial->nfun == 0) {
+    if (stats) *stats = st;
+    return 0;
+  }
+  cudaSetDevice(h->device);
+  cudaStream_t s = h->stream;
+  cudaStream_t user = stream ? (cudaStream_t)stream : h->stream;
+  const bool host_out = out_kind == BGB_OUT_HOST_C64 || out_kind == BGB_OUT_HOST_C32;
+  const bool c64 = out_kind == BGB_OUT_HOST_C64 || out_kind == BGB_OUT_DEVICE_C64;
+  const size_t esz = c64 ? 16 : 8;
+  if (!host_out && user != s) {
+    BGB_CUDA(cudaEventRecord(h->ev[7], user));
+    BGB_CUDA(cudaStreamWaitEvent(s, h->ev[7], 0));
+  }
+  CurveBufs& B = h->curve;
+  if ((rc = upload_curve(s, test, B.verts_t, B.segs_t, B.geo_t)) || (rc = upload_curve(s, trial, B.verts_b, B.segs_b, B.geo_b)))
+    return rc;
+  if ((rc = B.rules.ensure(sizeof(Rules)))) return rc;
+  BGB_CUDA(cudaMemcpyAsync(B.rules.p, &R, sizeof(Rules), cudaMemcpyHostToDevice, s));
+  int launches = test->ns > 0 ? 1 : 0;
+  launches += trial->ns > 0 ? 1 : 0;
+
+  // test side: supports of the rows, local test segments
+  std::vector<int> scratch((size_t)std::max(test->ns, trial->ns) + 1, -1);
+  CurveSupports TS = curve_supports(test, row0, row0 + nrows);
+  std::vector<int> T, tcode;
+  localise(TS, T, tcode, scratch);
+  const int nT = (int)T.size();
+  if ((rc = put(s, B.T, T)) || (rc = put(s, B.tsup_off, TS.off)) || (rc = put(s, B.tsup_i, tcode)) ||
+      (rc = put(s, B.tsup_c, TS.coef)))
+    return rc;
+
+  // column blocks sized to the HBM budget: local matrices of nT x |S_b| pairs (|S_b| <= 2 per column)
+  size_t freeb = 0, totalb = 0;
+  cudaMemGetInfo(&freeb, &totalb);
+  const int64_t budget = h->cfg.hbm_budget_bytes > 0 ? h->cfg.hbm_budget_bytes : (int64_t)(0.9 * (double)freeb);
+  const int64_t ncols = trial->nfun;
+  const int64_t per_col = 2 * (int64_t)std::max(1, nT) * o.LS * 16 + (host_out ? nrows * (int64_t)esz : 0);
+  const int64_t cols_per_block = std::max<int64_t>(1, std::min<int64_t>(ncols, budget / 2 / std::max<int64_t>(1, per_col)));
+  std::vector<unsigned char> seen((size_t)trial->ns, 0);
+  int64_t computed = 0, nonfar[5] = {0, 0, 0, 0, 0};
+  double ms_cls = 0, ms_far = 0, ms_sp = 0, ms_copy = 0;
+  int nblocks = 0;
+  int cap = std::max(1 << 16, 8 * nT);
+  for (int64_t c0 = 0; c0 < ncols; c0 += cols_per_block) {
+    if (h->abort_host && *h->abort_host) { set_error("aborted by bgb_abort"); return BGB_ERR_ABORTED; }
+    const int64_t c1 = std::min(ncols, c0 + cols_per_block);
+    ++nblocks;
+    CurveSupports BS = curve_supports(trial, c0, c1);
+    std::vector<int> S, bcode;
+    localise(BS, S, bcode, scratch);
+    const int nS = (int)S.size();
+    std::vector<unsigned char> own((size_t)std::max(1, nS));
+    for (int k = 0; k < nS; ++k) {
+      own[(size_t)k] = !seen[(size_t)S[(size_t)k]];
+      seen[(size_t)S[(size_t)k]] = 1;
+    }
+    if ((rc = put(s, B.S, S)) || (rc = put(s, B.own, own)) || (rc = put(s, B.bsup_off, BS.off)) ||
+        (rc = put(s, B.bsup_i, bcode)) || (rc = put(s, B.bsup_c, BS.coef)))
+      return rc;
+    const int64_t npairs = (int64_t)nT * nS;
+    computed += npairs;
+    if ((rc = B.L.ensure(sizeof(double2) * (size_t)std::max<int64_t>(1, npairs * o.LS)))) return rc;
+    if ((rc = B.counts.ensure(sizeof(int) * 8))) return rc;
+    int counts[8] = {0};
+    if (nT > 0 && nS > 0) {
+      for (int attempt = 0; attempt < 2; ++attempt) {
+        if ((rc = B.list.ensure(sizeof(Special) * (size_t)cap))) return rc;
+        BGB_CUDA(cudaMemsetAsync(B.counts.p, 0, sizeof(int) * 8, s));
+        BGB_CUDA(cudaEventRecord(h->ev[0], s));
+        dim3 grid((nT + 255) / 256, std::min(nS, 65535));
+        k_curve_classify<<<grid, 256, 0, s>>>(B.geo_t.as<SegGeo>(), B.geo_b.as<SegGeo>(), B.T.as<int>(), nT, B.S.as<int>(),
+                                              nS, B.own.as<unsigned char>(), o.k2, o.LS, B.list.as<Special>(), cap,
+                                              B.counts.as<int>());
+        BGB_CUDA(cudaGetLastError());
+        BGB_CUDA(cudaEventRecord(h->ev[1], s));
+        BGB_CUDA(cudaMemcpyAsync(counts, B.counts.p, sizeof(int) * 8, cudaMemcpyDeviceToHost, s));
+        BGB_CUDA(cudaStreamSynchronize(s));
+        ms_cls += event_ms(h->ev[0], h->ev[1]);
+        ++launches;
+        if (counts[1]) { set_error("degenerate geometry: a segment pair shares more than two vertices"); return BGB_ERR_INVALID; }
+        if (counts[0] <= cap) break;
+        cap = counts[0];
+      }
+      for (int c = 1; c < 5; ++c) nonfar[c] += counts[2 + c];
+      BGB_CUDA(cudaEventRecord(h->ev[2], s));
+      BGB_CURVE_DISPATCH(o.kind, launch_far, o, B.rules.as<Rules>(), B.geo_t.as<SegGeo>(), B.geo_b.as<SegGeo>(),
+                         B.T.as<int>(), nT, B.S.as<int>(), nS, B.L.as<double2>(), s);
+      BGB_CUDA(cudaGetLastError());
+      BGB_CUDA(cudaEventRecord(h->ev[3], s));
+      BGB_CURVE_DISPATCH(o.kind, launch_special, o, B.rules.as<Rules>(), B.geo_t.as<SegGeo>(), B.geo_b.as<SegGeo>(),
+                         B.list.as<Special>(), counts[0], B.L.as<double2>(), h->num_sms, s);
+      BGB_CUDA(cudaGetLastError());
+      BGB_CUDA(cudaEventRecord(h->ev[4], s));
+      launches += 1 + (counts[0] > 0);
+    } else {
+      BGB_CUDA(cudaEventRecord(h->ev[2], s));
+      BGB_CUDA(cudaEventRecord(h->ev[3], s));
+      BGB_CUDA(cudaEventRecord(h->ev[4], s));
+    }
+    // gather into the output (device) or the staging buffer (host)
+    const int64_t bc = c1 - c0;
+    void* dst;
+    int64_t dld;
+    if (host_out) {
+      if ((rc = B.stage.ensure(esz * (size_t)nrows * (size_t)bc))) return rc;
+      dst = B.stage.p;
+      dld = nrows;
+    } else {
+      dst = (char*)out + esz * (size_t)c0 * (size_t)ld;
+      dld = ld;
+    }
+    dim3 gg((unsigned)((nrows + 255) / 256), (unsigned)std::min<int64_t>(bc, 65535));
+    if (c64)
+      k_curve_gather<double2><<<gg, 256, 0, s>>>(B.L.as<double2>(), nT, o.LS, o.nsB, (int)nrows, (int)bc, B.tsup_off.as<int64_t>(),
+                                                 B.tsup_i.as<int>(), B.tsup_c.as<double>(), B.bsup_off.as<int64_t>(),
+                                                 B.bsup_i.as<int>(), B.bsup_c.as<double>(), (double2*)dst, dld);
+    else
+      k_curve_gather<float2><<<gg, 256, 0, s>>>(B.L.as<double2>(), nT, o.LS, o.nsB, (int)nrows, (int)bc, B.tsup_off.as<int64_t>(),
+                                                B.tsup_i.as<int>(), B.tsup_c.as<double>(), B.bsup_off.as<int64_t>(),
+                                                B.bsup_i.as<int>(), B.bsup_c.as<double>(), (float2*)dst, dld);
+    BGB_CUDA(cudaGetLastError());
+    ++launches;
+    BGB_CUDA(cudaEventRecord(h->ev[5], s));
+    if (host_out) {
+      BGB_CUDA(cudaMemcpy2DAsync((char*)out + esz * (size_t)c0 * (size_t)ld, esz * (size_t)ld, B.stage.p,
+                                 esz * (size_t)nrows, esz * (size_t)nrows, (size_t)bc, cudaMemcpyDeviceToHost, s));
+    }
+    BGB_CUDA(cudaEventRecord(h->ev[6], s));
+    BGB_CUDA(cudaStreamSynchronize(s));
+    ms_far += event_ms(h->ev[2], h->ev[3]) + event_ms(h->ev[4], h->ev[5]);
+    ms_sp += event_ms(h->ev[3], h->ev[4]);
+    ms_copy += event_ms(h->ev[5], h->ev[6]);
+  }
+  if (!host_out && user != s) {
+    BGB_CUDA(cudaEventRecord(h->ev[7], s));
+    BGB_CUDA(cudaStreamWaitEvent(user, h->ev[7], 0));
+  }
+  st.pairs_total = (int64_t)nT * trial->ns;
+  int64_t nf = 0;
+  for (int c = 1; c < 5; ++c) {
+    st.pairs_class[c] = nonfar[c];
+    nf += nonfar[c];
+  }
+  st.pairs_class[0] = st.pairs_total - nf;
+  st.pairs_computed = computed;
+  st.ms_classify = ms_cls;
+  st.ms_far = ms_far;
+  st.ms_singular = ms_sp;
+  st.ms_copy = ms_copy;
+  st.out_blocks = nblocks;
+  st.tile_config = -1;
+  st.kernel_launches = launches;
+  st.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+  st.ms_pipeline = st.ms_total;
+  if (stats) *stats = st;
+  return 0;
+}
+
+int bgb_local_matrices_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_curve_space* test,
+                             const bgb_curve_space* trial, const bgb_quadstrat2d* qs, int64_t npairs,
+                             const int32_t* tau, const int32_t* sigma, int32_t force_class, double* out,
+                             int8_t* cls_out) {
+  if (!h) { set_error("handle is NULL"); return BGB_ERR_INVALID; }
+  std::lock_guard<std::mutex> lk(h->mu);
+  int rc;
+  if ((rc = validate_curve(test, "test")) || (rc = validate_curve(trial, "trial"))) return rc;
+  Op o;
+  Rules R;
+  if ((rc = make_op(op, test, trial, &o)) || (rc = make_rules(qs, &R))) return rc;
+  if (npairs < 0 || (npairs > 0 && (!tau || !sigma || !out))) { set_error("invalid pair list"); return BGB_ERR_INVALID; }
+  if (force_class != -1 && force_class != 0 && force_class != 1 && force_class != 3 && force_class != 4) {
+    set_error("force_class %d is not a curve pair class", force_class);
+    return BGB_ERR_INVALID;
+  }
+  if (npairs > (int64_t)1 << 28) { set_error("at most 2^28 pairs per call"); return BGB_ERR_INVALID; }
+  std::vector<int2> pairs((size_t)npairs);
+  for (int64_t p = 0; p < npairs; ++p) {
+    if (tau[p] < 0 || tau[p] >= test->ns || sigma[p] < 0 || sigma[p] >= trial->ns) {
+      set_error("pair %lld: segment index out of range", (long long)p);
+      return BGB_ERR_INVALID;
+    }
+    pairs[(size_t)p] = make_int2(tau[p], sigma[p]);
+  }
+  if (npairs == 0) return 0;
+  cudaSetDevice(h->device);
+  cudaStream_t s = h->stream;
+  CurveBufs& B = h->curve;
+  if ((rc = upload_curve(s, test, B.verts_t, B.segs_t, B.geo_t)) || (rc = upload_curve(s, trial, B.verts_b, B.segs_b, B.geo_b)))
+    return rc;
+  if ((rc = B.rules.ensure(sizeof(Rules)))) return rc;
+  BGB_CUDA(cudaMemcpyAsync(B.rules.p, &R, sizeof(Rules), cudaMemcpyHostToDevice, s));
+  if ((rc = put(s, B.pairs, pairs)) || (rc = B.out.ensure(sizeof(double2) * 4 * (size_t)npairs)) ||
+      (rc = B.own.ensure((size_t)npairs)) || (rc = B.list.ensure(sizeof(Special) * (size_t)npairs)) ||
+      (rc = B.counts.ensure(sizeof(int) * 8)))
+    return rc;
+  BGB_CUDA(cudaMemsetAsync(B.out.p, 0, sizeof(double2) * 4 * (size_t)npairs, s));
+  BGB_CUDA(cudaMemsetAsync(B.counts.p, 0, sizeof(int) * 8, s));
+  BGB_CURVE_DISPATCH(o.kind, launch_pairs, o, B.rules.as<Rules>(), B.geo_t.as<SegGeo>(), B.geo_b.as<SegGeo>(),
+                     B.pairs.as<int2>(), npairs, force_class, B.out.as<double2>(), (signed char*)B.own.p,
+                     B.list.as<Special>(), B.counts.as<int>(), s);
+  BGB_CUDA(cudaGetLastError());
+  int counts[8] = {0};
+  BGB_CUDA(cudaMemcpyAsync(counts, B.counts.p, sizeof(int) * 8, cudaMemcpyDeviceToHost, s));
+  BGB_CUDA(cudaStreamSynchronize(s));
+  if (counts[1]) {
+    set_error("a pair is degenerate or its forced rule does not match its class");
+    return BGB_ERR_INVALID;
+  }
+  BGB_CURVE_DISPATCH(o.kind, launch_special, o, B.rules.as<Rules>(), B.geo_t.as<SegGeo>(), B.geo_b.as<SegGeo>(),
+                     B.list.as<Special>(), counts[0], B.out.as<double2>(), h->num_sms, s);
+  BGB_CUDA(cudaGetLastError());
+  std::vector<double2> L((size_t)npairs * 4);
+  std::vector<signed char> cls((size_t)npairs);
+  BGB_CUDA(cudaMemcpyAsync(L.data(), B.out.p, sizeof(double2) * L.size(), cudaMemcpyDeviceToHost, s));
+  BGB_CUDA(cudaMemcpyAsync(cls.data(), B.own.p, (size_t)npairs, cudaMemcpyDeviceToHost, s));
+  BGB_CUDA(cudaStreamSynchronize(s));
+  for (int64_t p = 0; p < npairs; ++p) {
+    for (int i = 0; i < 2; ++i)
+      for (int j = 0; j < 2; ++j) {
+        double2 v = make_double2(0.0, 0.0);
+        if (i < o.nsA && j < o.nsB) v = L[(size_t)p * 4 + i * o.nsB + j];
+        out[p * 8 + (i * 2 + j) * 2] = v.x;
+        out[p * 8 + (i * 2 + j) * 2 + 1] = v.y;
+      }
+    if (cls_out) cls_out[p] = cls[(size_t)p];
+  }
+  return 0;
+}
+
+}  // extern "C"

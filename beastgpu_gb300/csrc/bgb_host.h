@@ -37,6 +37,17 @@ struct DevBuf {
   T* as() const { return (T*)p; }
 };
 
+// Scratch of the curve (2-D) path.
+struct CurveBufs {
+  DevBuf verts_t, segs_t, geo_t, verts_b, segs_b, geo_b, rules, L, list, counts, tsup_i, tsup_c, tsup_off, bsup_i,
+      bsup_c, bsup_off, T, S, own, pairs, out, stage;
+  void release() {
+    DevBuf* all[] = {&verts_t, &segs_t, &geo_t, &verts_b, &segs_b, &geo_b, &rules, &L, &list, &counts, &tsup_i,
+                     &tsup_c, &tsup_off, &bsup_i, &bsup_c, &bsup_off, &T, &S, &own, &pairs, &out, &stage};
+    for (DevBuf* b : all) b->release();
+  }
+};
+
 }  // namespace bgb
 
 struct bgb_handle {
@@ -58,6 +69,7 @@ struct bgb_handle {
   bgb::DevBuf tplan_i, tplan_l, tplan_d, tplan_f;  // test-side tile tables (shared by all output blocks)
   bgb::DevBuf stage[kSlots];
   bgb::DevBuf diag_a, diag_b, diag_c, diag_d;
+  bgb::CurveBufs curve;
   cudaEvent_t ev[8] = {};
   cudaEvent_t ev2[4 * kSlots] = {};  // per output-block slot: far start / end, copy start / end
   cudaEvent_t ring_ev[2] = {};
@@ -122,5 +134,7 @@ double max_edge(const bgb_space* s);
 // wave number and k R below the range of the df sin / cos.
 bool df_singular_ok(const OpParams& op, double edge_t, double edge_b);
 double event_ms(cudaEvent_t a, cudaEvent_t b);
+// Gauss-Legendre rule on [0, 1], nodes ascending (n <= 64).
+void gauss_legendre01(int n, double* x, double* w);
 
 }  // namespace bgb

@@ -18,6 +18,7 @@ from __future__ import annotations
 
 import numpy as np
 
+from .curves import CurveMesh, curve_lagrangec0d1, curve_lagrangecxd0
 from .meshes import Mesh
 
 REFSPACE_LAGRANGE_C0D1 = 0
@@ -117,12 +118,14 @@ def boundary_vertices(mesh: Mesh) -> np.ndarray:
     return bnd
 
 
-def lagrangec0d1(mesh: Mesh, dirichlet: bool = True) -> Space:
+def lagrangec0d1(mesh, dirichlet: bool = True):
     """Continuous piecewise-linear Lagrange space: one function per vertex.
 
     With dirichlet=True (BEAST's default) vertices on the mesh boundary carry no function;
-    on closed surfaces every vertex does.
+    on closed surfaces every vertex does.  On a curve mesh this is the curve space of hats.
     """
+    if isinstance(mesh, CurveMesh):
+        return curve_lagrangec0d1(mesh, dirichlet)
     keep = np.ones(mesh.nv, dtype=bool)
     if dirichlet:
         keep &= ~boundary_vertices(mesh)
@@ -134,3 +137,10 @@ def lagrangec0d1(mesh: Mesh, dirichlet: bool = True) -> Space:
     fn_index = fnum[mesh.triangles].astype(np.int32)
     fn_coef = np.where(fn_index >= 0, 1.0, 0.0)
     return Space(mesh, REFSPACE_LAGRANGE_C0D1, fn_index, fn_coef, int(keep.sum()), "lagrangec0d1")
+
+
+def lagrangecxd0(mesh):
+    """Piecewise constants; implemented on curve meshes (one function per segment)."""
+    if isinstance(mesh, CurveMesh):
+        return curve_lagrangecxd0(mesh)
+    raise NotImplementedError("piecewise-constant spaces are implemented on curve meshes only")

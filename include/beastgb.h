@@ -24,7 +24,7 @@
 extern "C" {
 #endif
 
-#define BGB_ABI_VERSION 2
+#define BGB_ABI_VERSION 3
 
 /* bgb_config.flags: copy pageable host outputs through the pinned ring even when the device
  * reaches pageable memory through the host page tables (by default such outputs are written
@@ -221,6 +221,71 @@ int bgb_classify_csr_noalloc(const double* d_vertices_test, const int32_t* d_tri
                              double k2, int64_t* d_offsets, int32_t* d_tau, int32_t* d_sigma,
                              int8_t* d_class, int64_t capacity, int64_t* total, void* stream);
 
+/* ---- Curves: BEAST Helmholtz2D on polygonal curves ----------------------------------------
+ * The 2-D family of the reference's hypersingular prototype (old_code/doubleQuadRule_2d_gpu.jl:
+ * kernel at :72-78, integrand at :88-97, double quadrature at :129-210 and :265-465), widened to
+ * the four Helmholtz2D operators and to whole matrices.
+ * Kernel: G(R) = -(i/4) H0^(2)(kR) for k > 0, -(1/2 pi) ln R for k = 0; grad_x G = (x - y) g1(R).
+ * Cells are straight segments (v0, v1), chart x(s) = (1 - s) v0 + s v1 (s in [0, 1]), length l,
+ * normal n = (d_y, -d_x) / l with d = v1 - v0 (outward on a counter-clockwise closed curve). */
+typedef enum {
+  BGB_OP2D_SL = 0,  /* alpha int int G f g */
+  BGB_OP2D_DL = 1,  /* alpha int int f (n_y . grad_y G) g */
+  BGB_OP2D_DLT = 2, /* alpha int int f (n_x . grad_x G) g */
+  BGB_OP2D_HS = 3   /* int int G [alpha (n_x . n_y) f g + beta f' g'], f' the arc-length derivative
+                       (BEAST and the prototype: alpha = -k^2, beta = 1) */
+} bgb_op2d_kind;
+typedef struct {
+  int32_t kind;       /* bgb_op2d_kind */
+  double wavenumber;  /* real k >= 0 */
+  double alpha[2];
+  double beta[2];     /* hypersingular only */
+} bgb_operator2d;
+typedef enum {
+  BGB_REFSPACE2D_LAGRANGE_C0D1 = 0, /* hats 1 - s (vertex v0) and s (v1); derivatives -1/l, +1/l */
+  BGB_REFSPACE2D_LAGRANGE_CXD0 = 1  /* one constant per segment (column 1 of the tables unused) */
+} bgb_refspace2d;
+typedef struct {
+  int32_t refspace;          /* bgb_refspace2d */
+  int32_t nv, ns, nfun;
+  const double* vertices;    /* [nv][2] */
+  const int32_t* segments;   /* [ns][2], 0-based vertex indices (v0, v1) */
+  const int32_t* fn_index;   /* [ns][2], global function of local shape i, -1 if none */
+  const double* fn_coef;     /* [ns][2] */
+} bgb_curve_space;
+/* Rules of the curve path.  Pair classes: the predicate of bgb_classify_block over the two
+ * vertices of each segment, with the trial segment's length as its chart volume: 3 coincident
+ * (two shared vertices), 1 common vertex, 4 near, 0 far.
+ *   far pairs:   Gauss-Legendre far_test x far_trial points (1..32);
+ *   near pairs:  near x near Gauss-Legendre points (1..32) on the leaves of a bisection of the
+ *                chart square (the longer piece is halved until each piece pair is at least as
+ *                far apart as its longer piece is long, at most 16 times);
+ *   coincident / common vertex: order `singular` (1..16) graded rules after a split of the
+ *                chart square along its diagonal: (3n + 1) n graded points (n Gauss points on
+ *                3n + 1 intervals of ratio 0.35 towards the singularity) times n Gauss points.
+ * Double layers vanish on coincident segments. */
+typedef struct {
+  int32_t far_test, far_trial;
+  int32_t near;
+  int32_t singular;
+} bgb_quadstrat2d;
+/* Assemble rows [row0, row0 + nrows) of the curve operator's matrix in FP64 (the outputs may be
+ * complex float); arguments, output layout, streams and errors as bgb_assemble.  stats: pairs
+ * over all test segments of the rows and all trial segments, classes 0 far, 1 common vertex,
+ * 3 coincident, 4 near.
+ * Replaces: momintegrals_gpu_doubleQuad! of the 2-D prototype (doubleQuadRule_2d_gpu.jl:265-465),
+ * one segment pair per call there, all pairs and the assembly here. */
+int bgb_assemble_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_curve_space* test,
+                       const bgb_curve_space* trial, const bgb_quadstrat2d* qs, void* out, int32_t out_kind,
+                       int64_t ld, int64_t row0, int64_t nrows, void* stream, bgb_stats* stats);
+/* Local 2x2 complex matrices of a list of segment pairs (out: double[npairs][2][2][2], host;
+ * entries of absent shapes are zero) with the rule chosen by classification or forced
+ * (force_class 0 far or 4 near for any pair; 1 / 3 only for pairs of that class), computed by
+ * the kernels bgb_assemble_curve uses.  cls_out (optional): int8[npairs]. */
+int bgb_local_matrices_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_curve_space* test,
+                             const bgb_curve_space* trial, const bgb_quadstrat2d* qs, int64_t npairs,
+                             const int32_t* tau, const int32_t* sigma, int32_t force_class, double* out,
+                             int8_t* cls_out);
 /* Ask a running call on this handle to stop at its next check point (BGB_ERR_ABORTED). */
 int bgb_abort(bgb_handle* h);
 

@@ -31,7 +31,7 @@ def lib():
 def test_header_declares_the_expected_entry_points():
     names = declared_functions()
     for must in ("bgb_create", "bgb_destroy", "bgb_assemble", "bgb_assemble_batch", "bgb_classify_block",
-                 "bgb_local_matrices", "bgb_last_error"):
+                 "bgb_local_matrices", "bgb_last_error", "bgb_assemble_curve", "bgb_local_matrices_curve"):
         assert must in names
 
 
@@ -48,7 +48,7 @@ def test_no_undeclared_exports(lib):
 
 
 def test_abi_version(lib):
-    assert lib.bgb_abi_version() == _lib.ABI_VERSION == 2
+    assert lib.bgb_abi_version() == _lib.ABI_VERSION == 3
     n = lib.bgb_tile_info(None, 0)
     assert n >= 4
 
@@ -57,6 +57,8 @@ def test_invalid_handle_is_an_error_not_a_crash(lib):
     rc = lib.bgb_assemble(None, None, None, None, None, 0, None, 0, 1, 0, -1, None, None)
     assert rc == -1
     assert b"handle" in lib.bgb_last_error()
+    rc = lib.bgb_assemble_curve(None, None, None, None, None, None, 0, 1, 0, -1, None, None)
+    assert rc == -1
     assert lib.bgb_destroy(None) == 0
     assert lib.bgb_abort(None) == -1
 
