@@ -755,6 +755,7 @@ int bgb_assemble_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_curve_
         if (counts[0] <= cap) break;
         cap = counts[0];
       }
+      if (counts[0] > cap) { set_error("non-far pair list overflow"); return BGB_ERR_CAPACITY; }
       for (int c = 1; c < 5; ++c) nonfar[c] += counts[2 + c];
       BGB_CUDA(cudaEventRecord(h->ev[2], s));
       BGB_CURVE_DISPATCH(o.kind, launch_far, o, B.rules.as<Rules>(), B.geo_t.as<SegGeo>(), B.geo_b.as<SegGeo>(),
