@@ -227,11 +227,15 @@ def assemble_gpu(operator: Operator, test_functions: Space, trial_functions: Spa
 
 
 def _assemble_curve(operator, X, Y, config, quadstrat, out, dtype, rows, out_buffer, stream, return_stats):
-    """The curve (2-D) path: FP64 arithmetic; dtype complex128 (default) or complex64 output."""
+    """The curve (2-D) path: precision "fp64" (complex128 output by default) or "mixed" (FP32 far
+    pairs, complex64 output by default)."""
     if not isinstance(Y, CurveSpace) or not isinstance(operator, Operator2D):
         raise TypeError("curve spaces need a Helmholtz2D operator and a curve trial space")
     quadstrat = quadstrat or defaultquadstrat2d(operator, X, Y)
-    dtype = np.dtype(np.complex128 if dtype is None else dtype)
+    prec = _precision(config.precision)
+    if dtype is None:
+        dtype = np.complex128 if prec == _lib.PREC_FP64 else np.complex64
+    dtype = np.dtype(dtype)
     if dtype not in (np.complex128, np.complex64):
         raise ValueError("dtype must be complex128 or complex64")
     c64 = dtype == np.complex128
@@ -246,8 +250,8 @@ def _assemble_curve(operator, X, Y, config, quadstrat, out, dtype, rows, out_buf
         Z = np.empty((nrows, ncols), dtype=dtype, order="F") if out_buffer is None else out_buffer
         ptr = Z.data_ptr() if hasattr(Z, "data_ptr") else Z.ctypes.data
         kind = _lib.OUT_HOST_C64 if c64 else _lib.OUT_HOST_C32
-        _lib.check(lib.bgb_assemble_curve(h.ptr, C.byref(cop), C.byref(ct), C.byref(cb), C.byref(cq), C.c_void_p(ptr),
-                                          kind, max(1, nrows), row0, nrows, None, C.byref(stats)))
+        _lib.check(lib.bgb_assemble_curve(h.ptr, C.byref(cop), C.byref(ct), C.byref(cb), C.byref(cq), prec,
+                                          C.c_void_p(ptr), kind, max(1, nrows), row0, nrows, None, C.byref(stats)))
     elif out == "device":
         import torch
         tdt = torch.complex128 if c64 else torch.complex64
@@ -255,7 +259,7 @@ def _assemble_curve(operator, X, Y, config, quadstrat, out, dtype, rows, out_buf
             else out_buffer
         st = stream if stream is not None else torch.cuda.current_stream(config.device).cuda_stream
         kind = _lib.OUT_DEVICE_C64 if c64 else _lib.OUT_DEVICE_C32
-        _lib.check(lib.bgb_assemble_curve(h.ptr, C.byref(cop), C.byref(ct), C.byref(cb), C.byref(cq),
+        _lib.check(lib.bgb_assemble_curve(h.ptr, C.byref(cop), C.byref(ct), C.byref(cb), C.byref(cq), prec,
                                           C.c_void_p(Zt.data_ptr()), kind, max(1, nrows), row0, nrows, C.c_void_p(st),
                                           C.byref(stats)))
         Z = Zt.T
@@ -265,7 +269,8 @@ def _assemble_curve(operator, X, Y, config, quadstrat, out, dtype, rows, out_buf
 
 
 def local_matrices_curve(operator: Operator2D, test_functions: CurveSpace, trial_functions: CurveSpace, tau, sigma, *,
-                         quadstrat: QuadStrat2D = None, force_class: int = -1, device: int = 0):
+                         quadstrat: QuadStrat2D = None, precision: str = "fp64", force_class: int = -1,
+                         device: int = 0):
     """2x2 local matrices L[p, i, j] of explicit segment pairs and their classes (curve path)."""
     quadstrat = quadstrat or defaultquadstrat2d()
     tau = np.ascontiguousarray(tau, dtype=np.int32)
@@ -276,7 +281,8 @@ def local_matrices_curve(operator: Operator2D, test_functions: CurveSpace, trial
     cls = np.empty(tau.size, dtype=np.int8)
     _lib.check(_lib.load().bgb_local_matrices_curve(
         h.ptr, C.byref(c_operator2d(operator)), C.byref(c_curve_space(test_functions, keep)),
-        C.byref(c_curve_space(trial_functions, keep)), C.byref(c_quadstrat2d(quadstrat)), tau.size, tau.ctypes.data,
+        C.byref(c_curve_space(trial_functions, keep)), C.byref(c_quadstrat2d(quadstrat)), _precision(precision),
+        tau.size, tau.ctypes.data,
         sigma.ctypes.data, int(force_class), out.ctypes.data, cls.ctypes.data))
     return out[..., 0] + 1j * out[..., 1], cls
 

@@ -12,6 +12,8 @@
 // Hankel functions are CUDA's double-precision Bessel functions (the prototype's truncated series
 // at :31-64 hold only for small kR).
 #include "bgb_host.h"
+#include "besselfit.h"
+#include "bgb_df.cuh"
 
 #include <algorithm>
 #include <chrono>
@@ -27,6 +29,7 @@ struct SegGeo {
   double x0, y0, x1, y1;  // vertices v0, v1
   double dx, dy;          // v1 - v0
   double len, nx, ny;     // length and unit normal (dy, -dx) / len
+  double cx, cy;          // midpoint
 };
 
 constexpr int kMaxGL = 32;
@@ -47,7 +50,23 @@ struct Op {
   int kind, nsA, nsB, LS;  // LS = nsA * nsB entries per local matrix
   double k, k2;
   double ar, ai, br, bi;
+  float khi, klo;          // k as a double-float
+  float far_, fai, fbr, fbi;
 };
+
+// FP32 copy of a segment for the mixed kernels: midpoint as double-float, direction, normal, length.
+struct SegF {
+  float cxh, cxl, cyh, cyl;
+  float dx, dy, nx, ny;
+  float len, pad0, pad1, pad2;
+};
+
+template <class LT>
+__device__ __forceinline__ void store_l(LT* p, double re, double im);
+template <>
+__device__ __forceinline__ void store_l<double2>(double2* p, double re, double im) { *p = make_double2(re, im); }
+template <>
+__device__ __forceinline__ void store_l<float2>(float2* p, double re, double im) { *p = make_float2((float)re, (float)im); }
 
 // A non-far pair: its local matrix goes to L[slot .. slot + LS).
 struct Special {
@@ -64,7 +83,8 @@ struct Acc {
 // ----------------------------------------------------------------------------------------
 // Device functions
 // ----------------------------------------------------------------------------------------
-__global__ void k_curve_geo(const double* __restrict__ v, const int* __restrict__ seg, int ns, SegGeo* __restrict__ out) {
+__global__ void k_curve_geo(const double* __restrict__ v, const int* __restrict__ seg, int ns, SegGeo* __restrict__ out,
+                            SegF* __restrict__ outf) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= ns) return;
   const int a = seg[2 * e], b = seg[2 * e + 1];
@@ -78,7 +98,21 @@ __global__ void k_curve_geo(const double* __restrict__ v, const int* __restrict_
   g.len = __dsqrt_rn(__dadd_rn(__dmul_rn(g.dx, g.dx), __dmul_rn(g.dy, g.dy)));
   g.nx = __ddiv_rn(g.dy, g.len);
   g.ny = __ddiv_rn(-g.dx, g.len);
+  g.cx = __dadd_rn(g.x0, __dmul_rn(0.5, g.dx));
+  g.cy = __dadd_rn(g.y0, __dmul_rn(0.5, g.dy));
   out[e] = g;
+  SegF f;
+  f.cxh = (float)g.cx;
+  f.cxl = (float)(g.cx - (double)f.cxh);
+  f.cyh = (float)g.cy;
+  f.cyl = (float)(g.cy - (double)f.cyh);
+  f.dx = (float)g.dx;
+  f.dy = (float)g.dy;
+  f.nx = (float)g.nx;
+  f.ny = (float)g.ny;
+  f.len = (float)g.len;
+  f.pad0 = f.pad1 = f.pad2 = 0.f;
+  outf[e] = f;
 }
 
 // Pair class with BEAST's predicate over the segments' vertices (doubleQuadRuleMainCase.jl:187-200,
@@ -109,6 +143,24 @@ __device__ __forceinline__ int classify(const SegGeo& a, const SegGeo& b, double
   if (hits == 1) return 1;
   const double m = fmax(__dmul_rn(dmin2, k2), __ddiv_rn(dmin2, __dmul_rn(16.0, b.len)));
   return m >= xtol2 ? 0 : 4;
+}
+
+// True only for pairs the exact predicate classifies far: a lower bound of the least vertex
+// distance (midpoint distance minus the half lengths, less a bound of its FP32 rounding) already
+// passes the far thresholds with a margin of 0.25%.  Pairs it does not settle go to classify().
+__device__ __forceinline__ bool certainly_far(const SegGeo& A, const SegGeo& B, float k2f) {
+  const float dx = (float)(A.cx - B.cx), dy = (float)(A.cy - B.cy);
+  const float dc = sqrtf(fmaf(dx, dx, dy * dy));
+  const float hs = 0.5f * ((float)A.len + (float)B.len);
+  const float dlb = (dc - hs) - 4e-7f * (dc + hs);
+  if (!(dlb > 1e-12f)) return false;
+  const float d2 = dlb * dlb;
+  return d2 * k2f >= 0.0401f || d2 >= 0.0401f * 16.f * (float)B.len;
+}
+
+// Non-far mask: bit (sl * nT + tl) set for pairs the far kernels skip.
+__device__ __forceinline__ bool nonfar_bit(const unsigned* __restrict__ mask, int64_t idx) {
+  return (mask[idx >> 5] >> (idx & 31)) & 1u;
 }
 
 // One point pair: chart parameters s (test) and t (trial), separation r = x - y, rule weight w.
@@ -159,9 +211,9 @@ __device__ __forceinline__ void add_point(const Op& op, const SegGeo& A, const S
   }
 }
 
-template <int OP>
+template <int OP, class LT>
 __device__ __forceinline__ void finalize(const Op& op, const SegGeo& A, const SegGeo& B, const Acc& c,
-                                         double2* __restrict__ out) {
+                                         LT* __restrict__ out) {
   const double nn = A.nx * B.nx + A.ny * B.ny;
   const double dA[2] = {op.nsA == 2 ? -1.0 / A.len : 0.0, op.nsA == 2 ? 1.0 / A.len : 0.0};
   const double dB[2] = {op.nsB == 2 ? -1.0 / B.len : 0.0, op.nsB == 2 ? 1.0 / B.len : 0.0};
@@ -175,7 +227,7 @@ __device__ __forceinline__ void finalize(const Op& op, const SegGeo& A, const Se
         lr = lr * nn + bmr * d;
         li = li * nn + bmi * d;
       }
-      out[i * op.nsB + j] = make_double2(lr, li);
+      store_l(out + i * op.nsB + j, lr, li);
     }
 }
 
@@ -291,6 +343,203 @@ __device__ void singular_rule_warp(const Op& op, const Rules& R, const SegGeo& A
   }
 }
 
+// ---- Mixed precision: FP32 point pairs, the phase k R carried in FP64 per pair --------------
+// Polynomial approximations of H0^(2) and H1^(2) (besselfit.h: the forms of Abramowitz & Stegun
+// 9.4.1-9.4.6, coefficients fitted against scipy.special to 5e-9): x < 3 power series in
+// u = (x/3)^2 with the logarithmic part of Y explicit; x >= 3 modulus / phase in t = 3/x.
+__constant__ float c_P0[BGB_BESSEL_P0_N] = BGB_BESSEL_P0;
+__constant__ float c_Q0[BGB_BESSEL_Q0_N] = BGB_BESSEL_Q0;
+__constant__ float c_P1[BGB_BESSEL_P1_N] = BGB_BESSEL_P1;
+__constant__ float c_Q1[BGB_BESSEL_Q1_N] = BGB_BESSEL_Q1;
+__constant__ float c_F0[BGB_BESSEL_F0_N] = BGB_BESSEL_F0;
+__constant__ float c_G0[BGB_BESSEL_G0_N] = BGB_BESSEL_G0;
+__constant__ float c_F1[BGB_BESSEL_F1_N] = BGB_BESSEL_F1;
+__constant__ float c_G1[BGB_BESSEL_G1_N] = BGB_BESSEL_G1;
+
+template <int N>
+__device__ __forceinline__ float horner(const float (&c)[N], float u) {
+  float v = c[N - 1];
+#pragma unroll
+  for (int i = N - 2; i >= 0; --i) v = fmaf(v, u, c[i]);
+  return v;
+}
+
+constexpr float kTwoOverPiF = 0.636619772f, kInv2PiF = 0.159154943f, kTwoPiF = 6.28318531f;
+
+// sin / cos of an angle within a few multiples of pi, reduced to [-pi, pi] first.
+__device__ __forceinline__ void sincos_reduced(float th, float* s, float* c) {
+  th = fmaf(-kTwoPiF, rintf(th * kInv2PiF), th);
+  __sincosf(th, s, c);
+}
+
+// G = -(i/4) H0^(2)(x) with x = k R; phi equals x modulo 2 pi (carried in FP64 by the caller).
+__device__ __forceinline__ void hankel0_mixed(float x, float phi, float& Gr, float& Gi) {
+  if (x < 3.f) {
+    const float u = x * x * (1.f / 9.f);
+    const float j0 = horner(c_P0, u);
+    const float y0 = fmaf(kTwoOverPiF * __logf(0.5f * x), j0, horner(c_Q0, u));
+    Gr = -0.25f * y0;
+    Gi = -0.25f * j0;
+  } else {
+    const float t = __fdividef(3.f, x);
+    const float amp = horner(c_F0, t) * rsqrtf(x);
+    float sn, cs;
+    sincos_reduced(phi - 0.785398163f + horner(c_G0, t), &sn, &cs);
+    Gr = -0.25f * amp * sn;
+    Gi = -0.25f * amp * cs;
+  }
+}
+
+// g1 = (i k / 4) H1^(2)(x) / R = (k / 4R) (Y1 + i J1); phi as for hankel0_mixed.
+__device__ __forceinline__ void hankel1_mixed(float x, float phi, float k_over_4R, float& gr, float& gi) {
+  if (x < 3.f) {
+    const float u = x * x * (1.f / 9.f);
+    const float j1 = x * horner(c_P1, u);
+    const float y1 = __fdividef(fmaf(kTwoOverPiF * x * __logf(0.5f * x), j1, horner(c_Q1, u)), x);
+    gr = k_over_4R * y1;
+    gi = k_over_4R * j1;
+  } else {
+    const float t = __fdividef(3.f, x);
+    const float amp = horner(c_F1, t) * rsqrtf(x) * k_over_4R;
+    float sn, cs;
+    sincos_reduced(phi - 2.35619449f + horner(c_G1, t), &sn, &cs);
+    gr = amp * sn;
+    gi = amp * cs;
+  }
+}
+
+// Far pair in mixed precision.  Per pair in FP64: midpoint separation D, R0 = |D| and the phase
+// k R0 reduced modulo 2 pi.  Per point pair in FP32: w = (point offsets from the midpoints),
+// R = |D + w|, delta = R - R0 = (2 D.w + w.w) / (R + R0) without cancellation, x = k R and
+// phase phi0 + k delta.  The trial sums of each test point are formed first (moments S_j), then spread
+// over the test shapes.
+struct FAcc {
+  float pr[4], pi[4], mr, mi;
+};
+
+// k R0 modulo 2 pi for a double-float k R0 (Cody-Waite: 2 pi = P1 + P2 + P3, P1 = 6.28125 with 8
+// significant bits, so n P1 is exact for |n| < 2^16, i.e. k R0 < 4e5).
+__device__ __forceinline__ float reduce_2pi(dfl K) {
+  const float n = rintf(__fmul_rn(K.hi, 0.159154937f));
+  const float a = __fmaf_rn(-n, 6.28125f, K.hi);  // exact
+  const float q2 = __fmul_rn(n, 1.935307169e-03f);
+  const float q2e = __fmaf_rn(n, 1.935307169e-03f, -q2);
+  dfl t = df_add(dfl{a, K.lo}, dfl{-q2, -q2e});
+  return __fadd_rn(t.hi, __fsub_rn(t.lo, __fmul_rn(n, 1.025337627e-11f)));
+}
+
+// Far pair in mixed precision, all on the FP32 pipes.  Per pair in double-float: midpoint
+// separation D, R0 = |D| and the phase k R0 reduced modulo 2 pi.  Per point pair in FP32:
+// w = point offsets from the midpoints, R = |D + w|, delta = R - R0 = (2 D.w + w.w) / (R + R0)
+// without cancellation, x = k R and phase phi0 + k delta.  The trial sums of each test point are
+// formed first (moments S_j), then spread over the test shapes.
+template <int OP>
+__device__ __forceinline__ void far_pair_mixed(const Op& op, const float* fx, const float* fw, int nft,
+                                               const float* bx, const float* bw, int nfb, const SegF& A,
+                                               const SegF& B, FAcc& c) {
+  const dfl Dx = df_sub(dfl{A.cxh, A.cxl}, dfl{B.cxh, B.cxl});
+  const dfl Dy = df_sub(dfl{A.cyh, A.cyl}, dfl{B.cyh, B.cyl});
+  const float dfx = Dx.hi + Dx.lo, dfy = Dy.hi + Dy.lo;
+  float r0 = 0.f, phi0 = 0.f;
+  const float kf = op.khi;
+  if (kf != 0.f) {
+    const dfl R0sq = df_add(df_mul(Dx, Dx), df_mul(Dy, Dy));
+    const dfl R0 = df_mul(R0sq, df_rsqrt(R0sq));
+    r0 = R0.hi + R0.lo;
+    phi0 = reduce_2pi(df_mul(R0, dfl{op.khi, op.klo}));
+  }
+  float pr[4] = {0.f, 0.f, 0.f, 0.f}, pi[4] = {0.f, 0.f, 0.f, 0.f}, mr = 0.f, mi = 0.f;
+  for (int p = 0; p < nft; ++p) {
+    const float sp = fx[p];
+    const float ox = (sp - 0.5f) * A.dx, oy = (sp - 0.5f) * A.dy;
+    float s0r = 0.f, s0i = 0.f, s1r = 0.f, s1i = 0.f;
+    for (int q = 0; q < nfb; ++q) {
+      const float tq = bx[q];
+      const float wx = ox - (tq - 0.5f) * B.dx, wy = oy - (tq - 0.5f) * B.dy;
+      // R from r = D + w itself (no cancellation against R0^2 for close, parallel segments); the
+      // phase increment delta from q = 2 D.w + w.w, accurate in absolute terms
+      const float rx = dfx + wx, ry = dfy + wy;
+      const float R2 = fmaf(rx, rx, ry * ry);
+      const float invR = rsqrtf(R2);
+      const float R = R2 * invR;
+      float Kr, Ki;
+      if (OP == BGB_OP2D_SL || OP == BGB_OP2D_HS) {
+        if (kf == 0.f) {
+          Kr = -kInv2PiF * __logf(R);
+          Ki = 0.f;
+        } else {
+          const float qv = fmaf(2.f * dfx + wx, wx, (2.f * dfy + wy) * wy);
+          const float delta = __fdividef(qv, R + r0);
+          hankel0_mixed(kf * R, fmaf(kf, delta, phi0), Kr, Ki);
+        }
+      } else {
+        float gr, gi;
+        if (kf == 0.f) {
+          gr = -kInv2PiF * invR * invR;
+          gi = 0.f;
+        } else {
+          const float qv = fmaf(2.f * dfx + wx, wx, (2.f * dfy + wy) * wy);
+          const float delta = __fdividef(qv, R + r0);
+          hankel1_mixed(kf * R, fmaf(kf, delta, phi0), 0.25f * kf * invR, gr, gi);
+        }
+        const float proj = OP == BGB_OP2D_DL ? -(rx * B.nx + ry * B.ny) : rx * A.nx + ry * A.ny;
+        Kr = gr * proj;
+        Ki = gi * proj;
+      }
+      const float wq = bw[q] * B.len;
+      const float g0 = op.nsB == 1 ? wq : wq * (1.f - tq), g1 = wq * tq;
+      s0r = fmaf(Kr, g0, s0r);
+      s0i = fmaf(Ki, g0, s0i);
+      s1r = fmaf(Kr, g1, s1r);
+      s1i = fmaf(Ki, g1, s1i);
+    }
+    const float wp = fw[p] * A.len;
+    const float f0 = op.nsA == 1 ? wp : wp * (1.f - sp), f1 = wp * sp;
+    pr[0] = fmaf(f0, s0r, pr[0]);
+    pi[0] = fmaf(f0, s0i, pi[0]);
+    pr[1] = fmaf(f0, s1r, pr[1]);
+    pi[1] = fmaf(f0, s1i, pi[1]);
+    pr[2] = fmaf(f1, s0r, pr[2]);
+    pi[2] = fmaf(f1, s0i, pi[2]);
+    pr[3] = fmaf(f1, s1r, pr[3]);
+    pi[3] = fmaf(f1, s1i, pi[3]);
+    if (OP == BGB_OP2D_HS) {
+      const float sr = op.nsB == 1 ? s0r : s0r + s1r, si = op.nsB == 1 ? s0i : s0i + s1i;
+      mr = fmaf(wp, sr, mr);
+      mi = fmaf(wp, si, mi);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    c.pr[k] = pr[k];
+    c.pi[k] = pi[k];
+  }
+  c.mr = mr;
+  c.mi = mi;
+}
+
+// The local matrix of a mixed far pair, in FP32.
+template <int OP, class LT>
+__device__ __forceinline__ void finalize_mixed(const Op& op, const SegF& A, const SegF& B, const FAcc& c,
+                                               LT* __restrict__ out) {
+  const float nn = A.nx * B.nx + A.ny * B.ny;
+  const float ia = 1.f / A.len, ib = 1.f / B.len;
+  const float dA[2] = {op.nsA == 2 ? -ia : 0.f, op.nsA == 2 ? ia : 0.f};
+  const float dB[2] = {op.nsB == 2 ? -ib : 0.f, op.nsB == 2 ? ib : 0.f};
+  const float bmr = op.fbr * c.mr - op.fbi * c.mi, bmi = op.fbr * c.mi + op.fbi * c.mr;
+  for (int i = 0; i < op.nsA; ++i)
+    for (int j = 0; j < op.nsB; ++j) {
+      const float pr = c.pr[2 * i + j], pi = c.pi[2 * i + j];
+      float lr = op.far_ * pr - op.fai * pi, li = op.far_ * pi + op.fai * pr;
+      if (OP == BGB_OP2D_HS) {
+        const float d = dA[i] * dB[j];
+        lr = fmaf(lr, nn, bmr * d);
+        li = fmaf(li, nn, bmi * d);
+      }
+      out[i * op.nsB + j] = LT{lr, li};
+    }
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
@@ -300,20 +549,25 @@ __device__ __forceinline__ double warp_sum(double v) {
 // ----------------------------------------------------------------------------------------
 // Kernels
 // ----------------------------------------------------------------------------------------
-// counts[0]: list length, [1]: degenerate-pair flag, [2 + class]: non-far pairs of owned columns.
+// counts[0]: list length, [1]: degenerate-pair flag, [2 + class]: non-far pairs of owned columns;
+// mask: bit (sl * nT + tl) set for every non-far pair.
 __global__ void __launch_bounds__(256) k_curve_classify(const SegGeo* __restrict__ gT, const SegGeo* __restrict__ gB,
                                                         const int* __restrict__ T, int nT, const int* __restrict__ S,
                                                         int nS, const unsigned char* __restrict__ own, double k2,
                                                         int LS, Special* __restrict__ list, int cap,
-                                                        int* __restrict__ counts) {
+                                                        int* __restrict__ counts, unsigned* __restrict__ mask) {
   const int tl = blockIdx.x * blockDim.x + threadIdx.x;
   if (tl >= nT) return;
   const SegGeo A = gT[T[tl]];
+  const float k2f = (float)k2;
   for (int sl = blockIdx.y; sl < nS; sl += gridDim.y) {
     const SegGeo B = gB[S[sl]];
+    if (certainly_far(A, B, k2f)) continue;
     int match;
     const int cls = classify(A, B, k2, &match);
     if (cls == 0) continue;
+    const int64_t bit = (int64_t)sl * nT + tl;
+    atomicOr(&mask[bit >> 5], 1u << (bit & 31));
     if (cls < 0) {
       atomicOr(&counts[1], 1);
       continue;
@@ -335,7 +589,8 @@ __global__ void __launch_bounds__(256) k_curve_classify(const SegGeo* __restrict
 template <int OP>
 __global__ void __launch_bounds__(128) k_curve_far(Op op, const Rules* __restrict__ rules, const SegGeo* __restrict__ gT,
                                                    const SegGeo* __restrict__ gB, const int* __restrict__ T, int nT,
-                                                   const int* __restrict__ S, int nS, double2* __restrict__ L) {
+                                                   const int* __restrict__ S, int nS, const unsigned* __restrict__ mask,
+                                                   double2* __restrict__ L) {
   __shared__ double fx[kMaxGL], fw[kMaxGL], bx[kMaxGL], bw[kMaxGL];
   const int nft = rules->nft, nfb = rules->nfb;
   for (int i = threadIdx.x; i < kMaxGL; i += blockDim.x) {
@@ -349,9 +604,8 @@ __global__ void __launch_bounds__(128) k_curve_far(Op op, const Rules* __restric
   if (tl >= nT) return;
   const SegGeo A = gT[T[tl]];
   for (int sl = blockIdx.y; sl < nS; sl += gridDim.y) {
+    if (nonfar_bit(mask, (int64_t)sl * nT + tl)) continue;
     const SegGeo B = gB[S[sl]];
-    int match;
-    if (classify(A, B, op.k2, &match) != 0) continue;
     Acc c;
     acc_zero(c);
     far_pair<OP>(op, fx, fw, nft, bx, bw, nfb, A, B, c);
@@ -360,10 +614,36 @@ __global__ void __launch_bounds__(128) k_curve_far(Op op, const Rules* __restric
 }
 
 template <int OP>
+__global__ void __launch_bounds__(128) k_curve_far_mixed(Op op, const Rules* __restrict__ rules,
+                                                         const SegF* __restrict__ gT, const SegF* __restrict__ gB,
+                                                         const int* __restrict__ T, int nT, const int* __restrict__ S,
+                                                         int nS, const unsigned* __restrict__ mask,
+                                                         float2* __restrict__ L) {
+  __shared__ float fx[kMaxGL], fw[kMaxGL], bx[kMaxGL], bw[kMaxGL];
+  const int nft = rules->nft, nfb = rules->nfb;
+  for (int i = threadIdx.x; i < kMaxGL; i += blockDim.x) {
+    fx[i] = (float)rules->ft_x[i];
+    fw[i] = (float)rules->ft_w[i];
+    bx[i] = (float)rules->fb_x[i];
+    bw[i] = (float)rules->fb_w[i];
+  }
+  __syncthreads();
+  const int tl = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tl >= nT) return;
+  const SegF A = gT[T[tl]];
+  for (int sl = blockIdx.y; sl < nS; sl += gridDim.y) {
+    if (nonfar_bit(mask, (int64_t)sl * nT + tl)) continue;
+    const SegF B = gB[S[sl]];
+    FAcc c;
+    far_pair_mixed<OP>(op, fx, fw, nft, bx, bw, nfb, A, B, c);
+    finalize_mixed<OP>(op, A, B, c, L + ((int64_t)sl * nT + tl) * op.LS);
+  }
+}
+
+template <int OP, class LT>
 __global__ void __launch_bounds__(256) k_curve_special(Op op, const Rules* __restrict__ rules,
                                                        const SegGeo* __restrict__ gT, const SegGeo* __restrict__ gB,
-                                                       const Special* __restrict__ list, int n,
-                                                       double2* __restrict__ L) {
+                                                       const Special* __restrict__ list, int n, LT* __restrict__ L) {
   __shared__ Rules sR;
   {
     const int* src = (const int*)rules;
@@ -395,8 +675,9 @@ __global__ void __launch_bounds__(256) k_curve_special(Op op, const Rules* __res
 // for k_curve_special.  err[0]: list length, err[1]: invalid pair / rule.
 template <int OP>
 __global__ void __launch_bounds__(128) k_curve_pairs(Op op, const Rules* __restrict__ rules, const SegGeo* __restrict__ gT,
-                                                     const SegGeo* __restrict__ gB, const int2* __restrict__ pairs,
-                                                     int64_t npairs, int force, double2* __restrict__ L,
+                                                     const SegGeo* __restrict__ gB, const SegF* __restrict__ gTf,
+                                                     const SegF* __restrict__ gBf, const int2* __restrict__ pairs,
+                                                     int64_t npairs, int force, int mixed, double2* __restrict__ L,
                                                      signed char* __restrict__ cls_out, Special* __restrict__ list,
                                                      int* __restrict__ err) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -411,10 +692,26 @@ __global__ void __launch_bounds__(128) k_curve_pairs(Op op, const Rules* __restr
     return;
   }
   if (rule == 0) {
-    Acc c;
-    acc_zero(c);
-    far_pair<OP>(op, rules->ft_x, rules->ft_w, rules->nft, rules->fb_x, rules->fb_w, rules->nfb, A, B, c);
-    finalize<OP>(op, A, B, c, L + p * 4);
+    if (mixed) {
+      float fx[kMaxGL], fw[kMaxGL], bx[kMaxGL], bw[kMaxGL];
+      for (int i = 0; i < rules->nft; ++i) {
+        fx[i] = (float)rules->ft_x[i];
+        fw[i] = (float)rules->ft_w[i];
+      }
+      for (int i = 0; i < rules->nfb; ++i) {
+        bx[i] = (float)rules->fb_x[i];
+        bw[i] = (float)rules->fb_w[i];
+      }
+      FAcc c;
+      const SegF Af = gTf[pairs[p].x], Bf = gBf[pairs[p].y];
+      far_pair_mixed<OP>(op, fx, fw, rules->nft, bx, bw, rules->nfb, Af, Bf, c);
+      finalize_mixed<OP>(op, Af, Bf, c, L + p * 4);
+    } else {
+      Acc c;
+      acc_zero(c);
+      far_pair<OP>(op, rules->ft_x, rules->ft_w, rules->nft, rules->fb_x, rules->fb_w, rules->nfb, A, B, c);
+      finalize<OP>(op, A, B, c, L + p * 4);
+    }
     return;
   }
   const int idx = atomicAdd(&err[0], 1);
@@ -428,26 +725,29 @@ __global__ void __launch_bounds__(128) k_curve_pairs(Op op, const Rules* __restr
 }
 
 // Z[m, n] = sum over supports (test outer, trial inner, both by segment) of c_m c_n L.
-template <typename OutT>
-__global__ void __launch_bounds__(256) k_curve_gather(const double2* __restrict__ L, int nT, int LS, int nsB,
+// Local matrices, coefficients and sums in FP64 (double2) or FP32 (float2, the mixed path).
+template <typename OutT, typename LT>
+__global__ void __launch_bounds__(256) k_curve_gather(const LT* __restrict__ L, int nT, int LS, int nsB,
                                                       int nrows, int ncols, const int64_t* __restrict__ toff,
-                                                      const int* __restrict__ tcode, const double* __restrict__ tcoef,
+                                                      const int* __restrict__ tcode,
+                                                      const decltype(LT::x)* __restrict__ tcoef,
                                                       const int64_t* __restrict__ boff, const int* __restrict__ bcode,
-                                                      const double* __restrict__ bcoef, OutT* __restrict__ out,
+                                                      const decltype(LT::x)* __restrict__ bcoef, OutT* __restrict__ out,
                                                       int64_t ld) {
+  typedef decltype(LT::x) R;
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= nrows) return;
   const int64_t a0 = toff[m], a1 = toff[m + 1];
   for (int n = blockIdx.y; n < ncols; n += gridDim.y) {
-    double zr = 0.0, zi = 0.0;
+    R zr = 0, zi = 0;
     const int64_t b0 = boff[n], b1 = boff[n + 1];
     for (int64_t a = a0; a < a1; ++a) {
       const int ta = tcode[a];
-      const double ca = tcoef[a];
+      const R ca = tcoef[a];
       for (int64_t b = b0; b < b1; ++b) {
         const int tb = bcode[b];
-        const double2 v = L[((int64_t)(tb >> 1) * nT + (ta >> 1)) * LS + (ta & 1) * nsB + (tb & 1)];
-        const double cb = bcoef[b];
+        const LT v = L[((int64_t)(tb >> 1) * nT + (ta >> 1)) * LS + (ta & 1) * nsB + (tb & 1)];
+        const R cb = bcoef[b];
         zr += (v.x * ca) * cb;
         zi += (v.y * ca) * cb;
       }
@@ -511,6 +811,12 @@ static int make_op(const bgb_operator2d* op, const bgb_curve_space* a, const bgb
   o.ai = op->alpha[1];
   o.br = op->beta[0];
   o.bi = op->beta[1];
+  o.khi = (float)o.k;
+  o.klo = (float)(o.k - (double)o.khi);
+  o.far_ = (float)o.ar;
+  o.fai = (float)o.ai;
+  o.fbr = (float)o.br;
+  o.fbi = (float)o.bi;
   *out = o;
   return 0;
 }
@@ -548,16 +854,19 @@ static int make_rules(const bgb_quadstrat2d* qs, Rules* R) {
   return 0;
 }
 
-static int upload_curve(cudaStream_t st, const bgb_curve_space* s, DevBuf& verts, DevBuf& segs, DevBuf& geo) {
+static int upload_curve(cudaStream_t st, const bgb_curve_space* s, DevBuf& verts, DevBuf& segs, DevBuf& geo,
+                        DevBuf& geof) {
   int rc;
   if ((rc = verts.ensure(sizeof(double) * 2 * (size_t)std::max(1, s->nv))) ||
       (rc = segs.ensure(sizeof(int) * 2 * (size_t)std::max(1, s->ns))) ||
-      (rc = geo.ensure(sizeof(SegGeo) * (size_t)std::max(1, s->ns))))
+      (rc = geo.ensure(sizeof(SegGeo) * (size_t)std::max(1, s->ns))) ||
+      (rc = geof.ensure(sizeof(SegF) * (size_t)std::max(1, s->ns))))
     return rc;
   if (s->nv) BGB_CUDA(cudaMemcpyAsync(verts.p, s->vertices, sizeof(double) * 2 * (size_t)s->nv, cudaMemcpyHostToDevice, st));
   if (s->ns) {
     BGB_CUDA(cudaMemcpyAsync(segs.p, s->segments, sizeof(int) * 2 * (size_t)s->ns, cudaMemcpyHostToDevice, st));
-    k_curve_geo<<<(s->ns + 255) / 256, 256, 0, st>>>(verts.as<double>(), segs.as<int>(), s->ns, geo.as<SegGeo>());
+    k_curve_geo<<<(s->ns + 255) / 256, 256, 0, st>>>(verts.as<double>(), segs.as<int>(), s->ns, geo.as<SegGeo>(),
+                                                     geof.as<SegF>());
     BGB_CUDA(cudaGetLastError());
   }
   return 0;
@@ -573,23 +882,39 @@ static int put(cudaStream_t st, DevBuf& buf, const std::vector<T>& v) {
 
 template <int OP>
 static void launch_far(const Op& op, const Rules* rules, const SegGeo* gT, const SegGeo* gB, const int* T, int nT,
-                       const int* S, int nS, double2* L, cudaStream_t st) {
+                       const int* S, int nS, const unsigned* mask, double2* L, cudaStream_t st) {
   dim3 grid((nT + 127) / 128, std::min(nS, 65535));
-  k_curve_far<OP><<<grid, 128, 0, st>>>(op, rules, gT, gB, T, nT, S, nS, L);
+  k_curve_far<OP><<<grid, 128, 0, st>>>(op, rules, gT, gB, T, nT, S, nS, mask, L);
+}
+
+template <int OP>
+static void launch_far_mixed(const Op& op, const Rules* rules, const SegF* gT, const SegF* gB, const int* T, int nT,
+                             const int* S, int nS, const unsigned* mask, float2* L, cudaStream_t st) {
+  dim3 grid((nT + 127) / 128, std::min(nS, 65535));
+  k_curve_far_mixed<OP><<<grid, 128, 0, st>>>(op, rules, gT, gB, T, nT, S, nS, mask, L);
+}
+
+template <int OP, class LT>
+static void launch_special_t(const Op& op, const Rules* rules, const SegGeo* gT, const SegGeo* gB, const Special* list,
+                             int n, LT* L, int num_sms, cudaStream_t st) {
+  if (n <= 0) return;
+  const int blocks = std::max(1, std::min((n + 7) / 8, num_sms * 8));
+  k_curve_special<OP, LT><<<blocks, 256, 0, st>>>(op, rules, gT, gB, list, n, L);
 }
 
 template <int OP>
 static void launch_special(const Op& op, const Rules* rules, const SegGeo* gT, const SegGeo* gB, const Special* list,
-                           int n, double2* L, int num_sms, cudaStream_t st) {
-  if (n <= 0) return;
-  const int blocks = std::max(1, std::min((n + 7) / 8, num_sms * 8));
-  k_curve_special<OP><<<blocks, 256, 0, st>>>(op, rules, gT, gB, list, n, L);
+                           int n, void* L, bool fp32_l, int num_sms, cudaStream_t st) {
+  if (fp32_l) launch_special_t<OP, float2>(op, rules, gT, gB, list, n, (float2*)L, num_sms, st);
+  else launch_special_t<OP, double2>(op, rules, gT, gB, list, n, (double2*)L, num_sms, st);
 }
 
 template <int OP>
-static void launch_pairs(const Op& op, const Rules* rules, const SegGeo* gT, const SegGeo* gB, const int2* pairs,
-                         int64_t np, int force, double2* L, signed char* cls, Special* list, int* err, cudaStream_t st) {
-  k_curve_pairs<OP><<<(unsigned)((np + 127) / 128), 128, 0, st>>>(op, rules, gT, gB, pairs, np, force, L, cls, list, err);
+static void launch_pairs(const Op& op, const Rules* rules, const SegGeo* gT, const SegGeo* gB, const SegF* gTf,
+                         const SegF* gBf, const int2* pairs, int64_t np, int force, int mixed, double2* L,
+                         signed char* cls, Special* list, int* err, cudaStream_t st) {
+  k_curve_pairs<OP><<<(unsigned)((np + 127) / 128), 128, 0, st>>>(op, rules, gT, gB, gTf, gBf, pairs, np, force, mixed,
+                                                                  L, cls, list, err);
 }
 
 #define BGB_CURVE_DISPATCH(kind, fn, ...)                              \
@@ -654,8 +979,8 @@ using namespace bgb::curve;
 extern "C" {
 
 int bgb_assemble_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_curve_space* test,
-                       const bgb_curve_space* trial, const bgb_quadstrat2d* qs, void* out, int32_t out_kind,
-                       int64_t ld, int64_t row0, int64_t nrows, void* stream, bgb_stats* stats) {
+                       const bgb_curve_space* trial, const bgb_quadstrat2d* qs, int32_t precision, void* out,
+                       int32_t out_kind, int64_t ld, int64_t row0, int64_t nrows, void* stream, bgb_stats* stats) {
   const auto t_start = std::chrono::steady_clock::now();
   if (!h) { set_error("handle is NULL"); return BGB_ERR_INVALID; }
   std::lock_guard<std::mutex> lk(h->mu);
@@ -664,6 +989,7 @@ int bgb_assemble_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_curve_
   Op o;
   Rules R;
   if ((rc = make_op(op, test, trial, &o)) || (rc = make_rules(qs, &R))) return rc;
+  if (precision != BGB_PREC_FP64 && precision != BGB_PREC_MIXED) { set_error("bad precision %d", precision); return BGB_ERR_INVALID; }
   if (out_kind < BGB_OUT_HOST_C64 || out_kind > BGB_OUT_DEVICE_C32) { set_error("bad out_kind %d", out_kind); return BGB_ERR_INVALID; }
   if (nrows < 0) nrows = (int64_t)test->nfun - row0;
   if (row0 < 0 || row0 + nrows > test->nfun) { set_error("row window [%lld, %lld) outside [0, %d)", (long long)row0, (long long)(row0 + nrows), test->nfun); return BGB_ERR_INVALID; }
@@ -686,7 +1012,8 @@ int bgb_assemble_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_curve_
     BGB_CUDA(cudaStreamWaitEvent(s, h->ev[7], 0));
   }
   CurveBufs& B = h->curve;
-  if ((rc = upload_curve(s, test, B.verts_t, B.segs_t, B.geo_t)) || (rc = upload_curve(s, trial, B.verts_b, B.segs_b, B.geo_b)))
+  if ((rc = upload_curve(s, test, B.verts_t, B.segs_t, B.geo_t, B.geof_t)) ||
+      (rc = upload_curve(s, trial, B.verts_b, B.segs_b, B.geo_b, B.geof_b)))
     return rc;
   if ((rc = B.rules.ensure(sizeof(Rules)))) return rc;
   BGB_CUDA(cudaMemcpyAsync(B.rules.p, &R, sizeof(Rules), cudaMemcpyHostToDevice, s));
@@ -699,8 +1026,11 @@ int bgb_assemble_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_curve_
   std::vector<int> T, tcode;
   localise(TS, T, tcode, scratch);
   const int nT = (int)T.size();
+  const bool fp32_l = precision == BGB_PREC_MIXED;  // mixed: local matrices, coefficients, gather in FP32
+  const size_t lsz = fp32_l ? sizeof(float2) : sizeof(double2);
+  std::vector<float> tcoef_f(TS.coef.begin(), TS.coef.end());
   if ((rc = put(s, B.T, T)) || (rc = put(s, B.tsup_off, TS.off)) || (rc = put(s, B.tsup_i, tcode)) ||
-      (rc = put(s, B.tsup_c, TS.coef)))
+      (rc = (fp32_l ? put(s, B.tsup_c, tcoef_f) : put(s, B.tsup_c, TS.coef))))
     return rc;
 
   // column blocks sized to the HBM budget: local matrices of nT x |S_b| pairs (|S_b| <= 2 per column)
@@ -708,7 +1038,7 @@ int bgb_assemble_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_curve_
   cudaMemGetInfo(&freeb, &totalb);
   const int64_t budget = h->cfg.hbm_budget_bytes > 0 ? h->cfg.hbm_budget_bytes : (int64_t)(0.9 * (double)freeb);
   const int64_t ncols = trial->nfun;
-  const int64_t per_col = 2 * (int64_t)std::max(1, nT) * o.LS * 16 + (host_out ? nrows * (int64_t)esz : 0);
+  const int64_t per_col = 2 * (int64_t)std::max(1, nT) * o.LS * (int64_t)lsz + (host_out ? nrows * (int64_t)esz : 0);
   const int64_t cols_per_block = std::max<int64_t>(1, std::min<int64_t>(ncols, budget / 2 / std::max<int64_t>(1, per_col)));
   std::vector<unsigned char> seen((size_t)trial->ns, 0);
   int64_t computed = 0, nonfar[5] = {0, 0, 0, 0, 0};
@@ -728,23 +1058,27 @@ int bgb_assemble_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_curve_
       own[(size_t)k] = !seen[(size_t)S[(size_t)k]];
       seen[(size_t)S[(size_t)k]] = 1;
     }
+    std::vector<float> bcoef_f(BS.coef.begin(), BS.coef.end());
     if ((rc = put(s, B.S, S)) || (rc = put(s, B.own, own)) || (rc = put(s, B.bsup_off, BS.off)) ||
-        (rc = put(s, B.bsup_i, bcode)) || (rc = put(s, B.bsup_c, BS.coef)))
+        (rc = put(s, B.bsup_i, bcode)) || (rc = (fp32_l ? put(s, B.bsup_c, bcoef_f) : put(s, B.bsup_c, BS.coef))))
       return rc;
     const int64_t npairs = (int64_t)nT * nS;
     computed += npairs;
-    if ((rc = B.L.ensure(sizeof(double2) * (size_t)std::max<int64_t>(1, npairs * o.LS)))) return rc;
+    if ((rc = B.L.ensure(lsz * (size_t)std::max<int64_t>(1, npairs * o.LS)))) return rc;
     if ((rc = B.counts.ensure(sizeof(int) * 8))) return rc;
+    const size_t mask_bytes = sizeof(unsigned) * (size_t)((npairs + 31) / 32);
+    if ((rc = B.mask.ensure(std::max<size_t>(4, mask_bytes)))) return rc;
     int counts[8] = {0};
     if (nT > 0 && nS > 0) {
       for (int attempt = 0; attempt < 2; ++attempt) {
         if ((rc = B.list.ensure(sizeof(Special) * (size_t)cap))) return rc;
         BGB_CUDA(cudaMemsetAsync(B.counts.p, 0, sizeof(int) * 8, s));
+        BGB_CUDA(cudaMemsetAsync(B.mask.p, 0, mask_bytes, s));
         BGB_CUDA(cudaEventRecord(h->ev[0], s));
         dim3 grid((nT + 255) / 256, std::min(nS, 65535));
         k_curve_classify<<<grid, 256, 0, s>>>(B.geo_t.as<SegGeo>(), B.geo_b.as<SegGeo>(), B.T.as<int>(), nT, B.S.as<int>(),
                                               nS, B.own.as<unsigned char>(), o.k2, o.LS, B.list.as<Special>(), cap,
-                                              B.counts.as<int>());
+                                              B.counts.as<int>(), B.mask.as<unsigned>());
         BGB_CUDA(cudaGetLastError());
         BGB_CUDA(cudaEventRecord(h->ev[1], s));
         BGB_CUDA(cudaMemcpyAsync(counts, B.counts.p, sizeof(int) * 8, cudaMemcpyDeviceToHost, s));
@@ -758,12 +1092,17 @@ int bgb_assemble_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_curve_
       if (counts[0] > cap) { set_error("non-far pair list overflow"); return BGB_ERR_CAPACITY; }
       for (int c = 1; c < 5; ++c) nonfar[c] += counts[2 + c];
       BGB_CUDA(cudaEventRecord(h->ev[2], s));
-      BGB_CURVE_DISPATCH(o.kind, launch_far, o, B.rules.as<Rules>(), B.geo_t.as<SegGeo>(), B.geo_b.as<SegGeo>(),
-                         B.T.as<int>(), nT, B.S.as<int>(), nS, B.L.as<double2>(), s);
+      if (precision == BGB_PREC_MIXED) {
+        BGB_CURVE_DISPATCH(o.kind, launch_far_mixed, o, B.rules.as<Rules>(), B.geof_t.as<SegF>(), B.geof_b.as<SegF>(),
+                           B.T.as<int>(), nT, B.S.as<int>(), nS, B.mask.as<unsigned>(), B.L.as<float2>(), s);
+      } else {
+        BGB_CURVE_DISPATCH(o.kind, launch_far, o, B.rules.as<Rules>(), B.geo_t.as<SegGeo>(), B.geo_b.as<SegGeo>(),
+                           B.T.as<int>(), nT, B.S.as<int>(), nS, B.mask.as<unsigned>(), B.L.as<double2>(), s);
+      }
       BGB_CUDA(cudaGetLastError());
       BGB_CUDA(cudaEventRecord(h->ev[3], s));
       BGB_CURVE_DISPATCH(o.kind, launch_special, o, B.rules.as<Rules>(), B.geo_t.as<SegGeo>(), B.geo_b.as<SegGeo>(),
-                         B.list.as<Special>(), counts[0], B.L.as<double2>(), h->num_sms, s);
+                         B.list.as<Special>(), counts[0], B.L.p, fp32_l, h->num_sms, s);
       BGB_CUDA(cudaGetLastError());
       BGB_CUDA(cudaEventRecord(h->ev[4], s));
       launches += 1 + (counts[0] > 0);
@@ -785,14 +1124,16 @@ int bgb_assemble_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_curve_
       dld = ld;
     }
     dim3 gg((unsigned)((nrows + 255) / 256), (unsigned)std::min<int64_t>(bc, 65535));
-    if (c64)
-      k_curve_gather<double2><<<gg, 256, 0, s>>>(B.L.as<double2>(), nT, o.LS, o.nsB, (int)nrows, (int)bc, B.tsup_off.as<int64_t>(),
-                                                 B.tsup_i.as<int>(), B.tsup_c.as<double>(), B.bsup_off.as<int64_t>(),
-                                                 B.bsup_i.as<int>(), B.bsup_c.as<double>(), (double2*)dst, dld);
-    else
-      k_curve_gather<float2><<<gg, 256, 0, s>>>(B.L.as<double2>(), nT, o.LS, o.nsB, (int)nrows, (int)bc, B.tsup_off.as<int64_t>(),
-                                                B.tsup_i.as<int>(), B.tsup_c.as<double>(), B.bsup_off.as<int64_t>(),
-                                                B.bsup_i.as<int>(), B.bsup_c.as<double>(), (float2*)dst, dld);
+#define BGB_CURVE_GATHER(OutT, LT)                                                                                 \
+  k_curve_gather<OutT, LT><<<gg, 256, 0, s>>>(B.L.as<LT>(), nT, o.LS, o.nsB, (int)nrows, (int)bc,                       \
+                                              B.tsup_off.as<int64_t>(), B.tsup_i.as<int>(),                             \
+                                              B.tsup_c.as<decltype(LT::x)>(), B.bsup_off.as<int64_t>(),                 \
+                                              B.bsup_i.as<int>(), B.bsup_c.as<decltype(LT::x)>(), (OutT*)dst, dld)
+    if (c64 && !fp32_l) BGB_CURVE_GATHER(double2, double2);
+    else if (c64) BGB_CURVE_GATHER(double2, float2);
+    else if (!fp32_l) BGB_CURVE_GATHER(float2, double2);
+    else BGB_CURVE_GATHER(float2, float2);
+#undef BGB_CURVE_GATHER
     BGB_CUDA(cudaGetLastError());
     ++launches;
     BGB_CUDA(cudaEventRecord(h->ev[5], s));
@@ -832,9 +1173,9 @@ int bgb_assemble_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_curve_
 }
 
 int bgb_local_matrices_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_curve_space* test,
-                             const bgb_curve_space* trial, const bgb_quadstrat2d* qs, int64_t npairs,
-                             const int32_t* tau, const int32_t* sigma, int32_t force_class, double* out,
-                             int8_t* cls_out) {
+                             const bgb_curve_space* trial, const bgb_quadstrat2d* qs, int32_t precision,
+                             int64_t npairs, const int32_t* tau, const int32_t* sigma, int32_t force_class,
+                             double* out, int8_t* cls_out) {
   if (!h) { set_error("handle is NULL"); return BGB_ERR_INVALID; }
   std::lock_guard<std::mutex> lk(h->mu);
   int rc;
@@ -842,6 +1183,7 @@ int bgb_local_matrices_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_
   Op o;
   Rules R;
   if ((rc = make_op(op, test, trial, &o)) || (rc = make_rules(qs, &R))) return rc;
+  if (precision != BGB_PREC_FP64 && precision != BGB_PREC_MIXED) { set_error("bad precision %d", precision); return BGB_ERR_INVALID; }
   if (npairs < 0 || (npairs > 0 && (!tau || !sigma || !out))) { set_error("invalid pair list"); return BGB_ERR_INVALID; }
   if (force_class != -1 && force_class != 0 && force_class != 1 && force_class != 3 && force_class != 4) {
     set_error("force_class %d is not a curve pair class", force_class);
@@ -860,7 +1202,8 @@ int bgb_local_matrices_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_
   cudaSetDevice(h->device);
   cudaStream_t s = h->stream;
   CurveBufs& B = h->curve;
-  if ((rc = upload_curve(s, test, B.verts_t, B.segs_t, B.geo_t)) || (rc = upload_curve(s, trial, B.verts_b, B.segs_b, B.geo_b)))
+  if ((rc = upload_curve(s, test, B.verts_t, B.segs_t, B.geo_t, B.geof_t)) ||
+      (rc = upload_curve(s, trial, B.verts_b, B.segs_b, B.geo_b, B.geof_b)))
     return rc;
   if ((rc = B.rules.ensure(sizeof(Rules)))) return rc;
   BGB_CUDA(cudaMemcpyAsync(B.rules.p, &R, sizeof(Rules), cudaMemcpyHostToDevice, s));
@@ -871,7 +1214,8 @@ int bgb_local_matrices_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_
   BGB_CUDA(cudaMemsetAsync(B.out.p, 0, sizeof(double2) * 4 * (size_t)npairs, s));
   BGB_CUDA(cudaMemsetAsync(B.counts.p, 0, sizeof(int) * 8, s));
   BGB_CURVE_DISPATCH(o.kind, launch_pairs, o, B.rules.as<Rules>(), B.geo_t.as<SegGeo>(), B.geo_b.as<SegGeo>(),
-                     B.pairs.as<int2>(), npairs, force_class, B.out.as<double2>(), (signed char*)B.own.p,
+                     B.geof_t.as<SegF>(), B.geof_b.as<SegF>(), B.pairs.as<int2>(), npairs, force_class, precision == BGB_PREC_MIXED ? 1 : 0,
+                     B.out.as<double2>(), (signed char*)B.own.p,
                      B.list.as<Special>(), B.counts.as<int>(), s);
   BGB_CUDA(cudaGetLastError());
   int counts[8] = {0};
@@ -882,7 +1226,7 @@ int bgb_local_matrices_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_
     return BGB_ERR_INVALID;
   }
   BGB_CURVE_DISPATCH(o.kind, launch_special, o, B.rules.as<Rules>(), B.geo_t.as<SegGeo>(), B.geo_b.as<SegGeo>(),
-                     B.list.as<Special>(), counts[0], B.out.as<double2>(), h->num_sms, s);
+                     B.list.as<Special>(), counts[0], B.out.p, false, h->num_sms, s);
   BGB_CUDA(cudaGetLastError());
   std::vector<double2> L((size_t)npairs * 4);
   std::vector<signed char> cls((size_t)npairs);

@@ -21,7 +21,7 @@ Other workloads print the same kind of line for their own configuration:
   --workload c5   EFIE on an icosphere of level 6 (81,920 triangles, 122,880 RWG), k = 2 pi * 8,
                   ComplexF32 output (121 GB) streamed to pinned host memory in output blocks
   --workload curve  Helmholtz2D hypersingular (the operator of the reference's 2-D prototype) on
-                  hats over a jittered ellipse of 16,384 segments, k = 2 pi * 100, FP64
+                  hats over a jittered ellipse of 16,384 segments, k = 2 pi * 100, mixed and FP64
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c2|c3|c4|c5|curve] [--impl reference]
 
@@ -199,11 +199,15 @@ def rows_error(Z_rows, ref):
 
 
 CURVE_N, CURVE_K, CURVE_ROWS = 16384, 2 * np.pi * 100, 64
-# FP64 flops (2 DFMA + DADD + DMUL thread instructions) per far point pair of the hypersingular far
-# kernel, counted by ncu on the 4,096-segment case (profiles/curve_hypersingular_ellipse.md), and
-# its DRAM bytes per segment pair (the 2x2 complex local matrix written once).
+# FP64 flops (2 DFMA + DADD + DMUL thread instructions) per far point pair of the plain hypersingular
+# far kernel, counted by ncu on the 4,096-segment case (profiles/curve_hypersingular_ellipse.md), and
+# its DRAM bytes per segment pair (the 2x2 complex double local matrix written once).
 CURVE_FP64_FLOPS_PER_POINT_PAIR = 239.5
 CURVE_DRAM_BYTES_PER_PAIR = 1.040e9 / (4096 * 4096)
+# The same for the mixed far kernel: FP32 flops (2 FFMA + FADD + FMUL) per far point pair and DRAM
+# bytes per segment pair (the local matrix as 2x2 complex float), ncu on the 4,096-segment case.
+CURVE_MIXED_FP32_FLOPS_PER_POINT_PAIR = 97.2
+CURVE_MIXED_DRAM_BYTES_PER_PAIR = 0.4755e9 / (4096 * 4096)
 
 
 def curve_workload(n=CURVE_N):
@@ -214,7 +218,7 @@ def curve_workload(n=CURVE_N):
 
 def curve_config(mesh, X, extra=None):
     d = {"workload": f"Helmholtz2D.hypersingular on lagrangec0d1 hats, jittered ellipse (1, 0.5) of {mesh.ns} "
-                     f"segments, k=2*pi*100, FP64 (far 4x4 Gauss, near 12, singular order 10)",
+                     f"segments, k=2*pi*100 (far 4x4 Gauss, near 12, singular order 10)",
          "segments": mesh.ns, "functions": X.nfun, "pairs_per_step": mesh.ns * mesh.ns,
          "l2": "outputs > L2; a 256 MiB buffer is written between timed steps"}
     d.update(extra or {})
@@ -241,7 +245,7 @@ def run_reference_curve(args):
             vals.append(CURVE_ROWS * pairs_per_row / dt)
     v = float(np.mean(vals))
     sample = f"{CURVE_ROWS} random rows per step ({CURVE_ROWS * pairs_per_row} segment pairs)"
-    print(json.dumps({"metric": "segment pair-interactions/s (2-D, FP64)", "value": v, "unit": UNIT,
+    print(json.dumps({"metric": "segment pair-interactions/s (2-D): mixed FP32 vs plain FP64", "value": v, "unit": UNIT,
                       "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
                       "ms_per_step": CURVE_ROWS * pairs_per_row / v * 1e3, "higher_is_better": True,
                       "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded ellipse)",
@@ -253,19 +257,22 @@ def run_reference_curve(args):
 
 
 def run_curve(args):
-    """2-D path: Helmholtz2D hypersingular on an ellipse, FP64, device output and e2e to pinned host."""
+    """2-D path: Helmholtz2D hypersingular on an ellipse; mixed (value) and plain FP64, device output,
+    and e2e of the mixed fill into pinned host memory."""
     import torch
     import oracle
     rank, world, local = dist_init(args.gpus)
     bg, mesh, X, op, qs = curve_workload(args.curve_segments)
     pairs = mesh.ns * mesh.ns
-    _, fp64_peak, _ = bg.measure_issue_peaks(local)
+    fp32_peak, fp64_peak, _ = bg.measure_issue_peaks(local)
     barrier(world)
     with ClockSampler(local) as clocks:
-        ms, st, _, Z = time_fill(bg, X, op, "fp64", args.steps, args.warmup, local)
+        ms_m, st_m, _, Zm = time_fill(bg, X, op, "mixed", args.steps, args.warmup, local)
     barrier(world)
-    m = max_over_ranks(float(np.mean(ms)), world, local)
+    m = max_over_ranks(float(np.mean(ms_m)), world, local)
     value = world * pairs / (m * 1e-3)
+    ms_d, st_d, _, Zd = time_fill(bg, X, op, "fp64", args.fp64_steps, min(args.warmup, 3), local)
+    md = max_over_ranks(float(np.mean(ms_d)), world, local)
     out = {}
     if rank == 0:
         rows = np.sort(np.random.default_rng(ERR_SEED).choice(X.nfun, CURVE_ROWS, replace=False)).astype(np.int32)
@@ -273,46 +280,60 @@ def run_curve(args):
         t0 = time.perf_counter()
         ref = oracle.assemble_rows_curve(op, X, X, qs, rows, nthreads=threads)
         cpu_s = time.perf_counter() - t0
-        ridx = torch.as_tensor(rows.astype(np.int64), device=Z.device)
-        out["error_vs_oracle"] = {"fp64": rows_error(Z[:, ridx].T.cpu().numpy(), ref), "rows": CURVE_ROWS,
+        ridx = torch.as_tensor(rows.astype(np.int64), device=Zm.device)
+        out["error_vs_oracle"] = {"mixed": rows_error(Zm[:, ridx].T.cpu().numpy().astype(np.complex128), ref),
+                                  "fp64": rows_error(Zd[:, ridx].T.cpu().numpy(), ref), "rows": CURVE_ROWS,
                                   "seed": ERR_SEED}
         cpu_pairs = CURVE_ROWS * 2 * mesh.ns
         out["cpu_baseline"] = {"value": cpu_pairs / cpu_s, "unit": UNIT, "cores": threads, "kind": "port",
                                "sample": f"{CURVE_ROWS} seeded rows ({cpu_pairs} segment pairs, {cpu_s:.1f} s), "
                                          f"FP64 curve oracle with OpenMP"}
-    del Z
+    del Zm, Zd
     torch.cuda.empty_cache()
     e2e = None
     if not args.no_e2e:
-        pinned = torch.empty((X.nfun, X.nfun), dtype=torch.complex128, pin_memory=True)
-        ms_e2e, st_e2e, _, _ = time_fill(bg, X, op, "fp64", max(2, args.steps // 2), 1, local, out="host",
+        pinned = torch.empty((X.nfun, X.nfun), dtype=torch.complex64, pin_memory=True)
+        ms_e2e, st_e2e, _, _ = time_fill(bg, X, op, "mixed", max(3, args.steps // 2), 1, local, out="host",
                                          pinned=pinned)
         e2e_ms = max_over_ranks(float(np.mean(ms_e2e)), world, local)
         h2d = X.mesh.vertices.nbytes + X.mesh.segments.nbytes + X.fn_index.nbytes + X.fn_coef.nbytes
         e2e = {"value": world * pairs / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(X.nfun) * int(X.nfun) * 16, "ms_per_step": e2e_ms,
+               "d2h_bytes_per_step": int(X.nfun) * int(X.nfun) * 8, "ms_per_step": e2e_ms,
                "ms_copy": float(np.mean([s["ms_copy"] for s in st_e2e]))}
         del pinned
     if rank != 0:
         return 0
-    far_ms = float(np.mean([s["ms_far"] for s in st]))
-    cls = st[0]["pairs_class"]
+    cls = st_m[0]["pairs_class"]
     point_pairs = cls[0] * qs.far_test * qs.far_trial
-    kern = {"far_and_gather": far_ms, "singular_and_near": float(np.mean([s["ms_singular"] for s in st])),
-            "classify": float(np.mean([s["ms_classify"] for s in st]))}
-    tf = point_pairs * CURVE_FP64_FLOPS_PER_POINT_PAIR / (far_ms * 1e-3) / 1e12
-    roof = {"kernel": "curve::k_curve_far<HS> (+ gather)", "bound": "fp64", "achieved": tf, "peak": fp64_peak,
-            "unit": "TFLOP/s", "frac": tf / fp64_peak, "traffic": CURVE_DRAM_BYTES_PER_PAIR * pairs,
+
+    def kernels(st):
+        return {"far_and_gather": float(np.mean([s["ms_far"] for s in st])),
+                "singular_and_near_fp64": float(np.mean([s["ms_singular"] for s in st])),
+                "classify": float(np.mean([s["ms_classify"] for s in st]))}
+    km, kd = kernels(st_m), kernels(st_d)
+    tf = point_pairs * CURVE_MIXED_FP32_FLOPS_PER_POINT_PAIR / (km["far_and_gather"] * 1e-3) / 1e12
+    roof = {"kernel": "curve::k_curve_far_mixed<HS> (+ gather)", "bound": "fp32", "achieved": tf, "peak": fp32_peak,
+            "unit": "TFLOP/s", "frac": tf / fp32_peak, "traffic": CURVE_MIXED_DRAM_BYTES_PER_PAIR * pairs,
             "traffic_source": "ncu dram__bytes of the 4,096-segment launch scaled by pairs (x16)",
-            "peak_source": "measured live by bgb_measure_issue_peaks (DFMA chains)",
-            "flop_convention": f"{CURVE_FP64_FLOPS_PER_POINT_PAIR} FP64 flops per far point pair (ncu count: "
-                               "2 DFMA + DADD + DMUL, CUDA's J0 and Y0 included)"}
-    line = line_base(args, world, value, m, "f64", curve_config(mesh, X, {
-        "parallelism": f"{world} independent matrices, one per rank, no collective" if world > 1 else "single GPU"}),
-        metric="segment pair-interactions/s (2-D, FP64)",
-        roofline=roof, kernels_ms=kern, far_point_pairs_per_s=point_pairs / (far_ms * 1e-3), pairs_class=cls,
-        fp64_peak_tflops=fp64_peak, clocks=clocks.summary(),
-        gpu_launches=int(sum(s["kernel_launches"] for s in st)), e2e=e2e)
+            "peak_source": "measured live by bgb_measure_issue_peaks (FFMA chains)",
+            "flop_convention": f"{CURVE_MIXED_FP32_FLOPS_PER_POINT_PAIR} FP32 flops per far point pair (ncu count: "
+                               "2 FFMA + FADD + FMUL, per-pair double-float setup included)",
+            "note": "issue-bound: 89% of issue slots (FMA 46%, ALU 45%, MUFU 19% of peak), ncu on 4,096 segments"}
+    tf64 = point_pairs * CURVE_FP64_FLOPS_PER_POINT_PAIR / (kd["far_and_gather"] * 1e-3) / 1e12
+    roof64 = {"kernel": "curve::k_curve_far<HS> (+ gather)", "bound": "fp64", "achieved": tf64, "peak": fp64_peak,
+              "unit": "TFLOP/s", "frac": tf64 / fp64_peak,
+              "flop_convention": f"{CURVE_FP64_FLOPS_PER_POINT_PAIR} FP64 flops per far point pair (ncu count, "
+                                 "CUDA's J0 and Y0 included)"}
+    line = line_base(args, world, value, m, "f32 far pairs (FP32 Hankel approximations, FP64-carried phase) + "
+                     "FP64 singular/near (mixed)", curve_config(mesh, X, {
+                         "parallelism": f"{world} independent matrices, one per rank, no collective" if world > 1
+                         else "single GPU"}),
+                     metric="segment pair-interactions/s (2-D): mixed FP32 vs plain FP64",
+                     fp64_value=world * pairs / (md * 1e-3), fp64_ms_per_step=md, mixed_over_fp64=md / m,
+                     roofline=roof, fp64_roofline=roof64, kernels_ms={"mixed": km, "fp64": kd},
+                     far_point_pairs_per_s=point_pairs / (km["far_and_gather"] * 1e-3), pairs_class=cls,
+                     clocks=clocks.summary(),
+                     gpu_launches=int(sum(s["kernel_launches"] for s in st_m)), e2e=e2e)
     line.update(out)
     print(json.dumps(line))
     return 0

@@ -269,23 +269,25 @@ typedef struct {
   int32_t near;
   int32_t singular;
 } bgb_quadstrat2d;
-/* Assemble rows [row0, row0 + nrows) of the curve operator's matrix in FP64 (the outputs may be
- * complex float); arguments, output layout, streams and errors as bgb_assemble.  stats: pairs
- * over all test segments of the rows and all trial segments, classes 0 far, 1 common vertex,
- * 3 coincident, 4 near.
+/* Assemble rows [row0, row0 + nrows) of the curve operator's matrix; arguments, output layout,
+ * streams and errors as bgb_assemble.  precision: BGB_PREC_FP64 (all FP64, CUDA's Bessel
+ * functions) or BGB_PREC_MIXED (far pairs in FP32 with polynomial Hankel approximations and the
+ * phase k R carried in FP64 per pair; coincident, common-vertex and near pairs in FP64).  stats:
+ * pairs over all test segments of the rows and all trial segments, classes 0 far, 1 common
+ * vertex, 3 coincident, 4 near.
  * Replaces: momintegrals_gpu_doubleQuad! of the 2-D prototype (doubleQuadRule_2d_gpu.jl:265-465),
  * one segment pair per call there, all pairs and the assembly here. */
 int bgb_assemble_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_curve_space* test,
-                       const bgb_curve_space* trial, const bgb_quadstrat2d* qs, void* out, int32_t out_kind,
-                       int64_t ld, int64_t row0, int64_t nrows, void* stream, bgb_stats* stats);
+                       const bgb_curve_space* trial, const bgb_quadstrat2d* qs, int32_t precision, void* out,
+                       int32_t out_kind, int64_t ld, int64_t row0, int64_t nrows, void* stream, bgb_stats* stats);
 /* Local 2x2 complex matrices of a list of segment pairs (out: double[npairs][2][2][2], host;
  * entries of absent shapes are zero) with the rule chosen by classification or forced
  * (force_class 0 far or 4 near for any pair; 1 / 3 only for pairs of that class), computed by
- * the kernels bgb_assemble_curve uses.  cls_out (optional): int8[npairs]. */
+ * the kernels bgb_assemble_curve uses for `precision`.  cls_out (optional): int8[npairs]. */
 int bgb_local_matrices_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_curve_space* test,
-                             const bgb_curve_space* trial, const bgb_quadstrat2d* qs, int64_t npairs,
-                             const int32_t* tau, const int32_t* sigma, int32_t force_class, double* out,
-                             int8_t* cls_out);
+                             const bgb_curve_space* trial, const bgb_quadstrat2d* qs, int32_t precision,
+                             int64_t npairs, const int32_t* tau, const int32_t* sigma, int32_t force_class,
+                             double* out, int8_t* cls_out);
 /* Ask a running call on this handle to stop at its next check point (BGB_ERR_ABORTED). */
 int bgb_abort(bgb_handle* h);
 

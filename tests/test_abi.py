@@ -57,7 +57,7 @@ def test_invalid_handle_is_an_error_not_a_crash(lib):
     rc = lib.bgb_assemble(None, None, None, None, None, 0, None, 0, 1, 0, -1, None, None)
     assert rc == -1
     assert b"handle" in lib.bgb_last_error()
-    rc = lib.bgb_assemble_curve(None, None, None, None, None, None, 0, 1, 0, -1, None, None)
+    rc = lib.bgb_assemble_curve(None, None, None, None, None, 0, None, 0, 1, 0, -1, None, None)
     assert rc == -1
     assert lib.bgb_destroy(None) == 0
     assert lib.bgb_abort(None) == -1

@@ -199,3 +199,47 @@ def test_oracle_rejects_bad_rules():
         oracle.local_matrices_curve(Operator2D(0, 1.0), X, X, QuadStrat2D(singular=17), [0], [0])
     with pytest.raises(RuntimeError):  # a common-vertex rule forced on a far pair
         oracle.local_matrices_curve(Operator2D(0, 1.0), X, X, QuadStrat2D(), [0], [4], force_class=1)
+
+
+def _besselfit():
+    import re
+    txt = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "beastgpu_gb300", "csrc",
+                            "besselfit.h")).read()
+    return {m.group(1): np.array([float(v.rstrip("f")) for v in m.group(2).split(",")], dtype=np.float32)
+            for m in re.finditer(r"#define BGB_BESSEL_(\w\w) \{([^}]*)\}", txt)}
+
+
+def _horner32(c, u):
+    v = np.full_like(u, c[-1])
+    for a in c[-2::-1]:
+        v = (v * u + a).astype(np.float32)
+    return v
+
+
+def test_fp32_hankel_approximations_of_the_mixed_kernels():
+    """besselfit.h evaluated in FP32 as the mixed kernels do (phase x mod 2 pi carried in FP64)
+    against scipy's Hankel functions: relative error below 1e-6 for 1e-4 <= x <= 1e5."""
+    c = _besselfit()
+    with np.errstate(all="ignore"):  # both branches are evaluated everywhere; np.where keeps the valid one
+        x = np.logspace(-4, 5, 20001)
+        xf = x.astype(np.float32)
+        phi = np.mod(x, 2 * np.pi).astype(np.float32)
+        for nu in (0, 1):
+            ref = special.hankel2(nu, x)
+            small = x < 3
+            u = (xf * xf * np.float32(1 / 9)).astype(np.float32)
+            lg = np.log(np.float32(0.5) * xf).astype(np.float32)
+            if nu == 0:
+                j = _horner32(c["P0"], u)
+                y = (np.float32(2 / np.pi) * lg * j + _horner32(c["Q0"], u)).astype(np.float32)
+            else:
+                j = (xf * _horner32(c["P1"], u)).astype(np.float32)
+                y = ((np.float32(2 / np.pi) * xf * lg * j + _horner32(c["Q1"], u)) / xf).astype(np.float32)
+            t = (np.float32(3) / xf).astype(np.float32)
+            F, G = _horner32(c[f"F{nu}"], t), _horner32(c[f"G{nu}"], t)
+            th = (phi - np.float32(np.pi / 4 * (1 + 2 * nu)) + G).astype(np.float32)
+            amp = (F / np.sqrt(xf)).astype(np.float32)
+            big = amp * (np.cos(th) - 1j * np.sin(th))
+            H = np.where(small, j - 1j * y, big)
+            err = np.abs(H - ref) / np.abs(ref)
+            assert err.max() < 1e-6, (nu, err.max(), x[np.argmax(err)])

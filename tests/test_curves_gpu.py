@@ -2,8 +2,10 @@
 bgb_local_matrices_curve through the C ABI).
 
 Bar: FP64 outputs within 1e-12 (relative Frobenius norm, and every local matrix within 1e-12
-of the oracle's), complex-float outputs within 1e-6; classes and class counts identical;
-results bit-identical from run to run and across column blocks.
+of the oracle's), complex-float outputs within 1e-6; the mixed path (FP32 far pairs) within 1e-5
+of the oracle with its coincident, common-vertex and near pairs identical to the FP64 path's;
+classes and class counts identical; results bit-identical from run to run and across column
+blocks.
 """
 import os
 
@@ -81,7 +83,8 @@ def test_distinct_test_and_trial_curves_rows_and_outputs():
     st = _lib.Stats()
     _lib.check(_lib.load().bgb_assemble_curve(h.ptr, C.byref(api.c_operator2d(op)), C.byref(api.c_curve_space(A, keep)),
                                               C.byref(api.c_curve_space(B, keep)),
-                                              C.byref(api.c_quadstrat2d(QuadStrat2D())), C.c_void_p(view.ctypes.data),
+                                              C.byref(api.c_quadstrat2d(QuadStrat2D())), _lib.PREC_FP64,
+                                              C.c_void_p(view.ctypes.data),
                                               _lib.OUT_HOST_C64, 35, 7, 20, None, C.byref(st)))
     assert rel(big[3:23], Zo[7:27]) < 1e-12
     assert np.all(big[:3] == 7 + 7j) and np.all(big[23:] == 7 + 7j)
@@ -152,3 +155,42 @@ def test_invalid_inputs_raise():
                         X.refspace, X.fn_index, X.fn_coef, X.nfun)
     with pytest.raises(bg._lib.BGBError):
         bg.assemble_gpu(Operator2D(0, 1.0), bad, bad)
+
+
+@pytest.mark.parametrize("curve", list(CURVES))
+@pytest.mark.parametrize("k", [0.0, 3.7, 40.0])
+def test_mixed_precision_matches_the_oracle(curve, k):
+    m = CURVES[curve]()
+    cfg = bg.GPUConfiguration(precision="mixed")
+    for X in (bg.curve_lagrangec0d1(m), bg.curve_lagrangecxd0(m)):
+        for op in _ops(k):
+            Z = bg.assemble_gpu(op, X, X, cfg)
+            assert Z.dtype == np.complex64
+            Zo = oracle.assemble_curve(op, X, X, QuadStrat2D())
+            assert rel(Z, Zo) < 1e-5, (curve, X, op, rel(Z, Zo))
+
+
+def test_mixed_local_matrices():
+    d = dict(np.load(FIX))
+    V = d["vertices"]
+    T = bg.curve_lagrangec0d1(bg.CurveMesh(V, d["test_segments"]), dirichlet=False)
+    B = bg.curve_lagrangec0d1(bg.CurveMesh(V, d["trial_segments"]), dirichlet=False)
+    for k in (0.0, 3.0, 10.0):
+        for kind in range(4):
+            op = Operator2D(kind, k, 0.7 - 0.2j, 1.3 + 0.4j)
+            Lm, cls = bg.local_matrices_curve(op, T, B, d["tau"], d["sigma"], precision="mixed")
+            Ld, _ = bg.local_matrices_curve(op, T, B, d["tau"], d["sigma"], precision="fp64")
+            far = cls == 0  # the near pairs of k <= 3 are far at k = 10
+            assert np.array_equal(Lm[~far], Ld[~far])  # singular and near pairs: the FP64 kernel
+            Lo, _ = oracle.local_matrices_curve(op, T, B, QuadStrat2D(), d["tau"][far], d["sigma"][far])
+            assert np.abs(Lm[far] - Lo).max() <= 1e-5 * np.abs(Lo).max(), (k, kind)
+
+
+def test_mixed_precision_at_high_frequency():
+    """k = 2 pi * 100 on 2,000 segments (k R up to 1,300): the phase is carried in FP64 per pair."""
+    X = bg.curve_lagrangec0d1(bg.ellipse(2000, 1.0, 0.5, jitter=0.2, seed=11))
+    op = bg.Helmholtz2D.hypersingular(wavenumber=2 * np.pi * 100)
+    Z = bg.assemble_gpu(op, X, X, bg.GPUConfiguration(precision="mixed"))
+    rows = np.random.default_rng(1).choice(X.nfun, 40, replace=False)
+    Zo = oracle.assemble_rows_curve(op, X, X, QuadStrat2D(), rows)
+    assert rel(Z[rows], Zo) < 1e-5
