@@ -39,11 +39,19 @@ constexpr int kMaxDepth = 16;  // bisections of a near pair
 constexpr double kInv2Pi = 0.15915494309189535;
 
 // Point rules of one call (copied to shared memory by the kernels that use them).
+constexpr int kSeries = 17;  // highest power of u = x^2/4 in the Bessel series (enough for x <= 4)
+
 struct Rules {
   int nft, nfb, nnear, nsing, ngraded, pad;
   double ft_x[kMaxGL], ft_w[kMaxGL], fb_x[kMaxGL], fb_w[kMaxGL], nr_x[kMaxGL], nr_w[kMaxGL];
   double sg_x[kMaxSing], sg_w[kMaxSing];  // Gauss-Legendre, smooth direction of the singular rules
   double gz[kMaxGraded], gwz[kMaxGraded];  // graded rule towards 0
+  double lnz[kMaxGraded];                  // ln of the graded nodes
+  double gl2_x[2], gl2_w[2];               // 2-point Gauss-Legendre (coincident pairs, across the diagonal)
+  // Power series in u = x^2/4 (Abramowitz & Stegun 9.1.10-9.1.13):
+  //   J0 = sum sa_m u^m,  Y0 = (2/pi) [(ln(x/2) + gamma) J0 + u sum sb_m u^m],
+  //   J1 = (x/2) sum sc_m u^m,  Y1 = (2/pi) ln(x/2) J1 - 2/(pi x) - (x/(2 pi)) sum sd_m u^m.
+  double sa[kSeries + 1], sb[kSeries], sc[kSeries + 1], sd[kSeries + 1];
 };
 
 struct Op {
@@ -51,6 +59,7 @@ struct Op {
   double k, k2;
   double ar, ai, br, bi;
   float khi, klo;          // k as a double-float
+  double lnk2;             // ln(k / 2), k > 0
   float far_, fai, fbr, fbi;
 };
 
@@ -163,6 +172,10 @@ __device__ __forceinline__ bool nonfar_bit(const unsigned* __restrict__ mask, in
   return (mask[idx >> 5] >> (idx & 31)) & 1u;
 }
 
+template <int OP>
+__device__ __forceinline__ void accumulate(const Op& op, const SegGeo& A, const SegGeo& B, double s, double t,
+                                           double Kr, double Ki, double w, Acc& c);
+
 // One point pair: chart parameters s (test) and t (trial), separation r = x - y, rule weight w.
 template <int OP>
 __device__ __forceinline__ void add_point(const Op& op, const SegGeo& A, const SegGeo& B, double s, double t,
@@ -192,6 +205,13 @@ __device__ __forceinline__ void add_point(const Op& op, const SegGeo& A, const S
     Kr = gr * proj;
     Ki = gi * proj;
   }
+  accumulate<OP>(op, A, B, s, t, Kr, Ki, w, c);
+}
+
+// Adds kernel value K (times the rule weight and the lengths) times the shape products.
+template <int OP>
+__device__ __forceinline__ void accumulate(const Op& op, const SegGeo& A, const SegGeo& B, double s, double t,
+                                           double Kr, double Ki, double w, Acc& c) {
   const double ww = w * A.len * B.len;
   Kr *= ww;
   Ki *= ww;
@@ -261,6 +281,88 @@ __device__ __forceinline__ double point_seg_dist2(double px, double py, double a
   return __dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey));
 }
 
+constexpr double kTwoOverPi = 0.6366197723675814, kEulerGamma = 0.5772156649015329;
+
+// The kernel at distance R with ln R given, for the singular and near rules: power series of
+// J0, Y0 (J1, Y1) up to u^M for x = k R <= 4, CUDA's Bessel functions beyond; the static kernel
+// for k = 0.  The logarithm comes from the caller (for the graded rules it is a sum of tabulated
+// logarithms), so most points need no transcendental function.
+template <int OP>
+__device__ __forceinline__ void kernel_series(const Op& op, const Rules& Rl, double R, double lnR, int M, double rx,
+                                              double ry, const SegGeo& A, const SegGeo& B, double& Kr, double& Ki) {
+  if (OP == BGB_OP2D_SL || OP == BGB_OP2D_HS) {
+    if (op.k == 0.0) {
+      Kr = -kInv2Pi * lnR;
+      Ki = 0.0;
+      return;
+    }
+    const double x = op.k * R;
+    if (x <= 4.0) {
+      const double u = 0.25 * x * x;
+      double j0 = Rl.sa[M];
+      for (int m = M - 1; m >= 0; --m) j0 = fma(j0, u, Rl.sa[m]);
+      double s0 = Rl.sb[M - 1];
+      for (int m = M - 2; m >= 0; --m) s0 = fma(s0, u, Rl.sb[m]);
+      const double y0v = kTwoOverPi * fma(lnR + op.lnk2 + kEulerGamma, j0, s0 * u);
+      Kr = -0.25 * y0v;
+      Ki = -0.25 * j0;
+    } else {
+      Kr = -0.25 * y0(x);
+      Ki = -0.25 * j0(x);
+    }
+    return;
+  }
+  double gr, gi;
+  if (op.k == 0.0) {
+    gr = -kInv2Pi / (R * R);
+    gi = 0.0;
+  } else {
+    const double x = op.k * R;
+    double j1v, y1v;
+    if (x <= 4.0) {
+      const double u = 0.25 * x * x;
+      double c1 = Rl.sc[M], d1 = Rl.sd[M];
+      for (int m = M - 1; m >= 0; --m) {
+        c1 = fma(c1, u, Rl.sc[m]);
+        d1 = fma(d1, u, Rl.sd[m]);
+      }
+      j1v = 0.5 * x * c1;
+      y1v = kTwoOverPi * (lnR + op.lnk2) * j1v - kTwoOverPi / x - x * kInv2Pi * d1;
+    } else {
+      j1v = j1(x);
+      y1v = y1(x);
+    }
+    const double f = op.k / (4.0 * R);
+    gr = f * y1v;
+    gi = f * j1v;
+  }
+  const double proj = OP == BGB_OP2D_DL ? -(rx * B.nx + ry * B.ny) : rx * A.nx + ry * A.ny;
+  Kr = gr * proj;
+  Ki = gi * proj;
+}
+
+// Series order for a pair whose points are at most Rmax apart: the smallest M with
+// u^M / (M!)^2 < 1e-18 at u = (k Rmax / 2)^2 (all of kSeries when k Rmax > 4).
+__device__ __forceinline__ int series_order(double k, double Rmax) {
+  const double u = 0.25 * (k * Rmax) * (k * Rmax);
+  if (u >= 4.0) return kSeries;
+  double term = 1.0;
+  int M = 1;
+  for (; M < kSeries; ++M) {
+    term *= u / ((double)M * M);
+    if (term < 1e-18) break;
+  }
+  return M;
+}
+
+__device__ __forceinline__ double max_vertex_distance(const SegGeo& A, const SegGeo& B) {
+  const double ax[2] = {A.x0, A.x1}, ay[2] = {A.y0, A.y1}, bx[2] = {B.x0, B.x1}, by[2] = {B.y0, B.y1};
+  double m = 0.0;
+  for (int i = 0; i < 2; ++i)
+    for (int j = 0; j < 2; ++j) m = fmax(m, (ax[i] - bx[j]) * (ax[i] - bx[j]) + (ay[i] - by[j]) * (ay[i] - by[j]));
+  return sqrt(m);
+}
+
 // Warp-cooperative rules: every lane runs the same control flow and integrates the points
 // k = lane, lane + 32, ... of each rule; the partial sums are reduced by the caller.
 template <int OP>
@@ -273,6 +375,7 @@ __device__ void near_rule_warp(const Op& op, const Rules& R, const SegGeo& A, co
   int top = 0;
   stack[top++] = Box{0.0, 1.0, 0.0, 1.0, 0};
   const int n = R.nnear;
+  const int M = series_order(op.k, max_vertex_distance(A, B));
   while (top > 0) {
     const Box b = stack[--top];
     const double p0x = __dadd_rn(A.x0, __dmul_rn(b.s0, A.dx)), p0y = __dadd_rn(A.y0, __dmul_rn(b.s0, A.dy));
@@ -301,7 +404,10 @@ __device__ void near_rule_warp(const Op& op, const Rules& R, const SegGeo& A, co
       const int p = k / n, q = k - p * n;
       const double s = b.s0 + hs * R.nr_x[p], t = b.t0 + ht * R.nr_x[q];
       const double rx = (A.x0 + s * A.dx) - (B.x0 + t * B.dx), ry = (A.y0 + s * A.dy) - (B.y0 + t * B.dy);
-      add_point<OP>(op, A, B, s, t, rx, ry, (hs * R.nr_w[p]) * (ht * R.nr_w[q]), c);
+      const double Rd = sqrt(rx * rx + ry * ry);
+      double Kr, Ki;
+      kernel_series<OP>(op, R, Rd, log(Rd), M, rx, ry, A, B, Kr, Ki);
+      accumulate<OP>(op, A, B, s, t, Kr, Ki, (hs * R.nr_w[p]) * (ht * R.nr_w[q]), c);
     }
   }
 }
@@ -310,26 +416,45 @@ __device__ void near_rule_warp(const Op& op, const Rules& R, const SegGeo& A, co
 // split along its diagonal, graded coordinate z towards the singularity, Gauss coordinate w.
 template <int OP>
 __device__ void singular_rule_warp(const Op& op, const Rules& R, const SegGeo& A, const SegGeo& B, int cls,
-                                   int match, int lane, Acc& c) {
+                                   int match, int lane, double* __restrict__ wtab, Acc& c) {
   const int n = R.nsing, nz = R.ngraded, per_half = nz * n;
+  const int M = series_order(op.k, max_vertex_distance(A, B));
   if (cls == 3) {
     if (OP == BGB_OP2D_DL || OP == BGB_OP2D_DLT) return;  // r lies along the segment
     const bool same = match == 0;
-    for (int k = lane; k < 2 * per_half; k += 32) {
-      const int half = k >= per_half;
-      const int rem = k - half * per_half, a = rem / n, b = rem - a * n;
-      const double z = R.gz[a], w = R.sg_x[b];
+    const double lnl = log(A.len);  // R = z l
+    // R depends on z only: across the diagonal the integrand is the product of two shapes linear
+    // in w, which the 2-point Gauss rule integrates exactly
+    const int ch = nz * 2;
+    for (int k = lane; k < 2 * ch; k += 32) {
+      const int half = k >= ch;
+      const int rem = k - half * ch, a = rem >> 1, b = rem & 1;
+      const double z = R.gz[a], w = R.gl2_x[b];
       double u, v, uv;
       if (!half) { u = z + (1.0 - z) * w; v = (1.0 - z) * w; uv = z; }
       else { u = (1.0 - z) * w; v = z + (1.0 - z) * w; uv = -z; }
-      const double wt = R.gwz[a] * R.sg_w[b] * (1.0 - z);
-      add_point<OP>(op, A, B, u, same ? v : 1.0 - v, uv * A.dx, uv * A.dy, wt, c);
+      const double wt = R.gwz[a] * R.gl2_w[b] * (1.0 - z);
+      double Kr, Ki;
+      kernel_series<OP>(op, R, z * A.len, R.lnz[a] + lnl, M, uv * A.dx, uv * A.dy, A, B, Kr, Ki);
+      accumulate<OP>(op, A, B, u, same ? v : 1.0 - v, Kr, Ki, wt, c);
     }
     return;
   }
   const int ma = match >> 1, mb = match & 1;
   const double ax = ma == 0 ? A.dx : -A.dx, ay = ma == 0 ? A.dy : -A.dy;
   const double bx = mb == 0 ? B.dx : -B.dx, by = mb == 0 ? B.dy : -B.dy;
+  // R = z |a - w b| (first half) or z |w a - b| (second half): the lengths and their logarithms per
+  // Gauss node w, one lane each, in this warp's table
+  if (lane < n) {
+    const double w = R.sg_x[lane];
+    const double l0 = sqrt((ax - w * bx) * (ax - w * bx) + (ay - w * by) * (ay - w * by));
+    const double l1 = sqrt((w * ax - bx) * (w * ax - bx) + (w * ay - by) * (w * ay - by));
+    wtab[lane] = l0;
+    wtab[kMaxSing + lane] = log(l0);
+    wtab[2 * kMaxSing + lane] = l1;
+    wtab[3 * kMaxSing + lane] = log(l1);
+  }
+  __syncwarp();
   for (int k = lane; k < 2 * per_half; k += 32) {
     const int half = k >= per_half;
     const int rem = k - half * per_half, a = rem / n, b = rem - a * n;
@@ -338,9 +463,13 @@ __device__ void singular_rule_warp(const Op& op, const Rules& R, const SegGeo& A
     if (!half) { xi = z; eta = z * w; }
     else { xi = z * w; eta = z; }
     const double wt = R.gwz[a] * R.sg_w[b] * z;
-    add_point<OP>(op, A, B, ma == 0 ? xi : 1.0 - xi, mb == 0 ? eta : 1.0 - eta, xi * ax - eta * bx,
-                  xi * ay - eta * by, wt, c);
+    const double* tb = wtab + 2 * kMaxSing * half;
+    double Kr, Ki;
+    kernel_series<OP>(op, R, z * tb[b], R.lnz[a] + tb[kMaxSing + b], M, xi * ax - eta * bx, xi * ay - eta * by, A, B,
+                      Kr, Ki);
+    accumulate<OP>(op, A, B, ma == 0 ? xi : 1.0 - xi, mb == 0 ? eta : 1.0 - eta, Kr, Ki, wt, c);
   }
+  __syncwarp();
 }
 
 // ---- Mixed precision: FP32 point pairs, the phase k R carried in FP64 per pair --------------
@@ -645,6 +774,7 @@ __global__ void __launch_bounds__(256) k_curve_special(Op op, const Rules* __res
                                                        const SegGeo* __restrict__ gT, const SegGeo* __restrict__ gB,
                                                        const Special* __restrict__ list, int n, LT* __restrict__ L) {
   __shared__ Rules sR;
+  __shared__ double wtabs[8][4 * kMaxSing];  // per warp: common-vertex lengths and logarithms
   {
     const int* src = (const int*)rules;
     int* dst = (int*)&sR;
@@ -652,6 +782,7 @@ __global__ void __launch_bounds__(256) k_curve_special(Op op, const Rules* __res
   }
   __syncthreads();
   const int lane = threadIdx.x & 31;
+  double* wtab = wtabs[threadIdx.x >> 5];
   const int nwarps = gridDim.x * (blockDim.x >> 5);
   for (int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < n; e += nwarps) {
     const Special sp = list[e];
@@ -659,7 +790,7 @@ __global__ void __launch_bounds__(256) k_curve_special(Op op, const Rules* __res
     Acc c;
     acc_zero(c);
     if (sp.cls == 4) near_rule_warp<OP>(op, sR, A, B, lane, c);
-    else singular_rule_warp<OP>(op, sR, A, B, sp.cls, sp.match, lane, c);
+    else singular_rule_warp<OP>(op, sR, A, B, sp.cls, sp.match, lane, wtab, c);
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       c.pr[k] = warp_sum(c.pr[k]);
@@ -811,6 +942,7 @@ static int make_op(const bgb_operator2d* op, const bgb_curve_space* a, const bgb
   o.ai = op->alpha[1];
   o.br = op->beta[0];
   o.bi = op->beta[1];
+  o.lnk2 = o.k > 0.0 ? std::log(0.5 * o.k) : 0.0;
   o.khi = (float)o.k;
   o.klo = (float)(o.k - (double)o.khi);
   o.far_ = (float)o.ar;
@@ -851,6 +983,25 @@ static int make_rules(const bgb_quadstrat2d* qs, Rules* R) {
     }
   }
   R->ngraded = k;
+  for (int i = 0; i < k; ++i) R->lnz[i] = std::log(R->gz[i]);
+  gauss_legendre01(2, R->gl2_x, R->gl2_w);
+  // series coefficients (A&S 9.1.10-9.1.13): factorials and harmonic numbers in FP64
+  double fact = 1.0, H = 0.0;  // m!, H_m
+  for (int m = 0; m <= kSeries; ++m) {
+    if (m > 0) {
+      fact *= m;
+      H += 1.0 / m;
+    }
+    const double sign = (m % 2) ? -1.0 : 1.0;
+    const double H1 = H + 1.0 / (m + 1);
+    R->sa[m] = sign / (fact * fact);
+    R->sc[m] = sign / (fact * fact * (m + 1));
+    R->sd[m] = sign * (H + H1 - 2.0 * 0.5772156649015329) / (fact * fact * (m + 1));
+    if (m < kSeries) {
+      const double f1 = fact * (m + 1);  // (m+1)!
+      R->sb[m] = sign * H1 / (f1 * f1);  // coefficient of u^(m+1): (-1)^m H_{m+1} / ((m+1)!)^2
+    }
+  }
   return 0;
 }
 
