@@ -35,6 +35,7 @@ struct SegGeo {
 constexpr int kMaxGL = 32;
 constexpr int kMaxSing = 16;
 constexpr int kMaxGraded = (3 * kMaxSing + 1) * kMaxSing;
+constexpr int kMaxGradedCv = ((3 * kMaxSing) / 2 + 1) * kMaxSing;
 constexpr int kMaxDepth = 16;  // bisections of a near pair
 constexpr double kInv2Pi = 0.15915494309189535;
 
@@ -45,8 +46,10 @@ struct Rules {
   int nft, nfb, nnear, nsing, ngraded, pad;
   double ft_x[kMaxGL], ft_w[kMaxGL], fb_x[kMaxGL], fb_w[kMaxGL], nr_x[kMaxGL], nr_w[kMaxGL];
   double sg_x[kMaxSing], sg_w[kMaxSing];  // Gauss-Legendre, smooth direction of the singular rules
-  double gz[kMaxGraded], gwz[kMaxGraded];  // graded rule towards 0
+  double gz[kMaxGraded], gwz[kMaxGraded];  // graded rule towards 0 (coincident pairs: 3n levels)
   double lnz[kMaxGraded];                  // ln of the graded nodes
+  int ngraded_cv, pad2;                    // common-vertex pairs (integrand ~ z ln z): 3n/2 levels
+  double gz_cv[kMaxGradedCv], gwz_cv[kMaxGradedCv], lnz_cv[kMaxGradedCv];
   double gl2_x[2], gl2_w[2];               // 2-point Gauss-Legendre (coincident pairs, across the diagonal)
   // Power series in u = x^2/4 (Abramowitz & Stegun 9.1.10-9.1.13):
   //   J0 = sum sa_m u^m,  Y0 = (2/pi) [(ln(x/2) + gamma) J0 + u sum sb_m u^m],
@@ -417,7 +420,7 @@ __device__ void near_rule_warp(const Op& op, const Rules& R, const SegGeo& A, co
 template <int OP>
 __device__ void singular_rule_warp(const Op& op, const Rules& R, const SegGeo& A, const SegGeo& B, int cls,
                                    int match, int lane, double* __restrict__ wtab, Acc& c) {
-  const int n = R.nsing, nz = R.ngraded, per_half = nz * n;
+  const int n = R.nsing, nz = R.ngraded;
   const int M = series_order(op.k, max_vertex_distance(A, B));
   if (cls == 3) {
     if (OP == BGB_OP2D_DL || OP == BGB_OP2D_DLT) return;  // r lies along the segment
@@ -455,18 +458,19 @@ __device__ void singular_rule_warp(const Op& op, const Rules& R, const SegGeo& A
     wtab[3 * kMaxSing + lane] = log(l1);
   }
   __syncwarp();
-  for (int k = lane; k < 2 * per_half; k += 32) {
-    const int half = k >= per_half;
-    const int rem = k - half * per_half, a = rem / n, b = rem - a * n;
-    const double z = R.gz[a], w = R.sg_x[b];
+  const int per_half_cv = R.ngraded_cv * n;  // ngraded_cv z nodes times n Gauss nodes
+  for (int k = lane; k < 2 * per_half_cv; k += 32) {
+    const int half = k >= per_half_cv;
+    const int rem = k - half * per_half_cv, a = rem / n, b = rem - a * n;
+    const double z = R.gz_cv[a], w = R.sg_x[b];
     double xi, eta;
     if (!half) { xi = z; eta = z * w; }
     else { xi = z * w; eta = z; }
-    const double wt = R.gwz[a] * R.sg_w[b] * z;
+    const double wt = R.gwz_cv[a] * R.sg_w[b] * z;
     const double* tb = wtab + 2 * kMaxSing * half;
     double Kr, Ki;
-    kernel_series<OP>(op, R, z * tb[b], R.lnz[a] + tb[kMaxSing + b], M, xi * ax - eta * bx, xi * ay - eta * by, A, B,
-                      Kr, Ki);
+    kernel_series<OP>(op, R, z * tb[b], R.lnz_cv[a] + tb[kMaxSing + b], M, xi * ax - eta * bx, xi * ay - eta * by, A,
+                      B, Kr, Ki);
     accumulate<OP>(op, A, B, ma == 0 ? xi : 1.0 - xi, mb == 0 ? eta : 1.0 - eta, Kr, Ki, wt, c);
   }
   __syncwarp();
@@ -971,19 +975,24 @@ static int make_rules(const bgb_quadstrat2d* qs, Rules* R) {
   gauss_legendre01(R->nnear, R->nr_x, R->nr_w);
   const int n = R->nsing;
   gauss_legendre01(n, R->sg_x, R->sg_w);
-  // graded rule: [0, q^(3n)] then [q^(lev+1), q^lev] for lev = 3n - 1 .. 0, n Gauss points each
+  // graded rules: [0, q^L] then [q^(lev+1), q^lev] for lev = L - 1 .. 0, n Gauss points each;
+  // L = 3n for coincident pairs (ln z), 3n/2 for common-vertex pairs (z ln z)
   const double q = 0.35;
-  int k = 0;
-  for (int lev = 3 * n; lev >= 0; --lev) {
-    const double a = lev == 3 * n ? 0.0 : std::pow(q, lev + 1), b = std::pow(q, lev);
-    for (int i = 0; i < n; ++i) {
-      R->gz[k] = a + (b - a) * R->sg_x[i];
-      R->gwz[k] = (b - a) * R->sg_w[i];
-      ++k;
+  auto graded = [&](int levels, double* gz, double* gwz, double* lnz) {
+    int k = 0;
+    for (int lev = levels; lev >= 0; --lev) {
+      const double a = lev == levels ? 0.0 : std::pow(q, lev + 1), b = std::pow(q, lev);
+      for (int i = 0; i < n; ++i) {
+        gz[k] = a + (b - a) * R->sg_x[i];
+        gwz[k] = (b - a) * R->sg_w[i];
+        lnz[k] = std::log(gz[k]);
+        ++k;
+      }
     }
-  }
-  R->ngraded = k;
-  for (int i = 0; i < k; ++i) R->lnz[i] = std::log(R->gz[i]);
+    return k / n;
+  };
+  R->ngraded = graded(3 * n, R->gz, R->gwz, R->lnz) * n;
+  R->ngraded_cv = graded((3 * n) / 2, R->gz_cv, R->gwz_cv, R->lnz_cv) * n;
   gauss_legendre01(2, R->gl2_x, R->gl2_w);
   // series coefficients (A&S 9.1.10-9.1.13): factorials and harmonic numbers in FP64
   double fact = 1.0, H = 0.0;  // m!, H_m

@@ -57,15 +57,15 @@ int orc2_green(double k, double R, double* out) {
   return 0;
 }
 
-int orc2_graded01(int32_t n, double* x, double* w) {
-  if (n < 1 || n > 16 || !x || !w) return -1;
+/* Graded rule on [0, 1] towards 0 with `levels` geometric levels (ratio 0.35): the intervals
+ * [0, q^levels], [q^levels, q^(levels-1)], ..., [q, 1], n Gauss-Legendre points each, ascending. */
+static int graded_levels(int n, int levels, double* x, double* w) {
   const double q = 0.35;
   double gx[16], gw[16];
-  if (orc_gauss_legendre01(n, gx, gw)) return -1;
+  if (n < 1 || n > 16 || orc_gauss_legendre01(n, gx, gw)) return -1;
   int k = 0;
-  for (int lev = 3 * n; lev >= 0; --lev) {
-    /* [0, q^(3n)] first, then [q^(lev+1), q^lev] */
-    const double a = (lev == 3 * n) ? 0.0 : pow(q, lev + 1);
+  for (int lev = levels; lev >= 0; --lev) {
+    const double a = (lev == levels) ? 0.0 : pow(q, lev + 1);
     const double b = pow(q, lev);
     for (int i = 0; i < n; ++i) {
       x[k] = a + (b - a) * gx[i];
@@ -74,6 +74,11 @@ int orc2_graded01(int32_t n, double* x, double* w) {
     }
   }
   return 0;
+}
+
+int orc2_graded01(int32_t n, double* x, double* w) {
+  if (n < 1 || n > 16 || !x || !w) return -1;
+  return graded_levels(n, 3 * n, x, w);
 }
 
 /* ------------------------------------------------------------------------------------ */
@@ -295,9 +300,12 @@ static int near_rule(acc_t* c, int n) {
 }
 
 static int singular_rule(acc_t* c, int cls, int ma, int mb, int n) {
+  /* coincident pairs: ln z integrands, 3n levels; common-vertex pairs carry the Jacobian z
+   * (z ln z), for which 3n/2 levels reach the same accuracy */
+  const int levels = cls == ORC2_CLASS_CF ? 3 * n : (3 * n) / 2;
   double gz[49 * 16], gwz[49 * 16], gx[16], gw[16];
-  if (orc2_graded01(n, gz, gwz) || orc_gauss_legendre01(n, gx, gw)) return -1;
-  const int nz = (3 * n + 1) * n;
+  if (graded_levels(n, levels, gz, gwz) || orc_gauss_legendre01(n, gx, gw)) return -1;
+  const int nz = (levels + 1) * n;
   const seg_t *A = c->A, *B = c->B;
   if (cls == ORC2_CLASS_CF) {
     /* same straight segment: double layers vanish (r is along the segment) */

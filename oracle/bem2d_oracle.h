@@ -48,6 +48,8 @@
  *   coincident (u, v in the test chart, singular on u = v): u = z + (1-z) w, v = (1-z) w and
  *   the mirror, weight (1 - z);  common vertex (xi, eta from the shared vertex, singular at
  *   the corner): xi = z, eta = z w and the mirror, weight z;  z graded, w Gauss-Legendre.
+ *   The coincident rule grades z over 3n levels (orc2_graded01); the common-vertex rule, whose
+ *   integrand carries the Jacobian z (z ln z), over 3n/2 levels (integer division).
  * Double layers vanish on coincident (straight) segments.
  */
 #ifndef BEM2D_ORACLE_H
