@@ -159,15 +159,17 @@ __device__ __forceinline__ int classify(const SegGeo& a, const SegGeo& b, double
 
 // True only for pairs the exact predicate classifies far: a lower bound of the least vertex
 // distance (midpoint distance minus the half lengths, less a bound of its FP32 rounding) already
-// passes the far thresholds with a margin of 0.25%.  Pairs it does not settle go to classify().
-__device__ __forceinline__ bool certainly_far(const SegGeo& A, const SegGeo& B, float k2f) {
-  const float dx = (float)(A.cx - B.cx), dy = (float)(A.cy - B.cy);
+// passes the far thresholds with a margin of 0.25%.  All FP32: the midpoints are double-float
+// (SegF), so their difference is accurate to a few units of FP32 rounding of the distance.
+// Pairs it does not settle go to classify().
+__device__ __forceinline__ bool certainly_far(const SegF& A, const SegF& B, float k2f) {
+  const float dx = (A.cxh - B.cxh) + (A.cxl - B.cxl), dy = (A.cyh - B.cyh) + (A.cyl - B.cyl);
   const float dc = sqrtf(fmaf(dx, dx, dy * dy));
-  const float hs = 0.5f * ((float)A.len + (float)B.len);
+  const float hs = 0.5f * (A.len + B.len);
   const float dlb = (dc - hs) - 4e-7f * (dc + hs);
   if (!(dlb > 1e-12f)) return false;
   const float d2 = dlb * dlb;
-  return d2 * k2f >= 0.0401f || d2 >= 0.0401f * 16.f * (float)B.len;
+  return d2 * k2f >= 0.0401f || d2 >= 0.0401f * 16.f * B.len;
 }
 
 // Non-far mask: bit (sl * nT + tl) set for pairs the far kernels skip.
@@ -685,17 +687,18 @@ __device__ __forceinline__ double warp_sum(double v) {
 // counts[0]: list length, [1]: degenerate-pair flag, [2 + class]: non-far pairs of owned columns;
 // mask: bit (sl * nT + tl) set for every non-far pair.
 __global__ void __launch_bounds__(256) k_curve_classify(const SegGeo* __restrict__ gT, const SegGeo* __restrict__ gB,
+                                                        const SegF* __restrict__ gTf, const SegF* __restrict__ gBf,
                                                         const int* __restrict__ T, int nT, const int* __restrict__ S,
                                                         int nS, const unsigned char* __restrict__ own, double k2,
                                                         int LS, Special* __restrict__ list, int cap,
                                                         int* __restrict__ counts, unsigned* __restrict__ mask) {
   const int tl = blockIdx.x * blockDim.x + threadIdx.x;
   if (tl >= nT) return;
-  const SegGeo A = gT[T[tl]];
+  const SegF Af = gTf[T[tl]];
   const float k2f = (float)k2;
   for (int sl = blockIdx.y; sl < nS; sl += gridDim.y) {
-    const SegGeo B = gB[S[sl]];
-    if (certainly_far(A, B, k2f)) continue;
+    if (certainly_far(Af, gBf[S[sl]], k2f)) continue;
+    const SegGeo A = gT[T[tl]], B = gB[S[sl]];
     int match;
     const int cls = classify(A, B, k2, &match);
     if (cls == 0) continue;
@@ -1236,7 +1239,8 @@ int bgb_assemble_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_curve_
         BGB_CUDA(cudaMemsetAsync(B.mask.p, 0, mask_bytes, s));
         BGB_CUDA(cudaEventRecord(h->ev[0], s));
         dim3 grid((nT + 255) / 256, std::min(nS, 65535));
-        k_curve_classify<<<grid, 256, 0, s>>>(B.geo_t.as<SegGeo>(), B.geo_b.as<SegGeo>(), B.T.as<int>(), nT, B.S.as<int>(),
+        k_curve_classify<<<grid, 256, 0, s>>>(B.geo_t.as<SegGeo>(), B.geo_b.as<SegGeo>(), B.geof_t.as<SegF>(),
+                                              B.geof_b.as<SegF>(), B.T.as<int>(), nT, B.S.as<int>(),
                                               nS, B.own.as<unsigned char>(), o.k2, o.LS, B.list.as<Special>(), cap,
                                               B.counts.as<int>(), B.mask.as<unsigned>());
         BGB_CUDA(cudaGetLastError());
