@@ -57,6 +57,17 @@ struct Rules {
   double sa[kSeries + 1], sb[kSeries], sc[kSeries + 1], sd[kSeries + 1];
 };
 
+// The singular rules and series of Rules as double-floats, for the mixed path's singular kernel:
+// weights pre-multiplied by the collapse Jacobians ((1 - z) coincident, z common vertex).
+struct RulesDF {
+  int n, nz, nzcv, pad;
+  dfl gz[kMaxGraded], wcf[kMaxGraded], lnz[kMaxGraded];
+  dfl gzc[kMaxGradedCv], wcv[kMaxGradedCv], lnzc[kMaxGradedCv];
+  dfl sgx[kMaxSing], sgw[kMaxSing], gl2x[2], gl2w[2];
+  dfl sa[kSeries + 1], sb[kSeries];
+  dfl inv2pi, two_over_pi;
+};
+
 struct Op {
   int kind, nsA, nsB, LS;  // LS = nsA * nsB entries per local matrix
   double k, k2;
@@ -809,6 +820,180 @@ __global__ void __launch_bounds__(256) k_curve_special(Op op, const Rules* __res
   }
 }
 
+// ---- Mixed path: coincident and common-vertex pairs in double-float ---------------------------
+// The FP64 rules and series of singular_rule_warp / kernel_series evaluated with double-float
+// arithmetic on the FP32 pipes (about 48 bits), single and hypersingular kernels (the double layers
+// keep the FP64 kernel).  Each lane sums the kernel times the weight into four moments
+// (1, s, t, s t), from which the shape products follow.
+struct DfMom {
+  dfl r[4], i[4];  // sum of K w, K w s, K w t, K w s t
+};
+
+__device__ __forceinline__ dfl df_scale(dfl a, float f) { return dfl{a.hi * f, a.lo * f}; }  // f a power of 2
+
+template <int OP>
+__device__ __forceinline__ void df_point(const Op& op, const RulesDF& R, dfl Rd, dfl lnR, int M, dfl lnk2g, dfl wl,
+                                         dfl s, dfl t, DfMom& mo) {
+  dfl Kr, Ki;
+  if (op.khi == 0.f) {
+    Kr = df_neg(df_mul(R.inv2pi, lnR));
+    Ki = dfl{0.f, 0.f};
+  } else {
+    const dfl x = df_mul(Rd, dfl{op.khi, op.klo});
+    if (x.hi <= 4.f) {
+      const dfl u = df_scale(df_mul(x, x), 0.25f);
+      dfl j0 = R.sa[M];
+      for (int m = M - 1; m >= 0; --m) j0 = df_add(df_mul(j0, u), R.sa[m]);
+      dfl s0 = R.sb[M - 1];
+      for (int m = M - 2; m >= 0; --m) s0 = df_add(df_mul(s0, u), R.sb[m]);
+      const dfl y0v = df_mul(R.two_over_pi, df_add(df_mul(df_add(lnR, lnk2g), j0), df_mul(s0, u)));
+      Kr = df_scale(y0v, -0.25f);
+      Ki = df_scale(j0, -0.25f);
+    } else {
+      const double xd = df_to_double(x);
+      const double yr = -0.25 * y0(xd), yi = -0.25 * j0(xd);
+      Kr.hi = (float)yr;
+      Kr.lo = (float)(yr - (double)Kr.hi);
+      Ki.hi = (float)yi;
+      Ki.lo = (float)(yi - (double)Ki.hi);
+    }
+  }
+  const dfl kwr = df_mul(Kr, wl), kwi = df_mul(Ki, wl);
+  const dfl st = df_mul(s, t);
+  mo.r[0] = df_add(mo.r[0], kwr);
+  mo.i[0] = df_add(mo.i[0], kwi);
+  mo.r[1] = df_add(mo.r[1], df_mul(kwr, s));
+  mo.i[1] = df_add(mo.i[1], df_mul(kwi, s));
+  mo.r[2] = df_add(mo.r[2], df_mul(kwr, t));
+  mo.i[2] = df_add(mo.i[2], df_mul(kwi, t));
+  mo.r[3] = df_add(mo.r[3], df_mul(kwr, st));
+  mo.i[3] = df_add(mo.i[3], df_mul(kwi, st));
+}
+
+__device__ __forceinline__ dfl df_from_double(double v) {
+  const float h = (float)v;
+  return dfl{h, (float)(v - (double)h)};
+}
+
+template <int OP>
+__device__ void singular_rule_warp_df(const Op& op, const RulesDF& R, const SegGeo& A, const SegGeo& B, int cls,
+                                      int match, int lane, dfl* __restrict__ wtab, DfMom& mo) {
+  const int n = R.n;
+  const int M = series_order(op.k, max_vertex_distance(A, B));
+  const dfl lnk2g = df_from_double(op.lnk2 + kEulerGamma);
+  const dfl ll = df_from_double(A.len * B.len);
+  const dfl one{1.f, 0.f};
+  if (cls == 3) {
+    const bool same = match == 0;
+    const dfl lA = df_from_double(A.len), lnl = df_from_double(log(A.len));
+    const int ch = R.nz * 2;
+    for (int k = lane; k < 2 * ch; k += 32) {
+      const int half = k >= ch;
+      const int rem = k - half * ch, a = rem >> 1, b = rem & 1;
+      const dfl z = R.gz[a], w = R.gl2x[b];
+      const dfl t1 = df_mul(df_sub(one, z), w);  // (1 - z) w
+      const dfl u = half ? t1 : df_add(z, t1), v = half ? df_add(z, t1) : t1;
+      const dfl wl = df_mul(df_mul(R.wcf[a], R.gl2w[b]), ll);
+      df_point<OP>(op, R, df_mul(z, lA), df_add(R.lnz[a], lnl), M, lnk2g, wl, u, same ? v : df_sub(one, v), mo);
+    }
+    return;
+  }
+  const int ma = match >> 1, mb = match & 1;
+  const double ax = ma == 0 ? A.dx : -A.dx, ay = ma == 0 ? A.dy : -A.dy;
+  const double bx = mb == 0 ? B.dx : -B.dx, by = mb == 0 ? B.dy : -B.dy;
+  if (lane < n) {
+    const double w = (double)R.sgx[lane].hi + (double)R.sgx[lane].lo;
+    const double l0 = sqrt((ax - w * bx) * (ax - w * bx) + (ay - w * by) * (ay - w * by));
+    const double l1 = sqrt((w * ax - bx) * (w * ax - bx) + (w * ay - by) * (w * ay - by));
+    wtab[lane] = df_from_double(l0);
+    wtab[kMaxSing + lane] = df_from_double(log(l0));
+    wtab[2 * kMaxSing + lane] = df_from_double(l1);
+    wtab[3 * kMaxSing + lane] = df_from_double(log(l1));
+  }
+  __syncwarp();
+  const int per_half = R.nzcv * n;
+  for (int k = lane; k < 2 * per_half; k += 32) {
+    const int half = k >= per_half;
+    const int rem = k - half * per_half, a = rem / n, b = rem - a * n;
+    const dfl z = R.gzc[a], zw = df_mul(z, R.sgx[b]);
+    const dfl xi = half ? zw : z, eta = half ? z : zw;
+    const dfl* tb = wtab + 2 * kMaxSing * half;
+    const dfl wl = df_mul(df_mul(R.wcv[a], R.sgw[b]), ll);
+    df_point<OP>(op, R, df_mul(z, tb[b]), df_add(R.lnzc[a], tb[kMaxSing + b]), M, lnk2g, wl,
+                 ma == 0 ? xi : df_sub(one, xi), mb == 0 ? eta : df_sub(one, eta), mo);
+  }
+  __syncwarp();
+}
+
+__device__ __forceinline__ dfl warp_sum_df(dfl v) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const dfl o{__shfl_xor_sync(0xffffffffu, v.hi, off), __shfl_xor_sync(0xffffffffu, v.lo, off)};
+    v = df_add(v, o);
+  }
+  return v;
+}
+
+// Mixed path, single layer and hypersingular: coincident and common-vertex pairs in double-float,
+// near pairs by the FP64 rule (rules read from global memory).
+template <int OP, class LT>
+__global__ void __launch_bounds__(256) k_curve_special_df(Op op, const Rules* __restrict__ rules,
+                                                          const RulesDF* __restrict__ rdf,
+                                                          const SegGeo* __restrict__ gT, const SegGeo* __restrict__ gB,
+                                                          const Special* __restrict__ list, int n, LT* __restrict__ L) {
+  __shared__ RulesDF sR;
+  __shared__ dfl wtabs[8][4 * kMaxSing];
+  {
+    const int* src = (const int*)rdf;
+    int* dst = (int*)&sR;
+    for (int i = threadIdx.x; i < (int)(sizeof(RulesDF) / sizeof(int)); i += blockDim.x) dst[i] = src[i];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  dfl* wtab = wtabs[threadIdx.x >> 5];
+  const int nwarps = gridDim.x * (blockDim.x >> 5);
+  for (int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < n; e += nwarps) {
+    const Special sp = list[e];
+    const SegGeo A = gT[sp.tau], B = gB[sp.sigma];
+    Acc c;
+    acc_zero(c);
+    if (sp.cls == 4) {
+      near_rule_warp<OP>(op, *rules, A, B, lane, c);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        c.pr[k] = warp_sum(c.pr[k]);
+        c.pi[k] = warp_sum(c.pi[k]);
+      }
+      c.mr = warp_sum(c.mr);
+      c.mi = warp_sum(c.mi);
+    } else {
+      DfMom mo;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) mo.r[k] = mo.i[k] = dfl{0.f, 0.f};
+      singular_rule_warp_df<OP>(op, sR, A, B, sp.cls, sp.match, lane, wtab, mo);
+      double mr[4], mi[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        mr[k] = df_to_double(warp_sum_df(mo.r[k]));
+        mi[k] = df_to_double(warp_sum_df(mo.i[k]));
+      }
+      // shape products from the moments: f = (1 - s, s) or 1, g = (1 - t, t) or 1
+      const bool hA = op.nsA == 2, hB = op.nsB == 2;
+      c.pr[0] = mr[0] - (hA ? mr[1] : 0.0) - (hB ? mr[2] : 0.0) + (hA && hB ? mr[3] : 0.0);
+      c.pi[0] = mi[0] - (hA ? mi[1] : 0.0) - (hB ? mi[2] : 0.0) + (hA && hB ? mi[3] : 0.0);
+      c.pr[1] = mr[2] - (hA ? mr[3] : 0.0);
+      c.pi[1] = mi[2] - (hA ? mi[3] : 0.0);
+      c.pr[2] = mr[1] - (hB ? mr[3] : 0.0);
+      c.pi[2] = mi[1] - (hB ? mi[3] : 0.0);
+      c.pr[3] = mr[3];
+      c.pi[3] = mi[3];
+      c.mr = mr[0];
+      c.mi = mi[0];
+    }
+    if (lane == 0) finalize<OP>(op, A, B, c, L + sp.slot);
+  }
+}
+
 // Explicit pairs (bgb_local_matrices_curve): far pairs by the far-kernel code, the others listed
 // for k_curve_special.  err[0]: list length, err[1]: invalid pair / rule.
 template <int OP>
@@ -1066,10 +1251,50 @@ static void launch_special_t(const Op& op, const Rules* rules, const SegGeo* gT,
 }
 
 template <int OP>
-static void launch_special(const Op& op, const Rules* rules, const SegGeo* gT, const SegGeo* gB, const Special* list,
-                           int n, void* L, bool fp32_l, int num_sms, cudaStream_t st) {
+static void launch_special(const Op& op, const Rules* rules, const RulesDF* rdf, const SegGeo* gT, const SegGeo* gB,
+                           const Special* list, int n, void* L, bool fp32_l, int num_sms, cudaStream_t st) {
+  if (n <= 0) return;
+  const int blocks = std::max(1, std::min((n + 7) / 8, num_sms * 8));
+  if (rdf && (OP == BGB_OP2D_SL || OP == BGB_OP2D_HS)) {
+    if (fp32_l) k_curve_special_df<OP, float2><<<blocks, 256, 0, st>>>(op, rules, rdf, gT, gB, list, n, (float2*)L);
+    else k_curve_special_df<OP, double2><<<blocks, 256, 0, st>>>(op, rules, rdf, gT, gB, list, n, (double2*)L);
+    return;
+  }
   if (fp32_l) launch_special_t<OP, float2>(op, rules, gT, gB, list, n, (float2*)L, num_sms, st);
   else launch_special_t<OP, double2>(op, rules, gT, gB, list, n, (double2*)L, num_sms, st);
+}
+
+static void make_rules_df(const Rules& R, RulesDF* D) {
+  std::memset(D, 0, sizeof(RulesDF));
+  auto df = [](double v) {
+    const float h = (float)v;
+    return dfl{h, (float)(v - (double)h)};
+  };
+  D->n = R.nsing;
+  D->nz = R.ngraded;
+  D->nzcv = R.ngraded_cv;
+  for (int a = 0; a < R.ngraded; ++a) {
+    D->gz[a] = df(R.gz[a]);
+    D->wcf[a] = df(R.gwz[a] * (1.0 - R.gz[a]));
+    D->lnz[a] = df(R.lnz[a]);
+  }
+  for (int a = 0; a < R.ngraded_cv; ++a) {
+    D->gzc[a] = df(R.gz_cv[a]);
+    D->wcv[a] = df(R.gwz_cv[a] * R.gz_cv[a]);
+    D->lnzc[a] = df(R.lnz_cv[a]);
+  }
+  for (int b = 0; b < R.nsing; ++b) {
+    D->sgx[b] = df(R.sg_x[b]);
+    D->sgw[b] = df(R.sg_w[b]);
+  }
+  for (int b = 0; b < 2; ++b) {
+    D->gl2x[b] = df(R.gl2_x[b]);
+    D->gl2w[b] = df(R.gl2_w[b]);
+  }
+  for (int m = 0; m <= kSeries; ++m) D->sa[m] = df(R.sa[m]);
+  for (int m = 0; m < kSeries; ++m) D->sb[m] = df(R.sb[m]);
+  D->inv2pi = df(0.15915494309189535);
+  D->two_over_pi = df(0.6366197723675814);
 }
 
 template <int OP>
@@ -1180,6 +1405,11 @@ int bgb_assemble_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_curve_
     return rc;
   if ((rc = B.rules.ensure(sizeof(Rules)))) return rc;
   BGB_CUDA(cudaMemcpyAsync(B.rules.p, &R, sizeof(Rules), cudaMemcpyHostToDevice, s));
+  RulesDF RD;
+  make_rules_df(R, &RD);
+  if ((rc = B.rulesdf.ensure(sizeof(RulesDF)))) return rc;
+  BGB_CUDA(cudaMemcpyAsync(B.rulesdf.p, &RD, sizeof(RulesDF), cudaMemcpyHostToDevice, s));
+  BGB_CUDA(cudaStreamSynchronize(s));  // RD lives on this stack frame
   int launches = test->ns > 0 ? 1 : 0;
   launches += trial->ns > 0 ? 1 : 0;
 
@@ -1265,8 +1495,9 @@ int bgb_assemble_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_curve_
       }
       BGB_CUDA(cudaGetLastError());
       BGB_CUDA(cudaEventRecord(h->ev[3], s));
-      BGB_CURVE_DISPATCH(o.kind, launch_special, o, B.rules.as<Rules>(), B.geo_t.as<SegGeo>(), B.geo_b.as<SegGeo>(),
-                         B.list.as<Special>(), counts[0], B.L.p, fp32_l, h->num_sms, s);
+      BGB_CURVE_DISPATCH(o.kind, launch_special, o, B.rules.as<Rules>(), fp32_l ? B.rulesdf.as<RulesDF>() : nullptr,
+                         B.geo_t.as<SegGeo>(), B.geo_b.as<SegGeo>(), B.list.as<Special>(), counts[0], B.L.p, fp32_l,
+                         h->num_sms, s);
       BGB_CUDA(cudaGetLastError());
       BGB_CUDA(cudaEventRecord(h->ev[4], s));
       launches += 1 + (counts[0] > 0);
@@ -1371,6 +1602,11 @@ int bgb_local_matrices_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_
     return rc;
   if ((rc = B.rules.ensure(sizeof(Rules)))) return rc;
   BGB_CUDA(cudaMemcpyAsync(B.rules.p, &R, sizeof(Rules), cudaMemcpyHostToDevice, s));
+  RulesDF RD;
+  make_rules_df(R, &RD);
+  if ((rc = B.rulesdf.ensure(sizeof(RulesDF)))) return rc;
+  BGB_CUDA(cudaMemcpyAsync(B.rulesdf.p, &RD, sizeof(RulesDF), cudaMemcpyHostToDevice, s));
+  BGB_CUDA(cudaStreamSynchronize(s));  // RD lives on this stack frame
   if ((rc = put(s, B.pairs, pairs)) || (rc = B.out.ensure(sizeof(double2) * 4 * (size_t)npairs)) ||
       (rc = B.own.ensure((size_t)npairs)) || (rc = B.list.ensure(sizeof(Special) * (size_t)npairs)) ||
       (rc = B.counts.ensure(sizeof(int) * 8)))
@@ -1389,8 +1625,9 @@ int bgb_local_matrices_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_
     set_error("a pair is degenerate or its forced rule does not match its class");
     return BGB_ERR_INVALID;
   }
-  BGB_CURVE_DISPATCH(o.kind, launch_special, o, B.rules.as<Rules>(), B.geo_t.as<SegGeo>(), B.geo_b.as<SegGeo>(),
-                     B.list.as<Special>(), counts[0], B.out.p, false, h->num_sms, s);
+  BGB_CURVE_DISPATCH(o.kind, launch_special, o, B.rules.as<Rules>(),
+                     precision == BGB_PREC_MIXED ? B.rulesdf.as<RulesDF>() : nullptr, B.geo_t.as<SegGeo>(),
+                     B.geo_b.as<SegGeo>(), B.list.as<Special>(), counts[0], B.out.p, false, h->num_sms, s);
   BGB_CUDA(cudaGetLastError());
   std::vector<double2> L((size_t)npairs * 4);
   std::vector<signed char> cls((size_t)npairs);

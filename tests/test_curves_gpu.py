@@ -3,7 +3,8 @@ bgb_local_matrices_curve through the C ABI).
 
 Bar: FP64 outputs within 1e-12 (relative Frobenius norm, and every local matrix within 1e-12
 of the oracle's), complex-float outputs within 1e-6; the mixed path (FP32 far pairs) within 1e-5
-of the oracle with its coincident, common-vertex and near pairs identical to the FP64 path's;
+of the oracle with its coincident, common-vertex (double-float) and near (FP64) pairs within 1e-12
+of the FP64 path's;
 classes and class counts identical; results bit-identical from run to run and across column
 blocks.
 """
@@ -181,7 +182,10 @@ def test_mixed_local_matrices():
             Lm, cls = bg.local_matrices_curve(op, T, B, d["tau"], d["sigma"], precision="mixed")
             Ld, _ = bg.local_matrices_curve(op, T, B, d["tau"], d["sigma"], precision="fp64")
             far = cls == 0  # the near pairs of k <= 3 are far at k = 10
-            assert np.array_equal(Lm[~far], Ld[~far])  # singular and near pairs: the FP64 kernel
+            # singular pairs in double-float (single layer, hypersingular) or FP64, near pairs in FP64
+            nf = np.abs(Ld[~far]).max(axis=(1, 2))
+            err = np.abs(Lm[~far] - Ld[~far]).max(axis=(1, 2))
+            assert np.all(err <= 1e-12 * np.where(nf > 0, nf, 1e-300)), (k, kind, err / np.where(nf > 0, nf, 1))
             Lo, _ = oracle.local_matrices_curve(op, T, B, QuadStrat2D(), d["tau"][far], d["sigma"][far])
             assert np.abs(Lm[far] - Lo).max() <= 1e-5 * np.abs(Lo).max(), (k, kind)
 
