@@ -308,7 +308,7 @@ def run_curve(args):
 
     def kernels(st):
         return {"far_and_gather": float(np.mean([s["ms_far"] for s in st])),
-                "singular_and_near_fp64": float(np.mean([s["ms_singular"] for s in st])),
+                "singular_and_near": float(np.mean([s["ms_singular"] for s in st])),
                 "classify": float(np.mean([s["ms_classify"] for s in st]))}
     km, kd = kernels(st_m), kernels(st_d)
     tf = point_pairs * CURVE_MIXED_FP32_FLOPS_PER_POINT_PAIR / (km["far_and_gather"] * 1e-3) / 1e12
@@ -324,8 +324,8 @@ def run_curve(args):
               "unit": "TFLOP/s", "frac": tf64 / fp64_peak,
               "flop_convention": f"{CURVE_FP64_FLOPS_PER_POINT_PAIR} FP64 flops per far point pair (ncu count, "
                                  "CUDA's J0 and Y0 included)"}
-    line = line_base(args, world, value, m, "f32 far pairs (FP32 Hankel approximations, FP64-carried phase) + "
-                     "FP64 singular/near (mixed)", curve_config(mesh, X, {
+    line = line_base(args, world, value, m, "f32 far pairs (FP32 Hankel approximations, double-float phase) + "
+                     "double-float singular, FP64 near (mixed)", curve_config(mesh, X, {
                          "parallelism": f"{world} independent matrices, one per rank, no collective" if world > 1
                          else "single GPU"}),
                      metric="segment pair-interactions/s (2-D): mixed FP32 vs plain FP64",
