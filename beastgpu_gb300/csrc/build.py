@@ -18,7 +18,7 @@ OUT = os.path.join(PKG, "libbeastgb.so")
 BUILD = os.path.join(HERE, "_build")
 SOURCES = ["bgb_api.cu", "bgb_plan.cu", "bgb_singular.cu", "bgb_far.cu", "bgb_peaks.cu", "bgb_noalloc.cu", "bgb_batch.cu", "bgb_singular_df.cu", "bgb_curve.cu"] + [
     f"bgb_far_{p}_op{o}.cu" for p in ("mixed", "fp64") for o in (0, 1, 2, 3, 4, 5)]
-HEADERS = ["bgb_common.cuh", "bgb_kernels.cuh", "bgb_far_impl.cuh", "bgb_host.h", "bgb_df.cuh", "bgb_ss.cuh", "trirules.h", os.path.join("..", "..", "include", "beastgb.h")]
+HEADERS = ["bgb_common.cuh", "bgb_kernels.cuh", "bgb_far_impl.cuh", "bgb_host.h", "bgb_df.cuh", "bgb_ss.cuh", "trirules.h", "besselfit.h", os.path.join("..", "..", "include", "beastgb.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr",
               "-I", os.path.join(ROOT, "include")]
