@@ -1432,12 +1432,28 @@ int bgb_assemble_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_curve_
   const int64_t budget = h->cfg.hbm_budget_bytes > 0 ? h->cfg.hbm_budget_bytes : (int64_t)(0.9 * (double)freeb);
   const int64_t ncols = trial->nfun;
   const int64_t per_col = 2 * (int64_t)std::max(1, nT) * o.LS * (int64_t)lsz + (host_out ? nrows * (int64_t)esz : 0);
-  const int64_t cols_per_block = std::max<int64_t>(1, std::min<int64_t>(ncols, budget / 2 / std::max<int64_t>(1, per_col)));
+  int64_t cols_per_block = std::max<int64_t>(1, std::min<int64_t>(ncols, budget / 2 / std::max<int64_t>(1, per_col)));
+  if (host_out) {
+    // host outputs: about 8 blocks (of at least 32 MiB), each copied on the copy stream while the
+    // next block is computed; two staging slots
+    const int64_t min_cols = ((int64_t)32 << 20) / std::max<int64_t>(1, nrows * (int64_t)esz);
+    cols_per_block = std::min(cols_per_block, std::max<int64_t>((ncols + 7) / 8, std::max<int64_t>(1, min_cols)));
+  }
+  double ms_cls = 0, ms_far = 0, ms_sp = 0, ms_copy_acc = 0;
+  int pending[2] = {0, 0};  // staging slot holds a copy in flight
+  auto finish_copy = [&](int slot) -> int {
+    if (!pending[slot]) return 0;
+    BGB_CUDA(cudaEventSynchronize(h->ev2[4 * slot + 2]));
+    ms_copy_acc += event_ms(h->ev2[4 * slot + 1], h->ev2[4 * slot + 2]);
+    pending[slot] = 0;
+    return 0;
+  };
   std::vector<unsigned char> seen((size_t)trial->ns, 0);
   int64_t computed = 0, nonfar[5] = {0, 0, 0, 0, 0};
-  double ms_cls = 0, ms_far = 0, ms_sp = 0, ms_copy = 0;
   int nblocks = 0;
   int cap = std::max(1 << 16, 8 * nT);
+  // the block loop; on any early return the copies still in flight are drained below
+  auto run_blocks = [&]() -> int {
   for (int64_t c0 = 0; c0 < ncols; c0 += cols_per_block) {
     if (h->abort_host && *h->abort_host) { set_error("aborted by bgb_abort"); return BGB_ERR_ABORTED; }
     const int64_t c1 = std::min(ncols, c0 + cols_per_block);
@@ -1508,11 +1524,14 @@ int bgb_assemble_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_curve_
     }
     // gather into the output (device) or the staging buffer (host)
     const int64_t bc = c1 - c0;
+    const int slot = (nblocks - 1) & 1;
+    DevBuf& stage = slot ? B.stage2 : B.stage;
     void* dst;
     int64_t dld;
     if (host_out) {
-      if ((rc = B.stage.ensure(esz * (size_t)nrows * (size_t)bc))) return rc;
-      dst = B.stage.p;
+      if ((rc = finish_copy(slot))) return rc;  // the copy of block b - 2 left this slot
+      if ((rc = stage.ensure(esz * (size_t)nrows * (size_t)cols_per_block))) return rc;
+      dst = stage.p;
       dld = nrows;
     } else {
       dst = (char*)out + esz * (size_t)c0 * (size_t)ld;
@@ -1533,15 +1552,27 @@ int bgb_assemble_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_curve_
     ++launches;
     BGB_CUDA(cudaEventRecord(h->ev[5], s));
     if (host_out) {
-      BGB_CUDA(cudaMemcpy2DAsync((char*)out + esz * (size_t)c0 * (size_t)ld, esz * (size_t)ld, B.stage.p,
-                                 esz * (size_t)nrows, esz * (size_t)nrows, (size_t)bc, cudaMemcpyDeviceToHost, s));
+      // copy on the copy stream: the next block's classification and far pairs run meanwhile
+      BGB_CUDA(cudaEventRecord(h->ev2[4 * slot], s));
+      BGB_CUDA(cudaStreamWaitEvent(h->copy_stream, h->ev2[4 * slot], 0));
+      BGB_CUDA(cudaEventRecord(h->ev2[4 * slot + 1], h->copy_stream));
+      BGB_CUDA(cudaMemcpy2DAsync((char*)out + esz * (size_t)c0 * (size_t)ld, esz * (size_t)ld, stage.p,
+                                 esz * (size_t)nrows, esz * (size_t)nrows, (size_t)bc, cudaMemcpyDeviceToHost,
+                                 h->copy_stream));
+      BGB_CUDA(cudaEventRecord(h->ev2[4 * slot + 2], h->copy_stream));
+      pending[slot] = 1;
     }
-    BGB_CUDA(cudaEventRecord(h->ev[6], s));
     BGB_CUDA(cudaStreamSynchronize(s));
     ms_far += event_ms(h->ev[2], h->ev[3]) + event_ms(h->ev[4], h->ev[5]);
     ms_sp += event_ms(h->ev[3], h->ev[4]);
-    ms_copy += event_ms(h->ev[5], h->ev[6]);
   }
+  for (int k = 0; k < 2; ++k)
+    if ((rc = finish_copy(k))) return rc;
+  return 0;
+  };
+  rc = run_blocks();
+  if (host_out) cudaStreamSynchronize(h->copy_stream);
+  if (rc) return rc;
   if (!host_out && user != s) {
     BGB_CUDA(cudaEventRecord(h->ev[7], s));
     BGB_CUDA(cudaStreamWaitEvent(user, h->ev[7], 0));
@@ -1557,7 +1588,7 @@ int bgb_assemble_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_curve_
   st.ms_classify = ms_cls;
   st.ms_far = ms_far;
   st.ms_singular = ms_sp;
-  st.ms_copy = ms_copy;
+  st.ms_copy = ms_copy_acc;
   st.out_blocks = nblocks;
   st.tile_config = -1;
   st.kernel_launches = launches;

@@ -40,11 +40,12 @@ struct DevBuf {
 // Scratch of the curve (2-D) path.
 struct CurveBufs {
   DevBuf verts_t, segs_t, geo_t, geof_t, verts_b, segs_b, geo_b, geof_b, rules, rulesdf, L, list, counts, mask, tsup_i,
-      tsup_c, tsup_off, bsup_i, bsup_c, bsup_off, T, S, own, pairs, out, stage;
+      tsup_c, tsup_off, bsup_i, bsup_c, bsup_off, T, S, own, pairs, out, stage, stage2;
   void release() {
     DevBuf* all[] = {&verts_t, &segs_t, &geo_t, &geof_t, &verts_b, &segs_b, &geo_b, &geof_b, &rules, &rulesdf, &L, &list,
                      &counts,
-                     &mask, &tsup_i, &tsup_c, &tsup_off, &bsup_i, &bsup_c, &bsup_off, &T, &S, &own, &pairs, &out, &stage};
+                     &mask, &tsup_i, &tsup_c, &tsup_off, &bsup_i, &bsup_c, &bsup_off, &T, &S, &own, &pairs, &out, &stage,
+                     &stage2};
     for (DevBuf* b : all) b->release();
   }
 };
