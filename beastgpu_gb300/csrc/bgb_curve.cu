@@ -1358,6 +1358,25 @@ static void localise(const CurveSupports& C, std::vector<int>& segs, std::vector
   for (size_t k = 0; k < C.seg.size(); ++k) code[k] = 2 * map_scratch[(size_t)C.seg[k]] + C.loc[k];
 }
 
+// The mixed far kernels reduce k R0 modulo 2 pi with 2 pi split in three floats, exact for
+// k R0 < 4e5 (2^16 turns): reject problems whose k times the diameter of the two curves exceeds 3e5.
+static int check_mixed_range(const bgb_operator2d* op, const bgb_curve_space* a, const bgb_curve_space* b) {
+  double lo[2] = {1e300, 1e300}, hi[2] = {-1e300, -1e300};
+  for (const bgb_curve_space* sp : {a, b})
+    for (int64_t v = 0; v < sp->nv; ++v)
+      for (int c = 0; c < 2; ++c) {
+        lo[c] = std::min(lo[c], sp->vertices[2 * v + c]);
+        hi[c] = std::max(hi[c], sp->vertices[2 * v + c]);
+      }
+  const double diam = std::hypot(hi[0] - lo[0], hi[1] - lo[1]);
+  if (op->wavenumber * diam > 3e5) {
+    set_error("mixed precision covers k times the curves' diameter up to 3e5 (got %.3g); use BGB_PREC_FP64",
+              op->wavenumber * diam);
+    return BGB_ERR_NOT_SUPPORTED;
+  }
+  return 0;
+}
+
 }  // namespace curve
 }  // namespace bgb
 
@@ -1378,6 +1397,7 @@ int bgb_assemble_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_curve_
   Rules R;
   if ((rc = make_op(op, test, trial, &o)) || (rc = make_rules(qs, &R))) return rc;
   if (precision != BGB_PREC_FP64 && precision != BGB_PREC_MIXED) { set_error("bad precision %d", precision); return BGB_ERR_INVALID; }
+  if (precision == BGB_PREC_MIXED && (rc = check_mixed_range(op, test, trial))) return rc;
   if (out_kind < BGB_OUT_HOST_C64 || out_kind > BGB_OUT_DEVICE_C32) { set_error("bad out_kind %d", out_kind); return BGB_ERR_INVALID; }
   if (nrows < 0) nrows = (int64_t)test->nfun - row0;
   if (row0 < 0 || row0 + nrows > test->nfun) { set_error("row window [%lld, %lld) outside [0, %d)", (long long)row0, (long long)(row0 + nrows), test->nfun); return BGB_ERR_INVALID; }
@@ -1610,6 +1630,7 @@ int bgb_local_matrices_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_
   Rules R;
   if ((rc = make_op(op, test, trial, &o)) || (rc = make_rules(qs, &R))) return rc;
   if (precision != BGB_PREC_FP64 && precision != BGB_PREC_MIXED) { set_error("bad precision %d", precision); return BGB_ERR_INVALID; }
+  if (precision == BGB_PREC_MIXED && (rc = check_mixed_range(op, test, trial))) return rc;
   if (npairs < 0 || (npairs > 0 && (!tau || !sigma || !out))) { set_error("invalid pair list"); return BGB_ERR_INVALID; }
   if (force_class != -1 && force_class != 0 && force_class != 1 && force_class != 3 && force_class != 4) {
     set_error("force_class %d is not a curve pair class", force_class);

@@ -272,7 +272,9 @@ typedef struct {
 /* Assemble rows [row0, row0 + nrows) of the curve operator's matrix; arguments, output layout,
  * streams and errors as bgb_assemble.  precision: BGB_PREC_FP64 (all FP64, CUDA's Bessel
  * functions) or BGB_PREC_MIXED (far pairs in FP32 with polynomial Hankel approximations and the
- * phase k R carried in FP64 per pair; coincident, common-vertex and near pairs in FP64).  stats:
+ * phase k R carried in double-float per pair, for k times the curves' diameter up to 3e5, else
+ * BGB_ERR_NOT_SUPPORTED; coincident and common-vertex pairs in double-float (single layer,
+ * hypersingular) or FP64, near pairs in FP64).  stats:
  * pairs over all test segments of the rows and all trial segments, classes 0 far, 1 common
  * vertex, 3 coincident, 4 near.
  * Replaces: momintegrals_gpu_doubleQuad! of the 2-D prototype (doubleQuadRule_2d_gpu.jl:265-465),

@@ -156,6 +156,10 @@ def test_invalid_inputs_raise():
                         X.refspace, X.fn_index, X.fn_coef, X.nfun)
     with pytest.raises(bg._lib.BGBError):
         bg.assemble_gpu(Operator2D(0, 1.0), bad, bad)
+    # mixed precision carries the phase for k times the diameter up to 3e5
+    with pytest.raises(bg._lib.BGBError) as e:
+        bg.assemble_gpu(Operator2D(0, 2e5), X, X, bg.GPUConfiguration(precision="mixed"))
+    assert e.value.code == -7
 
 
 @pytest.mark.parametrize("curve", list(CURVES))
