@@ -312,6 +312,26 @@ bool df_singular_ok(const OpParams& op, double edge_t, double edge_b) {
          std::fabs(op.gamma[1]) * 2.0 * (edge_t + edge_b) < 350.0;
 }
 
+int check_mixed_range(const bgb_operator* op, const bgb_space* a, const bgb_space* b) {
+  // the mixed far kernels reduce k R0 modulo 2 pi with 2 pi split in three floats, exact for
+  // k R0 < 4e5 (2^16 turns)
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  for (const bgb_space* sp : {a, b})
+    for (int64_t v = 0; v < sp->nv; ++v)
+      for (int c = 0; c < 3; ++c) {
+        lo[c] = std::min(lo[c], sp->vertices[3 * v + c]);
+        hi[c] = std::max(hi[c], sp->vertices[3 * v + c]);
+      }
+  const double diam = std::sqrt((hi[0] - lo[0]) * (hi[0] - lo[0]) + (hi[1] - lo[1]) * (hi[1] - lo[1]) +
+                                (hi[2] - lo[2]) * (hi[2] - lo[2]));
+  const double kd = std::fabs(op->gamma[1]) * diam;
+  if (kd > 3e5) {
+    set_error("mixed precision covers k times the meshes' diameter up to 3e5 (got %.3g); use BGB_PREC_FP64", kd);
+    return BGB_ERR_NOT_SUPPORTED;
+  }
+  return 0;
+}
+
 static int ensure_ring(bgb_handle* h, size_t bytes) {
   if (h->ring && h->ring_bytes >= bytes) return 0;
   if (h->ring) cudaFreeHost(h->ring);
@@ -600,6 +620,7 @@ int bgb_local_matrices(bgb_handle* h, const bgb_operator* op, const bgb_space* t
   if (!qs) { set_error("quadstrat is NULL"); return BGB_ERR_INVALID; }
   if ((rc = make_quadsel(qs, &qsel))) return rc;
   if (precision != BGB_PREC_FP64 && precision != BGB_PREC_MIXED) { set_error("bad precision"); return BGB_ERR_INVALID; }
+  if (precision == BGB_PREC_MIXED && (rc = check_mixed_range(op, test, trial))) return rc;
   if (npairs < 0 || (npairs && (!tau || !sigma || !out)) || force_class > 4) { set_error("bad pair list"); return BGB_ERR_INVALID; }
   for (int64_t p = 0; p < npairs; ++p)
     if (tau[p] < 0 || tau[p] >= test->nt || sigma[p] < 0 || sigma[p] >= trial->nt) {
@@ -682,6 +703,7 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
   if (!qs) { set_error("quadstrat is NULL"); return BGB_ERR_INVALID; }
   if ((rc = make_quadsel(qs, &qsel))) return rc;
   if (precision != BGB_PREC_FP64 && precision != BGB_PREC_MIXED) { set_error("bad precision %d", precision); return BGB_ERR_INVALID; }
+  if (precision == BGB_PREC_MIXED && (rc = check_mixed_range(op, test, trial))) return rc;
   if (out_kind < BGB_OUT_HOST_C64 || out_kind > BGB_OUT_DEVICE_C32) { set_error("bad out_kind %d", out_kind); return BGB_ERR_INVALID; }
   if (nrows < 0) nrows = (int64_t)test->nfun - row0;
   if (row0 < 0 || row0 + nrows > test->nfun) { set_error("row window [%lld, %lld) outside [0, %d)", (long long)row0, (long long)(row0 + nrows), test->nfun); return BGB_ERR_INVALID; }

@@ -270,6 +270,7 @@ int bgb_batch_create(bgb_handle* h, int32_t n, const bgb_problem* problems, int3
       return BGB_ERR_NOT_SUPPORTED;
     }
     if (!q.out && q.test.nfun > 0 && q.trial.nfun > 0) { set_error("problem %d: out is NULL", p); return BGB_ERR_INVALID; }
+    if (precision == BGB_PREC_MIXED && (rc = check_mixed_range(&q.op, &q.test, &q.trial))) return rc;
     if (q.ld < std::max(1, q.test.nfun)) { set_error("problem %d: ld < number of rows", p); return BGB_ERR_INVALID; }
   }
   cudaSetDevice(h->device);

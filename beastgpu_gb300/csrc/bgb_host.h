@@ -136,6 +136,9 @@ double max_edge(const bgb_space* s);
 // wave number and k R below the range of the df sin / cos.
 bool df_singular_ok(const OpParams& op, double edge_t, double edge_b);
 double event_ms(cudaEvent_t a, cudaEvent_t b);
+// BGB_ERR_NOT_SUPPORTED when k times the diameter of the two meshes exceeds 3e5, the range of the
+// mixed far kernels' phase reduction.
+int check_mixed_range(const bgb_operator* op, const bgb_space* a, const bgb_space* b);
 // Gauss-Legendre rule on [0, 1], nodes ascending (n <= 64).
 void gauss_legendre01(int n, double* x, double* w);
 

@@ -140,6 +140,8 @@ int bgb_destroy(bgb_handle* h);
  * nrows < 0 means all rows.  Output is column-major (Julia layout): element (m, n) at
  * out[(m - row0) + n * ld], ld >= nrows.  Device outputs are written on `stream`
  * (a cudaStream_t, NULL = the handle's stream); host outputs are complete on return.
+ * BGB_PREC_MIXED reduces the phase k R exactly for k times the diameter of the two meshes up to
+ * 3e5 and returns BGB_ERR_NOT_SUPPORTED beyond (use BGB_PREC_FP64 there).
  * Replaces: assemble_gpu(op, X, Y, config, GpuWriteBackTrueInstance(); quadstrat)
  * (assamble_gpu.jl:25-137) and BEAST.assemble for the same operator (data/BEAST__multi.jl:15). */
 int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test,

@@ -256,6 +256,10 @@ def test_invalid_inputs_fail_cleanly_and_handle_survives(c1):
     with pytest.raises(bg._lib.BGBError) as e:
         bg.assemble_gpu(bg.Helmholtz3D.singlelayer(wavenumber=1.0), X, X)  # Helmholtz needs Lagrange
     assert e.value.code == -7
+    # mixed precision reduces the phase k R exactly for k times the diameter up to 3e5
+    with pytest.raises(bg._lib.BGBError) as e:
+        bg.assemble_gpu(bg.Maxwell3D.singlelayer(wavenumber=2e5), X, X, bg.GPUConfiguration(precision="mixed"))
+    assert e.value.code == -7
     # the handle still works
     z = bg.assemble_gpu(op, X, X, bg.GPUConfiguration(precision="mixed"))
     assert np.isfinite(z).all()
