@@ -1,16 +1,17 @@
-// Curve (2-D) path of libbeastgb: BEAST Helmholtz2D operators on polygonal curves, in FP64.
+// Curve (2-D) path of libbeastgb: BEAST Helmholtz2D operators on polygonal curves.
 //
 //   upload curves -> k_curve_geo -> per block of output columns:
-//     k_curve_classify (non-far pairs into a list) -> k_curve_far (one thread per far pair,
-//     Gauss-Legendre product rule) -> k_curve_special (one warp per coincident, common-vertex
-//     or near pair) -> k_curve_gather (one thread per matrix entry, supports in a fixed order)
+//     k_curve_classify (FP32 prefilter + exact FP64 predicate; non-far pairs into a list and a
+//     bit mask) -> far pairs: k_curve_far (FP64, CUDA's Bessel functions) or k_curve_far_mixed
+//     (FP32 Hankel approximations, double-float phase), one thread per pair -> coincident,
+//     common-vertex and near pairs: k_curve_special (FP64) or k_curve_special_df (double-float
+//     singular rules), one warp per pair -> k_curve_gather (one thread per matrix entry,
+//     supports in a fixed order, no atomics)
 //
 // The reference's 2-D prototype (old_code/doubleQuadRule_2d_gpu.jl:129-210, :265-465) integrates
 // one segment pair per host call, with one GPU thread per point pair and a reduction into the
-// 2x2 result.  Here one launch integrates every pair of a block of columns (a thread per far
-// pair, a warp per singular or near pair), and the matrix is gathered without atomics.  The
-// Hankel functions are CUDA's double-precision Bessel functions (the prototype's truncated series
-// at :31-64 hold only for small kR).
+// 2x2 result, and its Hankel functions are truncated power series (:31-64) that hold only for
+// small kR.  Here one launch integrates every pair of a block of columns.
 #include "bgb_host.h"
 #include "besselfit.h"
 #include "bgb_df.cuh"
@@ -39,9 +40,9 @@ constexpr int kMaxGradedCv = ((3 * kMaxSing) / 2 + 1) * kMaxSing;
 constexpr int kMaxDepth = 16;  // bisections of a near pair
 constexpr double kInv2Pi = 0.15915494309189535;
 
-// Point rules of one call (copied to shared memory by the kernels that use them).
 constexpr int kSeries = 17;  // highest power of u = x^2/4 in the Bessel series (enough for x <= 4)
 
+// Point rules of one call (copied to shared memory by the kernels that use them).
 struct Rules {
   int nft, nfb, nnear, nsing, ngraded, pad;
   double ft_x[kMaxGL], ft_w[kMaxGL], fb_x[kMaxGL], fb_w[kMaxGL], nr_x[kMaxGL], nr_w[kMaxGL];
