@@ -1512,8 +1512,11 @@ int bgb_assemble_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_curve_
                                               B.counts.as<int>(), B.mask.as<unsigned>());
         BGB_CUDA(cudaGetLastError());
         BGB_CUDA(cudaEventRecord(h->ev[1], s));
-        BGB_CUDA(cudaMemcpyAsync(counts, B.counts.p, sizeof(int) * 8, cudaMemcpyDeviceToHost, s));
+        // through the mapped mailbox: a copy would wait behind the previous block's output copy
+        launch_publish(B.counts.as<int>(), 8, h->mbox_dev, s);
+        BGB_CUDA(cudaGetLastError());
         BGB_CUDA(cudaStreamSynchronize(s));
+        for (int c = 0; c < 8; ++c) counts[c] = h->mbox_host[c];
         ms_cls += event_ms(h->ev[0], h->ev[1]);
         ++launches;
         if (counts[1]) { set_error("degenerate geometry: a segment pair shares more than two vertices"); return BGB_ERR_INVALID; }

@@ -534,18 +534,28 @@ __device__ void pair_integral64(const OpParams& op, const QuadSel& qs, const Rul
   finalize<OP>(op, A, B, cA, cB, acc, L);
 }
 
-template <int OP>
-__global__ void __launch_bounds__(256) k_singular(OpParams op, const __grid_constant__ QuadSel qs,
+// Singular / near pairs, one warp per entry.  BATCH: the operator constants of the test
+// triangle's problem (ops[tri_problem[tau]]) instead of op1.  perm (optional): the launch
+// integrates entries perm[0 .. n) instead of 0 .. n.  Single and batched assemblies share this
+// code, so their values are bit-identical.
+template <int OP, bool BATCH>
+__global__ void __launch_bounds__(256) k_singular(OpParams op1, const OpParams* __restrict__ ops,
+                                                  const int* __restrict__ tri_problem,
+                                                  const __grid_constant__ QuadSel qs,
                                                   const __grid_constant__ RuleTable rules,
                                                   const Geo64* __restrict__ tg, const Geo64* __restrict__ bg,
                                                   const int* __restrict__ ent_tau, const int* __restrict__ ent_sigma,
                                                   const int8_t* __restrict__ ent_cls, int64_t n,
-                                                  double2* __restrict__ out, const volatile int* abort_flag) {
+                                                  double2* __restrict__ out, const volatile int* abort_flag,
+                                                  const int* __restrict__ perm) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < n; e += warps) {
+  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
     if (abort_flag && *abort_flag) return;
-    const Geo64 A = tg[ent_tau[e]], B = bg[ent_sigma[e]];
+    const int64_t e = perm ? (int64_t)perm[i] : i;
+    const int tau = ent_tau[e];
+    const OpParams op = BATCH ? ops[tri_problem[tau]] : op1;
+    const Geo64 A = tg[tau], B = bg[ent_sigma[e]];
     double2 L[3][3];
     pair_integral64<OP>(op, qs, rules, ent_cls[e], A, B, L);
     if (lane < 9) {
@@ -641,35 +651,6 @@ __global__ void __launch_bounds__(256) k_classify_batched(const float4* __restri
   }
 }
 
-template <int OP>
-__global__ void __launch_bounds__(256) k_singular_batched(const OpParams* __restrict__ ops,
-                                                          const __grid_constant__ QuadSel qs,
-                                                          const __grid_constant__ RuleTable rules,
-                                                          const Geo64* __restrict__ tg, const Geo64* __restrict__ bg,
-                                                          const int* __restrict__ tri_problem,
-                                                          const int* __restrict__ ent_tau,
-                                                          const int* __restrict__ ent_sigma,
-                                                          const int8_t* __restrict__ ent_cls, int64_t n,
-                                                          double2* __restrict__ out, const volatile int* abort_flag) {
-  const int lane = threadIdx.x & 31;
-  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < n; e += warps) {
-    if (abort_flag && *abort_flag) return;
-    const int tau = ent_tau[e];
-    const OpParams op = ops[tri_problem[tau]];
-    const Geo64 A = tg[tau], B = bg[ent_sigma[e]];
-    double2 L[3][3];
-    pair_integral64<OP>(op, qs, rules, ent_cls[e], A, B, L);
-    if (lane < 9) {
-      double2 v = L[0][0];
-#pragma unroll
-      for (int q = 1; q < 9; ++q)
-        if (lane == q) v = L[q / 3][q % 3];
-      out[e * 9 + lane] = v;
-    }
-  }
-}
-
 // ----------------------------------------------------------------------------------------
 // Host launchers
 // ----------------------------------------------------------------------------------------
@@ -709,21 +690,61 @@ void launch_classify_dense(const Geo64* tg, const Geo64* bg, int t0, int t1, int
 }
 void launch_singular(const OpParams& op, const QuadSel& qs, const RuleTable& rules, int rsA, int rsB, const Geo64* tg,
                      const Geo64* bg, const int* et, const int* es, const int8_t* ec, int64_t n, double2* out,
-                     const volatile int* abort_flag, int num_sms, cudaStream_t st) {
+                     const volatile int* abort_flag, int num_sms, cudaStream_t st, const int* perm) {
   (void)rsA;
   (void)rsB;
   if (n <= 0) return;
   int64_t blocks = (n + 7) / 8;
   if (blocks > (int64_t)num_sms * 32) blocks = (int64_t)num_sms * 32;
+#define BGB_LAUNCH_SING(OPK)                                                                                   \
+  k_singular<OPK, false><<<(int)blocks, 256, 0, st>>>(op, nullptr, nullptr, qs, rules, tg, bg, et, es, ec, n, out, \
+                                                      abort_flag, perm)
   switch (op.kind) {
-    case BGB_OP_HELMHOLTZ3D_SL: k_singular<BGB_OP_HELMHOLTZ3D_SL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, et, es, ec, n, out, abort_flag); break;
-    case BGB_OP_MAXWELL3D_SL: k_singular<BGB_OP_MAXWELL3D_SL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, et, es, ec, n, out, abort_flag); break;
-    case BGB_OP_MAXWELL3D_DL: k_singular<BGB_OP_MAXWELL3D_DL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, et, es, ec, n, out, abort_flag); break;
-    case BGB_OP_HELMHOLTZ3D_DL: k_singular<BGB_OP_HELMHOLTZ3D_DL><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, et, es, ec, n, out, abort_flag); break;
-    case BGB_OP_HELMHOLTZ3D_DLT: k_singular<BGB_OP_HELMHOLTZ3D_DLT><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, et, es, ec, n, out, abort_flag); break;
-    case BGB_OP_HELMHOLTZ3D_HS: k_singular<BGB_OP_HELMHOLTZ3D_HS><<<(int)blocks, 256, 0, st>>>(op, qs, rules, tg, bg, et, es, ec, n, out, abort_flag); break;
+    case BGB_OP_HELMHOLTZ3D_SL: BGB_LAUNCH_SING(BGB_OP_HELMHOLTZ3D_SL); break;
+    case BGB_OP_MAXWELL3D_SL: BGB_LAUNCH_SING(BGB_OP_MAXWELL3D_SL); break;
+    case BGB_OP_MAXWELL3D_DL: BGB_LAUNCH_SING(BGB_OP_MAXWELL3D_DL); break;
+    case BGB_OP_HELMHOLTZ3D_DL: BGB_LAUNCH_SING(BGB_OP_HELMHOLTZ3D_DL); break;
+    case BGB_OP_HELMHOLTZ3D_DLT: BGB_LAUNCH_SING(BGB_OP_HELMHOLTZ3D_DLT); break;
+    case BGB_OP_HELMHOLTZ3D_HS: BGB_LAUNCH_SING(BGB_OP_HELMHOLTZ3D_HS); break;
+  }
+#undef BGB_LAUNCH_SING
+}
+// Entry groups (see launch_entry_groups): warp-aggregated counts and cursors, one atomic per
+// group present in a warp.
+template <bool FILL>
+__global__ void k_entry_groups(const int* __restrict__ es, int64_t n, const int* __restrict__ first_block,
+                               int* __restrict__ counts, int* __restrict__ cursor, int* __restrict__ perm) {
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); w < n; w += stride) {
+    const int64_t e = w + lane;
+    const bool valid = e < n;
+    const unsigned active = __ballot_sync(0xffffffffu, valid);
+    if (!valid) continue;
+    const int g = first_block[es[e]];
+    const unsigned peers = __match_any_sync(active, g);
+    const int leader = __ffs(peers) - 1;
+    if (!FILL) {
+      if (lane == leader) atomicAdd(&counts[g], __popc(peers));
+    } else {
+      int base = 0;
+      if (lane == leader) base = atomicAdd(&cursor[g], __popc(peers));
+      base = __shfl_sync(active, base, leader);
+      perm[base + __popc(peers & ((1u << lane) - 1u))] = (int)e;
+    }
   }
 }
+
+void launch_entry_groups(bool fill, const int* es, int64_t n, const int* first_block, int* counts, int* cursor,
+                         int* perm, int num_sms, cudaStream_t st) {
+  if (n <= 0) return;
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > (int64_t)num_sms * 8) blocks = (int64_t)num_sms * 8;
+  if (fill) k_entry_groups<true><<<(int)blocks, 256, 0, st>>>(es, n, first_block, counts, cursor, perm);
+  else k_entry_groups<false><<<(int)blocks, 256, 0, st>>>(es, n, first_block, counts, cursor, perm);
+}
+
+
 void launch_local_diag64(const OpParams& op, const QuadSel& qs, const RuleTable& rules, int rsA, int rsB,
                          const Geo64* tg, const Geo64* bg, const int* tau, const int* sigma, int64_t n, int force,
                          double2* out, int8_t* cls, int* err, int num_sms, cudaStream_t st, int16_t* mask) {
@@ -767,14 +788,18 @@ void launch_singular_batched(int op_kind, const OpParams* ops, const QuadSel& qs
   if (n <= 0) return;
   int64_t blocks = (n + 7) / 8;
   if (blocks > (int64_t)num_sms * 32) blocks = (int64_t)num_sms * 32;
+#define BGB_LAUNCH_SING(OPK)                                                                                  \
+  k_singular<OPK, true><<<(int)blocks, 256, 0, st>>>(OpParams{}, ops, tri_problem, qs, rules, tg, bg, et, es, ec, n, \
+                                                     out, abort_flag, nullptr)
   switch (op_kind) {
-    case BGB_OP_HELMHOLTZ3D_SL: k_singular_batched<BGB_OP_HELMHOLTZ3D_SL><<<(int)blocks, 256, 0, st>>>(ops, qs, rules, tg, bg, tri_problem, et, es, ec, n, out, abort_flag); break;
-    case BGB_OP_MAXWELL3D_SL: k_singular_batched<BGB_OP_MAXWELL3D_SL><<<(int)blocks, 256, 0, st>>>(ops, qs, rules, tg, bg, tri_problem, et, es, ec, n, out, abort_flag); break;
-    case BGB_OP_MAXWELL3D_DL: k_singular_batched<BGB_OP_MAXWELL3D_DL><<<(int)blocks, 256, 0, st>>>(ops, qs, rules, tg, bg, tri_problem, et, es, ec, n, out, abort_flag); break;
-    case BGB_OP_HELMHOLTZ3D_DL: k_singular_batched<BGB_OP_HELMHOLTZ3D_DL><<<(int)blocks, 256, 0, st>>>(ops, qs, rules, tg, bg, tri_problem, et, es, ec, n, out, abort_flag); break;
-    case BGB_OP_HELMHOLTZ3D_DLT: k_singular_batched<BGB_OP_HELMHOLTZ3D_DLT><<<(int)blocks, 256, 0, st>>>(ops, qs, rules, tg, bg, tri_problem, et, es, ec, n, out, abort_flag); break;
-    case BGB_OP_HELMHOLTZ3D_HS: k_singular_batched<BGB_OP_HELMHOLTZ3D_HS><<<(int)blocks, 256, 0, st>>>(ops, qs, rules, tg, bg, tri_problem, et, es, ec, n, out, abort_flag); break;
+    case BGB_OP_HELMHOLTZ3D_SL: BGB_LAUNCH_SING(BGB_OP_HELMHOLTZ3D_SL); break;
+    case BGB_OP_MAXWELL3D_SL: BGB_LAUNCH_SING(BGB_OP_MAXWELL3D_SL); break;
+    case BGB_OP_MAXWELL3D_DL: BGB_LAUNCH_SING(BGB_OP_MAXWELL3D_DL); break;
+    case BGB_OP_HELMHOLTZ3D_DL: BGB_LAUNCH_SING(BGB_OP_HELMHOLTZ3D_DL); break;
+    case BGB_OP_HELMHOLTZ3D_DLT: BGB_LAUNCH_SING(BGB_OP_HELMHOLTZ3D_DLT); break;
+    case BGB_OP_HELMHOLTZ3D_HS: BGB_LAUNCH_SING(BGB_OP_HELMHOLTZ3D_HS); break;
   }
+#undef BGB_LAUNCH_SING
 }
 
 }  // namespace bgb

@@ -190,6 +190,27 @@ def test_out_of_core_pipeline_pinned_pageable_and_ring(c1):
         np.testing.assert_array_equal(bg.assemble_gpu(op, X, X, via_ring), ref)
 
 
+@pytest.mark.parametrize("name", ["efie", "mfie", "hh"])
+def test_host_output_blocks_group_the_singular_pairs(plates, name):
+    """A host output in many column blocks integrates the singular and near pairs in groups, each
+    on a side stream just ahead of the first block that reads it: bit-identical to the one-block
+    device output in both precisions (the jittered plates put near pairs into most groups)."""
+    make, which = OPS[name]
+    sp = plates[which]
+    op = make(K1)
+    n = sp.nfun
+    for prec, esz in (("fp64", 16), ("mixed", 8)):
+        ref = bg.assemble_gpu(op, sp, sp, bg.GPUConfiguration(precision=prec), out="device").cpu().numpy()
+        cfg = bg.GPUConfiguration(precision=prec, total_GPU_budget=4 * 23 * n * esz)
+        for _ in range(2):  # the second call reuses the handle's group buffers and events
+            Z, st = bg.assemble_gpu(op, sp, sp, cfg, return_stats=True)
+            assert st["out_blocks"] >= n // 23
+            assert st["ms_singular"] > 0
+            np.testing.assert_array_equal(Z, ref)
+        part = bg.assemble_gpu(op, sp, sp, cfg, rows=(11, n - 30))
+        np.testing.assert_array_equal(part, ref[11:n - 19])
+
+
 def test_host_output_with_leading_dimension_keeps_other_rows(c1):
     """Host output with ld > nrows (a window into a larger column-major array): the rows
     outside the window are untouched, for pinned, pageable and ring destinations."""
