@@ -514,8 +514,7 @@ int bgb_create(bgb_handle** out, const bgb_config* cfg) {
   int rc = 0;
   if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess ||
       (e = cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking)) != cudaSuccess ||
-      (e = cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking)) != cudaSuccess ||
-      (e = cudaStreamCreateWithFlags(&h->sing_stream, cudaStreamNonBlocking)) != cudaSuccess) {
+      (e = cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking)) != cudaSuccess) {
     rc = cuda_fail(e, "cudaStreamCreate");
   }
   for (int i = 0; i < 8 && !rc; ++i)
@@ -551,11 +550,10 @@ int bgb_destroy(bgb_handle* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
   if (h->stream2) cudaStreamSynchronize(h->stream2);
-  if (h->sing_stream) cudaStreamSynchronize(h->sing_stream);
   DevBuf* bufs[] = {&h->verts_t, &h->tris_t, &h->verts_b, &h->tris_b, &h->geo_t, &h->geo_b, &h->bnd_t, &h->bnd_b, &h->bnd_c,
                     &h->rec_t, &h->rec_b, &h->cls_count, &h->cls_off, &h->ent_tau, &h->ent_sigma, &h->ent_cls, &h->ent_mask, &h->geodf_t, &h->geodf_b,
                     &h->sing_L, &h->err, &h->df_tab, &h->tplan_i, &h->tplan_l, &h->tplan_d, &h->tplan_f,
-                    &h->diag_a, &h->diag_b, &h->diag_c, &h->diag_d, &h->grp_first, &h->grp_cnt, &h->grp_perm};
+                    &h->diag_a, &h->diag_b, &h->diag_c, &h->diag_d};
   for (DevBuf* b : bufs) b->release();
   h->curve.release();
   for (int k = 0; k < bgb_handle::kSlots; ++k) {
@@ -569,12 +567,10 @@ int bgb_destroy(bgb_handle* h) {
     if (h->ev2[i]) cudaEventDestroy(h->ev2[i]);
   for (int i = 0; i < 2; ++i)
     if (h->ring_ev[i]) cudaEventDestroy(h->ring_ev[i]);
-  for (cudaEvent_t e2 : h->ev_grp) cudaEventDestroy(e2);
   if (h->ring) cudaFreeHost(h->ring);
   if (h->stream) cudaStreamDestroy(h->stream);
   if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
   if (h->stream2) cudaStreamDestroy(h->stream2);
-  if (h->sing_stream) cudaStreamDestroy(h->sing_stream);
   if (h->abort_host) cudaFreeHost((void*)h->abort_host);
   delete h;
   return 0;
@@ -801,7 +797,6 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
     size_t smem = 0;
     std::string err;
     double ms = 0;
-    std::atomic<bool> done{false};
   } PL;
   const int nth = planner_threads();
   const int target_occ = far_target_ctas_per_sm(precision);
@@ -885,7 +880,6 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
       PL.err = buf;
     }
     PL.ms = std::chrono::duration<double, std::milli>(clk::now() - t0).count();
-    PL.done.store(true, std::memory_order_release);
   };
   struct Joiner {
     std::thread& t;
@@ -956,8 +950,6 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
   if ((rc = h->sing_L.ensure(sizeof(double2) * 9 * std::max<int64_t>(1, nsing)))) return rc;
   const bool use_df = precision == BGB_PREC_MIXED && df_singular_ok(opp, max_edge(test), same ? max_edge(test) : max_edge(trial));
   std::vector<float> df_host;  // uploaded asynchronously: lives until the end of the call
-  DfTables dfM{};
-  std::vector<int64_t> grp_off;  // singular entry groups (host outputs in several blocks)
   if (use_df) {
     DfTables M;
     build_df_tables(qsel, R, df_host, M);
@@ -968,93 +960,15 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
       return rc;
     launch_prepare_geodf(gt, test->nt, h->geodf_t.as<GeoDf>(), h->stream);
     if (!same) launch_prepare_geodf(gb, trial->nt, h->geodf_b.as<GeoDf>(), h->stream);
-    dfM = M;
+    const GeoDf* dgt = h->geodf_t.as<GeoDf>();
+    const GeoDf* dgb = same ? dgt : h->geodf_b.as<GeoDf>();
+    launch_singular_df(opp.kind, make_opdf(opp), nullptr, nullptr, M, h->df_tab.as<float>(), dgt, dgb,
+                       h->ent_tau.as<int>(), h->ent_sigma.as<int>(), h->ent_cls.as<int8_t>(),
+                       h->ent_mask.as<int16_t>(), nsing, h->sing_L.as<double2>(), h->abort_dev, h->num_sms, h->stream);
     launches += 1 + (same ? 0 : 1);
-  }
-  const GeoDf* dgt = h->geodf_t.as<GeoDf>();
-  const GeoDf* dgb = same ? dgt : h->geodf_b.as<GeoDf>();
-  auto launch_sing = [&](cudaStream_t sst, const int* perm, int64_t n) {
-    if (use_df)
-      launch_singular_df(opp.kind, make_opdf(opp), nullptr, nullptr, dfM, h->df_tab.as<float>(), dgt, dgb,
-                         h->ent_tau.as<int>(), h->ent_sigma.as<int>(), h->ent_cls.as<int8_t>(),
-                         h->ent_mask.as<int16_t>(), n, h->sing_L.as<double2>(), h->abort_dev, h->num_sms, sst, perm);
-    else
-      launch_singular(opp, qsel, R, test->refspace, trial->refspace, gt, gb, h->ent_tau.as<int>(),
-                      h->ent_sigma.as<int>(), h->ent_cls.as<int8_t>(), n, h->sing_L.as<double2>(), h->abort_dev,
-                      h->num_sms, sst, perm);
-  };
-  // A host output in several blocks: the entries are grouped by the first output block that
-  // reads them (the lowest block of the functions on their trial triangle) and the groups are
-  // integrated in block order, so that block b's far kernel waits for groups 0 .. b only and the
-  // first copies start after one group instead of all of them.  While the host planner runs,
-  // groups go to the singular stream, at most two in flight; the rest are launched on the far
-  // kernels' streams, each just before its block (where it fills the tail of the previous
-  // block's far kernel: a far kernel launched beside a singular group would hold its SMs to the
-  // end and starve the group).  Each entry is integrated on its own: the values do not depend
-  // on the grouping.
-  const bool grouped = host_out && nblocks > 1 && nsing > 0 && nsing < (int64_t)INT32_MAX;
-  int groups_launched = 0;
-  double ms_sing_groups = 0;
-  auto launch_group = [&](cudaStream_t gst, int g) -> int {  // group g, after groups 0 .. g - 1
-    if (g > 0) BGB_CUDA(cudaStreamWaitEvent(gst, h->ev_grp[2 * (size_t)g - 1], 0));
-    BGB_CUDA(cudaEventRecord(h->ev_grp[2 * (size_t)g], gst));
-    launch_sing(gst, h->grp_perm.as<int>() + grp_off[(size_t)g], grp_off[(size_t)g + 1] - grp_off[(size_t)g]);
-    BGB_CUDA(cudaGetLastError());
-    BGB_CUDA(cudaEventRecord(h->ev_grp[2 * (size_t)g + 1], gst));
-    groups_launched = g + 1;
-    return 0;
-  };
-  struct SyncOnExit {  // no group kernel outlives the call, on any return path
-    cudaStream_t st = nullptr;
-    ~SyncOnExit() {
-      if (st) cudaStreamSynchronize(st);
-    }
-  } sync_sing;
-  if (grouped) {
-    std::vector<int> first((size_t)std::max(1, trial->nt), nblocks - 1);
-    for (int64_t t = 0; t < trial->nt; ++t)
-      for (int i = 0; i < 3; ++i) {
-        const int f = trial->fn_index[3 * t + i];
-        if (f < 0) continue;
-        const int b = (int)(std::upper_bound(col_start.begin(), col_start.end(), (int64_t)f) - col_start.begin()) - 1;
-        first[(size_t)t] = std::min(first[(size_t)t], b);
-      }
-    if ((rc = h->grp_first.ensure(sizeof(int) * first.size())) || (rc = h->grp_cnt.ensure(sizeof(int) * 2 * nblocks)) ||
-        (rc = h->grp_perm.ensure(sizeof(int) * (size_t)nsing)))
-      return rc;
-    while ((int)h->ev_grp.size() < 2 * nblocks) {
-      cudaEvent_t e2 = nullptr;
-      BGB_CUDA(cudaEventCreate(&e2));
-      h->ev_grp.push_back(e2);
-    }
-    if ((rc = upload(h, h->grp_first, first, 0))) return rc;
-    int* cnt = h->grp_cnt.as<int>();
-    BGB_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int) * nblocks, h->stream));
-    launch_entry_groups(false, h->ent_sigma.as<int>(), nsing, h->grp_first.as<int>(), cnt, nullptr, nullptr,
-                        h->num_sms, h->stream);
-    std::vector<int> gc((size_t)nblocks);
-    BGB_CUDA(cudaMemcpyAsync(gc.data(), cnt, sizeof(int) * nblocks, cudaMemcpyDeviceToHost, h->stream));
-    BGB_CUDA(cudaStreamSynchronize(h->stream));  // no output copy is in flight yet
-    grp_off.assign((size_t)nblocks + 1, 0);
-    for (int g = 0; g < nblocks; ++g) grp_off[(size_t)g + 1] = grp_off[(size_t)g] + gc[(size_t)g];
-    if (grp_off[(size_t)nblocks] != nsing) {
-      set_error("singular entry groups cover %lld of %lld entries", (long long)grp_off[(size_t)nblocks], (long long)nsing);
-      return BGB_ERR_INVALID;
-    }
-    std::vector<int> cursor(grp_off.begin(), grp_off.end() - 1);
-    BGB_CUDA(cudaMemcpyAsync(cnt + nblocks, cursor.data(), sizeof(int) * nblocks, cudaMemcpyHostToDevice, h->stream));
-    launch_entry_groups(true, h->ent_sigma.as<int>(), nsing, h->grp_first.as<int>(), nullptr, cnt + nblocks,
-                        h->grp_perm.as<int>(), h->num_sms, h->stream);
-    BGB_CUDA(cudaGetLastError());
-    BGB_CUDA(cudaEventRecord(h->ev[4], h->stream));
-    BGB_CUDA(cudaStreamWaitEvent(h->sing_stream, h->ev[4], 0));
-    sync_sing.st = h->sing_stream;
-    for (int g = 0; g < 2 && g < nblocks; ++g)
-      if ((rc = launch_group(h->sing_stream, g))) return rc;
-    BGB_CUDA(cudaStreamSynchronize(h->stream));  // the host vectors above were uploaded
-    launches += 2 + (nblocks - 1);  // grouping passes, further singular launches
   } else {
-    launch_sing(h->stream, nullptr, nsing);
+    launch_singular(opp, qsel, R, test->refspace, trial->refspace, gt, gb, h->ent_tau.as<int>(), h->ent_sigma.as<int>(),
+                    h->ent_cls.as<int8_t>(), nsing, h->sing_L.as<double2>(), h->abort_dev, h->num_sms, h->stream);
   }
   BGB_CUDA(cudaGetLastError());
   cudaEventRecord(h->ev[2], h->stream);
@@ -1068,14 +982,6 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
   launches += 2;
 
   // 4. the host plan (joined here) and the test-side tables, uploaded once
-  // singular groups on the singular stream while the planner runs, at most two in flight
-  while (grouped && groups_launched < nblocks && !PL.done.load(std::memory_order_acquire)) {
-    if (groups_launched < 2 || cudaEventQuery(h->ev_grp[2 * (size_t)(groups_launched - 2) + 1]) == cudaSuccess) {
-      if ((rc = launch_group(h->sing_stream, groups_launched))) return rc;
-    } else {
-      std::this_thread::sleep_for(std::chrono::microseconds(20));
-    }
-  }
   planner.join();
   st.ms_plan = PL.ms;
   if (PL.cfg_id < 0) {
@@ -1110,8 +1016,8 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
   int64_t pairs_computed = 0;
   constexpr int NS = bgb_handle::kSlots;
   bool pending[NS] = {};
-  // BGB_TRACE=1: one line per output block on stderr (far kernel and copy, ms from the call's
-  // first event; host time spent enqueueing the block) and per singular group
+  // BGB_TRACE set: one line per output block on stderr (far kernel and copy in ms from the call's
+  // first event, host time spent enqueueing the block)
   const bool trace = std::getenv("BGB_TRACE") != nullptr;
   int slot_block[NS] = {};
   std::vector<double> enq_ms((size_t)nblocks, 0.0);
@@ -1231,10 +1137,6 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
                                cudaMemcpyHostToDevice, cst));
     BGB_CUDA(cudaMemsetAsync(dctr, 0, sizeof(int), cst));
     const int ctas = (int)std::min<int64_t>((int64_t)H.items.size(), (int64_t)std::max(1, per_sm) * h->num_sms);
-    if (grouped) {  // singular groups 0 .. b before the far kernel
-      if (b < groups_launched) BGB_CUDA(cudaStreamWaitEvent(cst, h->ev_grp[2 * (size_t)b + 1], 0));
-      else if ((rc2 = launch_group(cst, b))) return rc2;
-    }
     BGB_CUDA(cudaEventRecord(h->ev2[slot * 4 + 0], cst));
     if ((rc2 = launch_far_persistent(precision, K.op_kind, gen, dK, dT, (const int4*)h->far_items[slot].p,
                                      (int)H.items.size(), dctr, smem, std::max(1, ctas), h->abort_dev, cst)))
@@ -1301,7 +1203,6 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
   auto drain = [&](int code) {  // the slots' host tables must outlive uploads still in flight
     cudaStreamSynchronize(h->stream);
     cudaStreamSynchronize(h->stream2);
-    cudaStreamSynchronize(h->sing_stream);
     cudaStreamSynchronize(h->copy_stream);
     return code;
   };
@@ -1313,7 +1214,6 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
   }
   BGB_CUDA(cudaStreamSynchronize(h->stream));
   BGB_CUDA(cudaStreamSynchronize(h->stream2));
-  BGB_CUDA(cudaStreamSynchronize(h->sing_stream));
   BGB_CUDA(cudaStreamSynchronize(h->copy_stream));
   for (int k = 0; k < NS; ++k) harvest(k);
   const double ms_pipe = std::chrono::duration<double, std::milli>(clk::now() - t_pipe).count();
@@ -1329,18 +1229,11 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
   st.pairs_total = (int64_t)test->nt * trial->nt;
   st.pairs_computed = pairs_computed;
   st.ms_classify = event_ms(h->ev[0], h->ev[1]);
-  if (grouped)
-    for (int g = 0; g < groups_launched; ++g) {
-      ms_sing_groups += event_ms(h->ev_grp[2 * (size_t)g], h->ev_grp[2 * (size_t)g + 1]);
-      if (trace)
-        fprintf(stderr, "bgb trace singular group %d: %.3f .. %.3f (%lld entries)\n", g,
-                event_ms(h->ev[0], h->ev_grp[2 * (size_t)g]), event_ms(h->ev[0], h->ev_grp[2 * (size_t)g + 1]),
-                (long long)(grp_off[(size_t)g + 1] - grp_off[(size_t)g]));
-    }
   if (trace)
-    fprintf(stderr, "bgb trace: classify end %.3f, pipeline start %.3f ms after the call's first event (host)\n",
-            event_ms(h->ev[0], h->ev[1]), std::chrono::duration<double, std::milli>(t_pipe - t_start).count());
-  st.ms_singular = grouped ? ms_sing_groups : event_ms(h->ev[1], h->ev[2]);
+    fprintf(stderr, "bgb trace: classify end %.3f, singular end %.3f, pipeline start %.3f (host) ms\n",
+            event_ms(h->ev[0], h->ev[1]), event_ms(h->ev[0], h->ev[2]),
+            std::chrono::duration<double, std::milli>(t_pipe - t_start).count());
+  st.ms_singular = event_ms(h->ev[1], h->ev[2]);
   st.ms_far = ms_far;
   if (stats) {
     std::vector<int8_t> cls((size_t)nsing);

@@ -59,7 +59,6 @@ struct bgb_handle {
   cudaStream_t copy_stream = nullptr;
   cudaStream_t stream2 = nullptr;  // second compute stream: consecutive output blocks alternate, so one
                                    // block's far kernel starts while the previous one drains
-  cudaStream_t sing_stream = nullptr;  // singular pairs grouped by output block, ahead of the far kernels
   bgb_config cfg{};
   volatile int* abort_host = nullptr;
   int* abort_dev = nullptr;
@@ -72,7 +71,6 @@ struct bgb_handle {
   // buffers
   bgb::DevBuf verts_t, tris_t, verts_b, tris_b, geo_t, geo_b, bnd_t, bnd_b, bnd_c, rec_t, rec_b;
   bgb::DevBuf cls_count, cls_off, ent_tau, ent_sigma, ent_cls, ent_mask, sing_L, err, geodf_t, geodf_b;
-  bgb::DevBuf grp_first, grp_cnt, grp_perm;  // singular entries grouped by the first output block reading them
   static constexpr int kSlots = 3;  // output-block slots in flight (staging, plan tables, events)
   bgb::DevBuf plan_i[kSlots], plan_l[kSlots], plan_d[kSlots], plan_f[kSlots], far_items[kSlots], far_const[kSlots], df_tab;
   bgb::DevBuf tplan_i, tplan_l, tplan_d, tplan_f;  // test-side tile tables (shared by all output blocks)
@@ -82,7 +80,6 @@ struct bgb_handle {
   cudaEvent_t ev[8] = {};
   cudaEvent_t ev2[4 * kSlots] = {};  // per output-block slot: far start / end, copy start / end
   cudaEvent_t ring_ev[2] = {};
-  std::vector<cudaEvent_t> ev_grp;  // end of each singular group (no timing)
   void* ring = nullptr;      // pinned host staging ring
   size_t ring_bytes = 0;
 };

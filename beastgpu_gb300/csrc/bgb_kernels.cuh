@@ -20,15 +20,9 @@ void launch_classify(bool fill, const float4* tb, const float4* bb, const Geo64*
 void launch_scan(const int* counts, int n, int64_t* offsets, cudaStream_t st);
 void launch_classify_dense(const Geo64* tg, const Geo64* bg, int t0, int t1, int s0, int s1, double k2, int8_t* out,
                            int* err, cudaStream_t st);
-// perm (optional): the launch integrates entries perm[0 .. n) instead of 0 .. n.
 void launch_singular(const OpParams& op, const QuadSel& qs, const RuleTable& rules, int rsA, int rsB, const Geo64* tg,
                      const Geo64* bg, const int* et, const int* es, const int8_t* ec, int64_t n, double2* out,
-                     const volatile int* abort_flag, int num_sms, cudaStream_t st, const int* perm = nullptr);
-// Entries grouped by the first output block that reads them: group g of entry e is
-// first_block[sigma[e]].  count: counts[g] += group sizes; fill: perm[cursor[g]++] = e (the order
-// within a group is unspecified; every entry is integrated on its own).
-void launch_entry_groups(bool fill, const int* es, int64_t n, const int* first_block, int* counts, int* cursor,
-                         int* perm, int num_sms, cudaStream_t st);
+                     const volatile int* abort_flag, int num_sms, cudaStream_t st);
 void launch_local_diag64(const OpParams& op, const QuadSel& qs, const RuleTable& rules, int rsA, int rsB,
                          const Geo64* tg, const Geo64* bg, const int* tau, const int* sigma, int64_t n, int force,
                          double2* out, int8_t* cls, int* err, int num_sms, cudaStream_t st, int16_t* mask = nullptr);
@@ -71,7 +65,7 @@ OpDf make_opdf(const OpParams& op);
 void launch_singular_df(int op_kind, const OpDf& op, const OpDf* opdf_array, const int* tri_problem,
                         const DfTables& M, const float* dtab, const GeoDf* tg, const GeoDf* bg, const int* et,
                         const int* es, const int8_t* ec, const int16_t* emask, int64_t n, double2* out,
-                        const volatile int* abort_flag, int num_sms, cudaStream_t st, const int* perm = nullptr);
+                        const volatile int* abort_flag, int num_sms, cudaStream_t st);
 
 // ---- bgb_far.cu ------------------------------------------------------------------------
 // Constants of the far-pair kernels (passed by value).

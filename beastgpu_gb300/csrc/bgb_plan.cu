@@ -37,19 +37,32 @@ std::vector<int> morton_rank(const bgb_space* s) {
       hi[k] = std::max(hi[k], v);
     }
   double span = std::max({hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2], 1e-300});
-  std::vector<std::pair<uint64_t, int>> key(nt);
+  std::vector<uint64_t> code((size_t)nt);
+  uint64_t all_or = 0;
   for (int t = 0; t < nt; ++t) {
-    uint64_t code = 0;
+    uint64_t cd = 0;
     for (int k = 0; k < 3; ++k) {
       double f = (c[3 * (size_t)t + k] - lo[k]) / span;
       uint64_t q = (uint64_t)std::min(std::max(f, 0.0) * 2097151.0, 2097151.0);
-      code |= spread3(q) << k;
+      cd |= spread3(q) << k;
     }
-    key[t] = {code, t};
+    code[(size_t)t] = cd;
+    all_or |= cd;
   }
-  std::sort(key.begin(), key.end());
+  // Triangles by (code, index): a stable LSD radix sort of the indices, 8 bits a pass, passes
+  // over bytes that are zero in every code skipped.
+  std::vector<int> idx((size_t)nt), tmp((size_t)nt);
+  for (int t = 0; t < nt; ++t) idx[(size_t)t] = t;
+  for (int shift = 0; shift < 64; shift += 8) {
+    if (((all_or >> shift) & 0xff) == 0) continue;
+    size_t cnt[257] = {0};
+    for (int t = 0; t < nt; ++t) ++cnt[((code[(size_t)idx[(size_t)t]] >> shift) & 0xff) + 1];
+    for (int d = 0; d < 256; ++d) cnt[d + 1] += cnt[d];
+    for (int t = 0; t < nt; ++t) tmp[cnt[(code[(size_t)idx[(size_t)t]] >> shift) & 0xff]++] = idx[(size_t)t];
+    idx.swap(tmp);
+  }
   std::vector<int> rank(nt);
-  for (int i = 0; i < nt; ++i) rank[key[i].second] = i;
+  for (int i = 0; i < nt; ++i) rank[(size_t)idx[(size_t)i]] = i;
   return rank;
 }
 
@@ -78,18 +91,30 @@ Supports build_supports(const bgb_space* s) {
   return S;
 }
 
-// Functions [f_begin, f_end) ordered by the Morton rank of their first support.
+// Functions [f_begin, f_end) ordered by the Morton rank of their first support (ties, and
+// functions without supports last, in index order).  The ranks are < rank.size(): a counting
+// sort when the range is not much smaller than the triangle count, a comparison sort else.
 std::vector<int> order_functions(const Supports& S, const std::vector<int>& rank, int f_begin, int f_end) {
-  std::vector<std::pair<int64_t, int>> key;
-  key.reserve(f_end - f_begin);
+  const int n = std::max(0, f_end - f_begin);
+  const int64_t none = (int64_t)rank.size();  // key of a function without supports
+  std::vector<int64_t> key((size_t)n);
   for (int f = f_begin; f < f_end; ++f) {
-    int64_t first = INT64_MAX;
+    int64_t first = none;
     for (int64_t k = S.off[f]; k < S.off[f + 1]; ++k) first = std::min<int64_t>(first, rank[S.tri[k]]);
-    key.push_back({first, f});
+    key[(size_t)(f - f_begin)] = first;
   }
-  std::sort(key.begin(), key.end());
-  std::vector<int> out(key.size());
-  for (size_t i = 0; i < key.size(); ++i) out[i] = key[i].second;
+  std::vector<int> out((size_t)n);
+  if ((int64_t)n * 4 >= none) {
+    std::vector<int> cnt((size_t)none + 2, 0);
+    for (int i = 0; i < n; ++i) ++cnt[(size_t)key[(size_t)i] + 1];
+    for (int64_t d = 0; d <= none; ++d) cnt[(size_t)d + 1] += cnt[(size_t)d];
+    for (int i = 0; i < n; ++i) out[(size_t)cnt[(size_t)key[(size_t)i]]++] = f_begin + i;
+  } else {
+    std::vector<std::pair<int64_t, int>> kp((size_t)n);
+    for (int i = 0; i < n; ++i) kp[(size_t)i] = {key[(size_t)i], f_begin + i};
+    std::sort(kp.begin(), kp.end());
+    for (int i = 0; i < n; ++i) out[(size_t)i] = kp[(size_t)i].second;
+  }
   return out;
 }
 
@@ -98,6 +123,20 @@ void plan_test_side(const Supports& S, const std::vector<int>& order, int FM, in
   P.tb_fn_off.push_back(0);
   P.fs_off.push_back(0);
   std::vector<int> tris;
+  // stamp[t] == b0: triangle t is already in the block starting at b0; slot[t]: its position
+  // in the block's sorted triangles
+  int ntri = 0;
+  size_t nsup = 0;
+  for (size_t i = 0; i < order.size(); ++i) {
+    for (int64_t k = S.off[order[i]]; k < S.off[order[i] + 1]; ++k) ntri = std::max(ntri, S.tri[k] + 1);
+    nsup += (size_t)(S.off[order[i] + 1] - S.off[order[i]]);
+  }
+  std::vector<int64_t> stamp((size_t)ntri, -1);
+  std::vector<int> slot_of((size_t)ntri, 0);
+  P.fs_code.reserve(P.fs_code.size() + nsup);
+  P.fs_coef.reserve(P.fs_coef.size() + nsup);
+  P.rows.reserve(P.rows.size() + order.size());
+  P.fs_off.reserve(P.fs_off.size() + order.size());
   size_t b0 = 0;
   while (b0 < order.size()) {
     // a block takes up to FM functions while its distinct triangles stay within tcap
@@ -107,18 +146,22 @@ void plan_test_side(const Supports& S, const std::vector<int>& order, int FM, in
       const int f = order[b1];
       int fresh = 0;
       for (int64_t k = S.off[f]; k < S.off[f + 1]; ++k)
-        if (std::find(tris.begin(), tris.end(), S.tri[k]) == tris.end()) ++fresh;
+        if (stamp[(size_t)S.tri[k]] != (int64_t)b0) ++fresh;
       if (b1 > b0 && (int)tris.size() + fresh > tcap) break;
       for (int64_t k = S.off[f]; k < S.off[f + 1]; ++k)
-        if (std::find(tris.begin(), tris.end(), S.tri[k]) == tris.end()) tris.push_back(S.tri[k]);
+        if (stamp[(size_t)S.tri[k]] != (int64_t)b0) {
+          stamp[(size_t)S.tri[k]] = (int64_t)b0;
+          tris.push_back(S.tri[k]);
+        }
       ++b1;
     }
     std::sort(tris.begin(), tris.end());
+    for (size_t i = 0; i < tris.size(); ++i) slot_of[(size_t)tris[i]] = (int)i;
     for (size_t i = b0; i < b1; ++i) {
       int f = order[i];
       int cnt = 0;
       for (int64_t k = S.off[f]; k < S.off[f + 1]; ++k) {
-        int slot = (int)(std::lower_bound(tris.begin(), tris.end(), S.tri[k]) - tris.begin());
+        const int slot = slot_of[(size_t)S.tri[k]];
         P.fs_code.push_back(slot << 2 | S.loc[k]);
         P.fs_coef.push_back(S.coef[k]);
         ++cnt;
@@ -143,31 +186,52 @@ void plan_trial_side(const Supports& S, const std::vector<int>& order, int FN, i
   P.grp_sup_off.push_back(0);
   std::vector<int> tris;
   struct Ent { int chunk, nl, slot, loc; double coef; };
-  std::vector<Ent> ents;
+  std::vector<Ent> ents, sorted;
+  std::vector<int> ccnt;
+  // stamp[t] == b0: triangle t is already in the block starting at b0; slot_of[t]: its position
+  // in the block's sorted triangles
+  int ntri = 0;
+  size_t nsup = 0;
+  for (size_t i = 0; i < order.size(); ++i) {
+    for (int64_t k = S.off[order[i]]; k < S.off[order[i] + 1]; ++k) ntri = std::max(ntri, S.tri[k] + 1);
+    nsup += (size_t)(S.off[order[i] + 1] - S.off[order[i]]);
+  }
+  std::vector<int64_t> stamp((size_t)ntri, -1);
+  std::vector<int> slot_of((size_t)ntri, 0);
+  P.gs_code.reserve(P.gs_code.size() + nsup);
+  P.gs_coef.reserve(P.gs_coef.size() + nsup);
+  P.cols.reserve(P.cols.size() + order.size());
   for (size_t b0 = 0; b0 < order.size(); b0 += FN) {
     size_t b1 = std::min(order.size(), b0 + FN);
     tris.clear();
     for (size_t i = b0; i < b1; ++i) {
       int f = order[i];
-      for (int64_t k = S.off[f]; k < S.off[f + 1]; ++k) tris.push_back(S.tri[k]);
+      for (int64_t k = S.off[f]; k < S.off[f + 1]; ++k)
+        if (stamp[(size_t)S.tri[k]] != (int64_t)b0) {
+          stamp[(size_t)S.tri[k]] = (int64_t)b0;
+          tris.push_back(S.tri[k]);
+        }
     }
     std::sort(tris.begin(), tris.end());
-    tris.erase(std::unique(tris.begin(), tris.end()), tris.end());
+    for (size_t i = 0; i < tris.size(); ++i) slot_of[(size_t)tris[i]] = (int)i;
     ents.clear();
     for (size_t i = b0; i < b1; ++i) {
       int f = order[i];
       for (int64_t k = S.off[f]; k < S.off[f + 1]; ++k) {
-        int slot = (int)(std::lower_bound(tris.begin(), tris.end(), S.tri[k]) - tris.begin());
+        const int slot = slot_of[(size_t)S.tri[k]];
         ents.push_back({slot / SC, (int)(i - b0), slot, S.loc[k], S.coef[k]});
       }
     }
-    // groups: per chunk, per local function, supports by slot (= trial triangle) ascending
-    std::sort(ents.begin(), ents.end(), [](const Ent& a, const Ent& b) {
-      if (a.chunk != b.chunk) return a.chunk < b.chunk;
-      if (a.nl != b.nl) return a.nl < b.nl;
-      return a.slot < b.slot;
-    });
+    // groups: per chunk, per local function, supports by slot (= trial triangle) ascending.
+    // The entries were made in (local function, slot) order (supports are sorted by triangle),
+    // so a stable counting sort by chunk orders them by (chunk, local function, slot).
     int nchunks = ((int)tris.size() + SC - 1) / SC;
+    ccnt.assign((size_t)nchunks + 1, 0);
+    for (const Ent& x : ents) ++ccnt[(size_t)x.chunk + 1];
+    for (int c = 0; c < nchunks; ++c) ccnt[(size_t)c + 1] += ccnt[(size_t)c];
+    sorted.resize(ents.size());
+    for (const Ent& x : ents) sorted[(size_t)ccnt[(size_t)x.chunk]++] = x;
+    ents.swap(sorted);
     size_t e = 0;
     for (int c = 0; c < nchunks; ++c) {
       while (e < ents.size() && ents[e].chunk == c) {

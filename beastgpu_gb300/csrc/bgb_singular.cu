@@ -535,9 +535,8 @@ __device__ void pair_integral64(const OpParams& op, const QuadSel& qs, const Rul
 }
 
 // Singular / near pairs, one warp per entry.  BATCH: the operator constants of the test
-// triangle's problem (ops[tri_problem[tau]]) instead of op1.  perm (optional): the launch
-// integrates entries perm[0 .. n) instead of 0 .. n.  Single and batched assemblies share this
-// code, so their values are bit-identical.
+// triangle's problem (ops[tri_problem[tau]]) instead of op1.  Single and batched assemblies
+// share this code, so their values are bit-identical.
 template <int OP, bool BATCH>
 __global__ void __launch_bounds__(256) k_singular(OpParams op1, const OpParams* __restrict__ ops,
                                                   const int* __restrict__ tri_problem,
@@ -546,13 +545,11 @@ __global__ void __launch_bounds__(256) k_singular(OpParams op1, const OpParams* 
                                                   const Geo64* __restrict__ tg, const Geo64* __restrict__ bg,
                                                   const int* __restrict__ ent_tau, const int* __restrict__ ent_sigma,
                                                   const int8_t* __restrict__ ent_cls, int64_t n,
-                                                  double2* __restrict__ out, const volatile int* abort_flag,
-                                                  const int* __restrict__ perm) {
+                                                  double2* __restrict__ out, const volatile int* abort_flag) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
+  for (int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < n; e += warps) {
     if (abort_flag && *abort_flag) return;
-    const int64_t e = perm ? (int64_t)perm[i] : i;
     const int tau = ent_tau[e];
     const OpParams op = BATCH ? ops[tri_problem[tau]] : op1;
     const Geo64 A = tg[tau], B = bg[ent_sigma[e]];
@@ -690,7 +687,7 @@ void launch_classify_dense(const Geo64* tg, const Geo64* bg, int t0, int t1, int
 }
 void launch_singular(const OpParams& op, const QuadSel& qs, const RuleTable& rules, int rsA, int rsB, const Geo64* tg,
                      const Geo64* bg, const int* et, const int* es, const int8_t* ec, int64_t n, double2* out,
-                     const volatile int* abort_flag, int num_sms, cudaStream_t st, const int* perm) {
+                     const volatile int* abort_flag, int num_sms, cudaStream_t st) {
   (void)rsA;
   (void)rsB;
   if (n <= 0) return;
@@ -698,7 +695,7 @@ void launch_singular(const OpParams& op, const QuadSel& qs, const RuleTable& rul
   if (blocks > (int64_t)num_sms * 32) blocks = (int64_t)num_sms * 32;
 #define BGB_LAUNCH_SING(OPK)                                                                                   \
   k_singular<OPK, false><<<(int)blocks, 256, 0, st>>>(op, nullptr, nullptr, qs, rules, tg, bg, et, es, ec, n, out, \
-                                                      abort_flag, perm)
+                                                      abort_flag)
   switch (op.kind) {
     case BGB_OP_HELMHOLTZ3D_SL: BGB_LAUNCH_SING(BGB_OP_HELMHOLTZ3D_SL); break;
     case BGB_OP_MAXWELL3D_SL: BGB_LAUNCH_SING(BGB_OP_MAXWELL3D_SL); break;
@@ -709,42 +706,6 @@ void launch_singular(const OpParams& op, const QuadSel& qs, const RuleTable& rul
   }
 #undef BGB_LAUNCH_SING
 }
-// Entry groups (see launch_entry_groups): warp-aggregated counts and cursors, one atomic per
-// group present in a warp.
-template <bool FILL>
-__global__ void k_entry_groups(const int* __restrict__ es, int64_t n, const int* __restrict__ first_block,
-                               int* __restrict__ counts, int* __restrict__ cursor, int* __restrict__ perm) {
-  const int lane = threadIdx.x & 31;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); w < n; w += stride) {
-    const int64_t e = w + lane;
-    const bool valid = e < n;
-    const unsigned active = __ballot_sync(0xffffffffu, valid);
-    if (!valid) continue;
-    const int g = first_block[es[e]];
-    const unsigned peers = __match_any_sync(active, g);
-    const int leader = __ffs(peers) - 1;
-    if (!FILL) {
-      if (lane == leader) atomicAdd(&counts[g], __popc(peers));
-    } else {
-      int base = 0;
-      if (lane == leader) base = atomicAdd(&cursor[g], __popc(peers));
-      base = __shfl_sync(active, base, leader);
-      perm[base + __popc(peers & ((1u << lane) - 1u))] = (int)e;
-    }
-  }
-}
-
-void launch_entry_groups(bool fill, const int* es, int64_t n, const int* first_block, int* counts, int* cursor,
-                         int* perm, int num_sms, cudaStream_t st) {
-  if (n <= 0) return;
-  int64_t blocks = (n + 255) / 256;
-  if (blocks > (int64_t)num_sms * 8) blocks = (int64_t)num_sms * 8;
-  if (fill) k_entry_groups<true><<<(int)blocks, 256, 0, st>>>(es, n, first_block, counts, cursor, perm);
-  else k_entry_groups<false><<<(int)blocks, 256, 0, st>>>(es, n, first_block, counts, cursor, perm);
-}
-
-
 void launch_local_diag64(const OpParams& op, const QuadSel& qs, const RuleTable& rules, int rsA, int rsB,
                          const Geo64* tg, const Geo64* bg, const int* tau, const int* sigma, int64_t n, int force,
                          double2* out, int8_t* cls, int* err, int num_sms, cudaStream_t st, int16_t* mask) {
@@ -790,7 +751,7 @@ void launch_singular_batched(int op_kind, const OpParams* ops, const QuadSel& qs
   if (blocks > (int64_t)num_sms * 32) blocks = (int64_t)num_sms * 32;
 #define BGB_LAUNCH_SING(OPK)                                                                                  \
   k_singular<OPK, true><<<(int)blocks, 256, 0, st>>>(OpParams{}, ops, tri_problem, qs, rules, tg, bg, et, es, ec, n, \
-                                                     out, abort_flag, nullptr)
+                                                     out, abort_flag)
   switch (op_kind) {
     case BGB_OP_HELMHOLTZ3D_SL: BGB_LAUNCH_SING(BGB_OP_HELMHOLTZ3D_SL); break;
     case BGB_OP_MAXWELL3D_SL: BGB_LAUNCH_SING(BGB_OP_MAXWELL3D_SL); break;

@@ -175,17 +175,15 @@ __global__ void __launch_bounds__(256) k_singular_df(OpDf op1, const OpDf* __res
                                                      const GeoDf* __restrict__ bg, const int* __restrict__ ent_tau,
                                                      const int* __restrict__ ent_sigma, const int8_t* __restrict__ ent_cls,
                                                      const int16_t* __restrict__ ent_mask, int64_t n,
-                                                     double2* __restrict__ out, const volatile int* abort_flag,
-                                                     const int* __restrict__ perm) {
+                                                     double2* __restrict__ out, const volatile int* abort_flag) {
   __shared__ float4 trig[128];
   for (int i = threadIdx.x; i < 128; i += blockDim.x) trig[i] = ((const float4*)(tab + M.trig_off))[i];
   __syncthreads();
   constexpr int NA = DfAcc<OP>::N;
   const int lane = threadIdx.x & 31;
   const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
+  for (int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < n; e += warps) {
     if (abort_flag && *abort_flag) return;
-    const int64_t e = perm ? (int64_t)perm[i] : i;
     const int tau = ent_tau[e];
     const OpDf op = BATCH ? ops[tri_problem[tau]] : op1;
     const GeoDf A = tg[tau], B = bg[ent_sigma[e]];
@@ -421,7 +419,7 @@ OpDf make_opdf(const OpParams& op) {
 void launch_singular_df(int op_kind, const OpDf& op, const OpDf* opdf_array, const int* tri_problem,
                         const DfTables& M, const float* dtab, const GeoDf* tg, const GeoDf* bg, const int* et,
                         const int* es, const int8_t* ec, const int16_t* emask, int64_t n, double2* out,
-                        const volatile int* abort_flag, int num_sms, cudaStream_t st, const int* perm) {
+                        const volatile int* abort_flag, int num_sms, cudaStream_t st) {
   if (n <= 0) return;
   int64_t blocks = (n + 7) / 8;
   if (blocks > (int64_t)num_sms * 32) blocks = (int64_t)num_sms * 32;
@@ -429,10 +427,10 @@ void launch_singular_df(int op_kind, const OpDf& op, const OpDf* opdf_array, con
 #define BGB_LAUNCH_DF(OPK)                                                                                        \
   if (batch)                                                                                                      \
     k_singular_df<OPK, true><<<(int)blocks, 256, 0, st>>>(op, opdf_array, tri_problem, M, dtab, tg, bg, et, es, ec, \
-                                                          emask, n, out, abort_flag, perm);                             \
+                                                          emask, n, out, abort_flag);                             \
   else                                                                                                            \
     k_singular_df<OPK, false><<<(int)blocks, 256, 0, st>>>(op, opdf_array, tri_problem, M, dtab, tg, bg, et, es, ec, \
-                                                           emask, n, out, abort_flag, perm);
+                                                           emask, n, out, abort_flag);
   if (op_kind == BGB_OP_HELMHOLTZ3D_SL) {
     BGB_LAUNCH_DF(BGB_OP_HELMHOLTZ3D_SL)
   } else if (op_kind == BGB_OP_MAXWELL3D_SL) {

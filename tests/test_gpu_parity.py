@@ -191,10 +191,10 @@ def test_out_of_core_pipeline_pinned_pageable_and_ring(c1):
 
 
 @pytest.mark.parametrize("name", ["efie", "mfie", "hh"])
-def test_host_output_blocks_group_the_singular_pairs(plates, name):
-    """A host output in many column blocks integrates the singular and near pairs in groups, each
-    on a side stream just ahead of the first block that reads it: bit-identical to the one-block
-    device output in both precisions (the jittered plates put near pairs into most groups)."""
+def test_host_output_blocks_on_plates_with_near_pairs(plates, name):
+    """A host output in many column blocks (RWG and Lagrange, the jittered plates' near pairs in
+    most blocks), called twice on one handle and on a row window: bit-identical to the one-block
+    device output in both precisions."""
     make, which = OPS[name]
     sp = plates[which]
     op = make(K1)
@@ -202,7 +202,7 @@ def test_host_output_blocks_group_the_singular_pairs(plates, name):
     for prec, esz in (("fp64", 16), ("mixed", 8)):
         ref = bg.assemble_gpu(op, sp, sp, bg.GPUConfiguration(precision=prec), out="device").cpu().numpy()
         cfg = bg.GPUConfiguration(precision=prec, total_GPU_budget=4 * 23 * n * esz)
-        for _ in range(2):  # the second call reuses the handle's group buffers and events
+        for _ in range(2):  # the second call reuses the handle's staging buffers and events
             Z, st = bg.assemble_gpu(op, sp, sp, cfg, return_stats=True)
             assert st["out_blocks"] >= n // 23
             assert st["ms_singular"] > 0
