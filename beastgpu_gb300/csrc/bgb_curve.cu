@@ -1460,6 +1460,15 @@ int bgb_assemble_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_curve_
     const int64_t min_cols = ((int64_t)32 << 20) / std::max<int64_t>(1, nrows * (int64_t)esz);
     cols_per_block = std::min(cols_per_block, std::max<int64_t>((ncols + 7) / 8, std::max<int64_t>(1, min_cols)));
   }
+  // Block boundaries.  With host outputs the last block is cut to about a quarter: its copy is
+  // the one not hidden behind the next block's kernels.
+  std::vector<int64_t> col_start;
+  for (int64_t c = 0; c < ncols; c += cols_per_block) col_start.push_back(c);
+  if (host_out && col_start.size() >= 4) {
+    const int64_t last = std::max<int64_t>(1, ncols - std::max<int64_t>(1, (cols_per_block + 3) / 4));
+    if (last > col_start.back()) col_start.push_back(last);
+  }
+  col_start.push_back(ncols);
   double ms_cls = 0, ms_far = 0, ms_sp = 0, ms_copy_acc = 0;
   int pending[2] = {0, 0};  // staging slot holds a copy in flight
   auto finish_copy = [&](int slot) -> int {
@@ -1475,9 +1484,9 @@ int bgb_assemble_curve(bgb_handle* h, const bgb_operator2d* op, const bgb_curve_
   int cap = std::max(1 << 16, 8 * nT);
   // the block loop; on any early return the copies still in flight are drained below
   auto run_blocks = [&]() -> int {
-  for (int64_t c0 = 0; c0 < ncols; c0 += cols_per_block) {
+  for (size_t bi = 0; bi + 1 < col_start.size(); ++bi) {
     if (h->abort_host && *h->abort_host) { set_error("aborted by bgb_abort"); return BGB_ERR_ABORTED; }
-    const int64_t c1 = std::min(ncols, c0 + cols_per_block);
+    const int64_t c0 = col_start[bi], c1 = col_start[bi + 1];
     ++nblocks;
     CurveSupports BS = curve_supports(trial, c0, c1);
     std::vector<int> S, bcode;
