@@ -228,7 +228,7 @@ FarConst make_farconst(const OpParams& op, const RuleTable& R, const QuadSel& qs
 }
 
 // ----------------------------------------------------------------------------------------
-// Host planning: Morton-ordered function blocks and their triangle sets
+// Host planning: function blocks (bisection patches) and their triangle sets
 // ----------------------------------------------------------------------------------------
 // Tile configurations: (FM, FN, SC) per precision.
 const TileCfg kTileCfgs[] = {
@@ -806,10 +806,13 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
     const Supports St = build_supports(test);
     const Supports Sb_own = same ? Supports() : build_supports(trial);
     const Supports& Sb = same ? St : Sb_own;
-    const std::vector<int> rank_t = morton_rank(test);
-    const std::vector<int> rank_b = same ? rank_t : morton_rank(trial);
-    const std::vector<int> ord_t = order_functions(St, rank_t, (int)row0, (int)(row0 + nrows));
+    const std::vector<double> cent_t = function_centres(test, St);
+    const std::vector<double> cent_b_own = same ? std::vector<double>() : function_centres(trial, Sb);
+    const std::vector<double>& cent_b = same ? cent_t : cent_b_own;
+    // function orders in runs of the tile widths (recomputed only when a width changes)
+    std::vector<int> ord_t;
     std::vector<std::vector<int>> ord_b(nblocks);
+    int ord_fm = -1, ord_fn = -1;
     // per output block: function order and trial-side plan, blocks spread over the planner's threads
     auto over_blocks = [&](auto fn) {
       if (nblocks == 1) {
@@ -824,10 +827,19 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
         });
       for (auto& x : th) x.join();
     };
-    over_blocks([&](int b, int) { ord_b[b] = order_functions(Sb, rank_b, (int)col_start[b], (int)col_start[b + 1]); });
     size_t smem = 0;
     for (int id : prefs) {
       const TileCfg tc = kTileCfgs[id];
+      if (tc.FM != ord_fm) {
+        ord_t = order_functions(St, cent_t, (int)row0, (int)(row0 + nrows), tc.FM);
+        ord_fm = tc.FM;
+      }
+      if (tc.FN != ord_fn) {
+        over_blocks([&](int b, int) {
+          ord_b[b] = order_functions(Sb, cent_b, (int)col_start[b], (int)col_start[b + 1], tc.FN);
+        });
+        ord_fn = tc.FN;
+      }
       PL.test = HostPlan();
       plan_test_side_par(St, ord_t, tc.FM, row0, PL.test, nth);
       PL.trial.assign(nblocks, HostPlan());

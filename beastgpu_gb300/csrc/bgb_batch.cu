@@ -122,7 +122,7 @@ int enqueue_device_work(bgb_batch* B, cudaStream_t st, bool far_only) {
 
 // Plans of every problem for tile configuration `cfg`; uploads them and the work items.
 int build_plans(bgb_batch* B, const bgb_problem* pr, const std::vector<Supports>& St, const std::vector<Supports>& Sb,
-                const std::vector<std::vector<int>>& ord_t, const std::vector<std::vector<int>>& ord_b,
+                const std::vector<std::vector<double>>& cent_t, const std::vector<std::vector<double>>& cent_b,
                 const std::vector<int>& tbase, const std::vector<int>& bbase, int cfg, int schedule, bool upload_all,
                 size_t* smem_out) {
   const TileCfg tc = kTileCfgs[cfg];
@@ -131,8 +131,9 @@ int build_plans(bgb_batch* B, const bgb_problem* pr, const std::vector<Supports>
   // one shared-memory layout for the whole launch: the batch-wide maxima
   int tmax = 1, nmax = 1, MAXS = 1, gmax = 1, gsmax = 1;
   for (int p = 0; p < n; ++p) {
-    plan_test_side(St[p], ord_t[p], tc.FM, 0, P[p]);
-    plan_trial_side(Sb[p], ord_b[p], tc.FN, tc.SC, P[p]);
+    // function orders in runs of this configuration's tile widths
+    plan_test_side(St[p], order_functions(St[p], cent_t[p], 0, pr[p].test.nfun, tc.FM), tc.FM, 0, P[p]);
+    plan_trial_side(Sb[p], order_functions(Sb[p], cent_b[p], 0, pr[p].trial.nfun, tc.FN), tc.FN, tc.SC, P[p]);
     for (int& t : P[p].tb_tris) t += tbase[p];
     for (int& t : P[p].bb_tris) t += bbase[p];
     tmax = std::max(tmax, P[p].tmax); nmax = std::max(nmax, P[p].nmax); MAXS = std::max(MAXS, P[p].MAXS);
@@ -413,18 +414,16 @@ int bgb_batch_create(bgb_handle* h, int32_t n, const bgb_problem* problems, int3
   // all device stages once, eagerly (sizes the pair list, and is the first assembly)
   // host plans
   std::vector<Supports> St(n), Sb(n);
-  std::vector<std::vector<int>> ord_t(n), ord_b(n);
+  std::vector<std::vector<double>> cent_t(n), cent_b(n);
   for (int p = 0; p < n; ++p) {
     St[p] = build_supports(&problems[p].test);
-    std::vector<int> rt = morton_rank(&problems[p].test);
-    ord_t[p] = order_functions(St[p], rt, 0, problems[p].test.nfun);
+    cent_t[p] = function_centres(&problems[p].test, St[p]);
     if (same_space(&problems[p].test, &problems[p].trial)) {
       Sb[p] = St[p];
-      ord_b[p] = ord_t[p];
+      cent_b[p] = cent_t[p];
     } else {
       Sb[p] = build_supports(&problems[p].trial);
-      std::vector<int> rb = morton_rank(&problems[p].trial);
-      ord_b[p] = order_functions(Sb[p], rb, 0, problems[p].trial.nfun);
+      cent_b[p] = function_centres(&problems[p].trial, Sb[p]);
     }
   }
   int smem_max = 0;
@@ -441,11 +440,11 @@ int bgb_batch_create(bgb_handle* h, int32_t n, const bgb_problem* problems, int3
   int first = -1;
   size_t smem = 0;
   for (int c : cands) {
-    if ((rc = build_plans(B, problems, St, Sb, ord_t, ord_b, tbase, bbase, c, 1, false, &smem))) return fail(rc);
+    if ((rc = build_plans(B, problems, St, Sb, cent_t, cent_b, tbase, bbase, c, 1, false, &smem))) return fail(rc);
     if (smem <= (size_t)smem_max) { first = c; break; }
   }
   if (first < 0) { set_error("bgb_batch_create: no tile shape fits shared memory"); return fail(BGB_ERR_CAPACITY); }
-  if ((rc = build_plans(B, problems, St, Sb, ord_t, ord_b, tbase, bbase, first, 1, true, &smem))) return fail(rc);
+  if ((rc = build_plans(B, problems, St, Sb, cent_t, cent_b, tbase, bbase, first, 1, true, &smem))) return fail(rc);
   auto set_cfg = [&](int cfg, size_t sm) -> int {
     B->cfg_id = cfg;
     B->smem = sm;
@@ -468,9 +467,9 @@ int bgb_batch_create(bgb_handle* h, int32_t n, const bgb_problem* problems, int3
     best_ms = 1e30;
     for (int c : cands)
       for (int sched = 0; sched < 2; ++sched) {
-        if ((rc = build_plans(B, problems, St, Sb, ord_t, ord_b, tbase, bbase, c, sched, false, &smem))) return fail(rc);
+        if ((rc = build_plans(B, problems, St, Sb, cent_t, cent_b, tbase, bbase, c, sched, false, &smem))) return fail(rc);
         if (smem > (size_t)smem_max) continue;
-        if ((rc = build_plans(B, problems, St, Sb, ord_t, ord_b, tbase, bbase, c, sched, true, &smem)) || (rc = set_cfg(c, smem)))
+        if ((rc = build_plans(B, problems, St, Sb, cent_t, cent_b, tbase, bbase, c, sched, true, &smem)) || (rc = set_cfg(c, smem)))
           return fail(rc);
         if ((rc = enqueue_device_work(B, st, true))) return fail(rc);  // warm-up
         cudaEventRecord(B->ev[0], st);
@@ -480,7 +479,7 @@ int bgb_batch_create(bgb_handle* h, int32_t n, const bgb_problem* problems, int3
         const double ms = event_ms(B->ev[0], B->ev[1]);
         if (ms < best_ms) { best_ms = ms; best_cfg = c; best_sched = sched; }
       }
-    if ((rc = build_plans(B, problems, St, Sb, ord_t, ord_b, tbase, bbase, best_cfg, best_sched, true, &smem)) ||
+    if ((rc = build_plans(B, problems, St, Sb, cent_t, cent_b, tbase, bbase, best_cfg, best_sched, true, &smem)) ||
         (rc = set_cfg(best_cfg, smem)))
       return fail(rc);
   }

@@ -1,7 +1,7 @@
 // Far-pair tile kernels (plain FP64 and mixed FP32) with the deterministic gather write.
 //
 // A CTA owns one output tile: a block of test functions (rows) x a block of trial
-// functions (columns), both taken from a Morton-ordered sweep so their supports are compact.
+// functions (columns), each a compact patch of a recursive coordinate bisection of the functions.
 // It stages the triangles supporting those functions ("halo" included) in shared memory,
 // sweeps the trial triangles in chunks, computes the 3x3 local matrix of every (test
 // triangle, trial triangle) pair of the chunk into shared memory, and then lets each thread

@@ -122,9 +122,11 @@ RuleTable make_rules();
 // no second reduction (phase_direct).
 FarConst make_farconst(const OpParams& op, const RuleTable& R, const QuadSel& qs, const bgb_space* test = nullptr,
                        const bgb_space* trial = nullptr);
-std::vector<int> morton_rank(const bgb_space* s);
 Supports build_supports(const bgb_space* s);
-std::vector<int> order_functions(const Supports& S, const std::vector<int>& rank, int f_begin, int f_end);
+std::vector<double> function_centres(const bgb_space* s, const Supports& S);
+// Functions [f_begin, f_end) in recursive-bisection order of their centres, in compact runs of `leaf`.
+std::vector<int> order_functions(const Supports& S, const std::vector<double>& centre, int f_begin, int f_end,
+                                 int leaf);
 // Test-side tiles: up to FM functions and at most tcap distinct triangles per tile.
 void plan_test_side(const Supports& S, const std::vector<int>& order, int FM, int64_t row0, HostPlan& P,
                     int tcap = 1 << 30);

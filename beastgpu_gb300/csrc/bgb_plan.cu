@@ -1,4 +1,4 @@
-// Host-side tile planning of the far-pair kernel: Morton order of the functions, supports,
+// Host-side tile planning of the far-pair kernel: bisection order of the functions, supports,
 // and the per-tile tables (triangles of a block of test / trial functions, the slot and local
 // shape of each support, the trial-side groups per chunk).  The plan of one side is built in
 // parallel over ranges of function blocks and merged by shifting offsets, so the result does
@@ -11,60 +11,6 @@
 #include <vector>
 
 namespace bgb {
-
-static inline uint64_t spread3(uint64_t x) {
-  x &= 0x1fffff;
-  x = (x | x << 32) & 0x1f00000000ffffULL;
-  x = (x | x << 16) & 0x1f0000ff0000ffULL;
-  x = (x | x << 8) & 0x100f00f00f00f00fULL;
-  x = (x | x << 4) & 0x10c30c30c30c30c3ULL;
-  x = (x | x << 2) & 0x1249249249249249ULL;
-  return x;
-}
-
-// Morton position of every triangle (rank in the order of 3-D Morton codes of centroids).
-std::vector<int> morton_rank(const bgb_space* s) {
-  const int nt = s->nt;
-  std::vector<double> c(3 * (size_t)nt);
-  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-  for (int t = 0; t < nt; ++t)
-    for (int k = 0; k < 3; ++k) {
-      double v = 0;
-      for (int a = 0; a < 3; ++a) v += s->vertices[3 * (int64_t)s->triangles[3 * (int64_t)t + a] + k];
-      v /= 3.0;
-      c[3 * (size_t)t + k] = v;
-      lo[k] = std::min(lo[k], v);
-      hi[k] = std::max(hi[k], v);
-    }
-  double span = std::max({hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2], 1e-300});
-  std::vector<uint64_t> code((size_t)nt);
-  uint64_t all_or = 0;
-  for (int t = 0; t < nt; ++t) {
-    uint64_t cd = 0;
-    for (int k = 0; k < 3; ++k) {
-      double f = (c[3 * (size_t)t + k] - lo[k]) / span;
-      uint64_t q = (uint64_t)std::min(std::max(f, 0.0) * 2097151.0, 2097151.0);
-      cd |= spread3(q) << k;
-    }
-    code[(size_t)t] = cd;
-    all_or |= cd;
-  }
-  // Triangles by (code, index): a stable LSD radix sort of the indices, 8 bits a pass, passes
-  // over bytes that are zero in every code skipped.
-  std::vector<int> idx((size_t)nt), tmp((size_t)nt);
-  for (int t = 0; t < nt; ++t) idx[(size_t)t] = t;
-  for (int shift = 0; shift < 64; shift += 8) {
-    if (((all_or >> shift) & 0xff) == 0) continue;
-    size_t cnt[257] = {0};
-    for (int t = 0; t < nt; ++t) ++cnt[((code[(size_t)idx[(size_t)t]] >> shift) & 0xff) + 1];
-    for (int d = 0; d < 256; ++d) cnt[d + 1] += cnt[d];
-    for (int t = 0; t < nt; ++t) tmp[cnt[(code[(size_t)idx[(size_t)t]] >> shift) & 0xff]++] = idx[(size_t)t];
-    idx.swap(tmp);
-  }
-  std::vector<int> rank(nt);
-  for (int i = 0; i < nt; ++i) rank[(size_t)idx[(size_t)i]] = i;
-  return rank;
-}
 
 Supports build_supports(const bgb_space* s) {
   Supports S;
@@ -91,31 +37,70 @@ Supports build_supports(const bgb_space* s) {
   return S;
 }
 
-// Functions [f_begin, f_end) ordered by the Morton rank of their first support (ties, and
-// functions without supports last, in index order).  The ranks are < rank.size(): a counting
-// sort when the range is not much smaller than the triangle count, a comparison sort else.
-std::vector<int> order_functions(const Supports& S, const std::vector<int>& rank, int f_begin, int f_end) {
-  const int n = std::max(0, f_end - f_begin);
-  const int64_t none = (int64_t)rank.size();  // key of a function without supports
-  std::vector<int64_t> key((size_t)n);
-  for (int f = f_begin; f < f_end; ++f) {
-    int64_t first = none;
-    for (int64_t k = S.off[f]; k < S.off[f + 1]; ++k) first = std::min<int64_t>(first, rank[S.tri[k]]);
-    key[(size_t)(f - f_begin)] = first;
+// Centre of every function: the mean of the centroids of its support triangles.
+std::vector<double> function_centres(const bgb_space* s, const Supports& S) {
+  std::vector<double> tc(3 * (size_t)s->nt);
+  for (int64_t t = 0; t < s->nt; ++t)
+    for (int k = 0; k < 3; ++k) {
+      double v = 0;
+      for (int a = 0; a < 3; ++a) v += s->vertices[3 * (int64_t)s->triangles[3 * t + a] + k];
+      tc[3 * (size_t)t + k] = v / 3.0;
+    }
+  std::vector<double> fc(3 * (size_t)s->nfun, 0.0);
+  for (int f = 0; f < s->nfun; ++f) {
+    const int64_t n = S.off[f + 1] - S.off[f];
+    if (n == 0) continue;
+    for (int64_t k = S.off[f]; k < S.off[f + 1]; ++k)
+      for (int c = 0; c < 3; ++c) fc[3 * (size_t)f + c] += tc[3 * (size_t)S.tri[k] + c];
+    for (int c = 0; c < 3; ++c) fc[3 * (size_t)f + c] /= (double)n;
   }
-  std::vector<int> out((size_t)n);
-  if ((int64_t)n * 4 >= none) {
-    std::vector<int> cnt((size_t)none + 2, 0);
-    for (int i = 0; i < n; ++i) ++cnt[(size_t)key[(size_t)i] + 1];
-    for (int64_t d = 0; d <= none; ++d) cnt[(size_t)d + 1] += cnt[(size_t)d];
-    for (int i = 0; i < n; ++i) out[(size_t)cnt[(size_t)key[(size_t)i]]++] = f_begin + i;
-  } else {
-    std::vector<std::pair<int64_t, int>> kp((size_t)n);
-    for (int i = 0; i < n; ++i) kp[(size_t)i] = {key[(size_t)i], f_begin + i};
-    std::sort(kp.begin(), kp.end());
-    for (int i = 0; i < n; ++i) out[(size_t)i] = kp[(size_t)i].second;
+  return fc;
+}
+
+// Functions [f_begin, f_end) in the order of a recursive coordinate bisection of their centres:
+// a range is split across its longest extent at a multiple of `leaf` functions near its middle,
+// down to ranges of at most `leaf`, so every aligned run of `leaf` functions (a tile of the far
+// kernel) is a compact patch and the triangles its supports share are few.  Ties go by function
+// index, each leaf is in index order (the order does not depend on the sort's implementation),
+// and functions without supports come last.
+std::vector<int> order_functions(const Supports& S, const std::vector<double>& centre, int f_begin, int f_end,
+                                 int leaf) {
+  leaf = std::max(1, leaf);
+  std::vector<int> idx, none;
+  idx.reserve((size_t)std::max(0, f_end - f_begin));
+  for (int f = f_begin; f < f_end; ++f) (S.off[f + 1] > S.off[f] ? idx : none).push_back(f);
+  struct Range { size_t lo, hi; };
+  std::vector<Range> stack{{0, idx.size()}};
+  while (!stack.empty()) {
+    const Range r = stack.back();
+    stack.pop_back();
+    const size_t n = r.hi - r.lo;
+    if (n <= (size_t)leaf) {
+      std::sort(idx.begin() + (std::ptrdiff_t)r.lo, idx.begin() + (std::ptrdiff_t)r.hi);
+      continue;
+    }
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (size_t i = r.lo; i < r.hi; ++i)
+      for (int c = 0; c < 3; ++c) {
+        const double v = centre[3 * (size_t)idx[i] + c];
+        lo[c] = std::min(lo[c], v);
+        hi[c] = std::max(hi[c], v);
+      }
+    int ax = 0;
+    for (int c = 1; c < 3; ++c)
+      if (hi[c] - lo[c] > hi[ax] - lo[ax]) ax = c;
+    size_t nl = (n / 2 + (size_t)leaf / 2) / (size_t)leaf * (size_t)leaf;
+    nl = std::min(std::max(nl, (size_t)leaf), n - 1);
+    std::nth_element(idx.begin() + (std::ptrdiff_t)r.lo, idx.begin() + (std::ptrdiff_t)(r.lo + nl),
+                     idx.begin() + (std::ptrdiff_t)r.hi, [&](int a, int b) {
+                       const double va = centre[3 * (size_t)a + ax], vb = centre[3 * (size_t)b + ax];
+                       return va < vb || (va == vb && a < b);
+                     });
+    stack.push_back({r.lo, r.lo + nl});
+    stack.push_back({r.lo + nl, r.hi});
   }
-  return out;
+  idx.insert(idx.end(), none.begin(), none.end());
+  return idx;
 }
 
 void plan_test_side(const Supports& S, const std::vector<int>& order, int FM, int64_t row0, HostPlan& P, int tcap) {
