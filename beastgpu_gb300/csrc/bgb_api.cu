@@ -831,13 +831,16 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
     for (int id : prefs) {
       const TileCfg tc = kTileCfgs[id];
       if (tc.FM != ord_fm) {
-        ord_t = order_functions(St, cent_t, (int)row0, (int)(row0 + nrows), tc.FM);
+        ord_t = order_functions(St, cent_t, (int)row0, (int)(row0 + nrows), tc.FM, nth);
         ord_fm = tc.FM;
       }
       if (tc.FN != ord_fn) {
-        over_blocks([&](int b, int) {
-          ord_b[b] = order_functions(Sb, cent_b, (int)col_start[b], (int)col_start[b + 1], tc.FN);
-        });
+        if (same && nblocks == 1 && row0 == 0 && nrows == ncols && tc.FN == tc.FM)
+          ord_b[0] = ord_t;  // the same functions and width: the same order
+        else
+          over_blocks([&](int b, int threads) {
+            ord_b[b] = order_functions(Sb, cent_b, (int)col_start[b], (int)col_start[b + 1], tc.FN, threads);
+          });
         ord_fn = tc.FN;
       }
       PL.test = HostPlan();

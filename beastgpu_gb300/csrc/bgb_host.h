@@ -126,7 +126,7 @@ Supports build_supports(const bgb_space* s);
 std::vector<double> function_centres(const bgb_space* s, const Supports& S);
 // Functions [f_begin, f_end) in recursive-bisection order of their centres, in compact runs of `leaf`.
 std::vector<int> order_functions(const Supports& S, const std::vector<double>& centre, int f_begin, int f_end,
-                                 int leaf);
+                                 int leaf, int nth = 1);
 // Test-side tiles: up to FM functions and at most tcap distinct triangles per tile.
 void plan_test_side(const Supports& S, const std::vector<int>& order, int FM, int64_t row0, HostPlan& P,
                     int tcap = 1 << 30);

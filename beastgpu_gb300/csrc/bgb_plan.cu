@@ -62,23 +62,18 @@ std::vector<double> function_centres(const bgb_space* s, const Supports& S) {
 // down to ranges of at most `leaf`, so every aligned run of `leaf` functions (a tile of the far
 // kernel) is a compact patch and the triangles its supports share are few.  Ties go by function
 // index, each leaf is in index order (the order does not depend on the sort's implementation),
-// and functions without supports come last.
+// and functions without supports come last.  The first levels are split on the calling thread,
+// the ranges below them on up to nth threads; the result does not depend on nth.
 std::vector<int> order_functions(const Supports& S, const std::vector<double>& centre, int f_begin, int f_end,
-                                 int leaf) {
+                                 int leaf, int nth) {
   leaf = std::max(1, leaf);
   std::vector<int> idx, none;
   idx.reserve((size_t)std::max(0, f_end - f_begin));
   for (int f = f_begin; f < f_end; ++f) (S.off[f + 1] > S.off[f] ? idx : none).push_back(f);
   struct Range { size_t lo, hi; };
-  std::vector<Range> stack{{0, idx.size()}};
-  while (!stack.empty()) {
-    const Range r = stack.back();
-    stack.pop_back();
+  // one bisection step of r (n > leaf) into its two halves
+  auto split = [&](const Range& r, Range& a, Range& b) {
     const size_t n = r.hi - r.lo;
-    if (n <= (size_t)leaf) {
-      std::sort(idx.begin() + (std::ptrdiff_t)r.lo, idx.begin() + (std::ptrdiff_t)r.hi);
-      continue;
-    }
     double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
     for (size_t i = r.lo; i < r.hi; ++i)
       for (int c = 0; c < 3; ++c) {
@@ -92,12 +87,58 @@ std::vector<int> order_functions(const Supports& S, const std::vector<double>& c
     size_t nl = (n / 2 + (size_t)leaf / 2) / (size_t)leaf * (size_t)leaf;
     nl = std::min(std::max(nl, (size_t)leaf), n - 1);
     std::nth_element(idx.begin() + (std::ptrdiff_t)r.lo, idx.begin() + (std::ptrdiff_t)(r.lo + nl),
-                     idx.begin() + (std::ptrdiff_t)r.hi, [&](int a, int b) {
-                       const double va = centre[3 * (size_t)a + ax], vb = centre[3 * (size_t)b + ax];
-                       return va < vb || (va == vb && a < b);
+                     idx.begin() + (std::ptrdiff_t)r.hi, [&](int x, int y) {
+                       const double vx = centre[3 * (size_t)x + ax], vy = centre[3 * (size_t)y + ax];
+                       return vx < vy || (vx == vy && x < y);
                      });
-    stack.push_back({r.lo, r.lo + nl});
-    stack.push_back({r.lo + nl, r.hi});
+    a = {r.lo, r.lo + nl};
+    b = {r.lo + nl, r.hi};
+  };
+  // the whole bisection below r
+  auto finish = [&](const Range& root) {
+    std::vector<Range> stack{root};
+    while (!stack.empty()) {
+      const Range r = stack.back();
+      stack.pop_back();
+      if (r.hi - r.lo <= (size_t)leaf) {
+        std::sort(idx.begin() + (std::ptrdiff_t)r.lo, idx.begin() + (std::ptrdiff_t)r.hi);
+        continue;
+      }
+      Range a, b;
+      split(r, a, b);
+      stack.push_back(a);
+      stack.push_back(b);
+    }
+  };
+  nth = std::max(1, nth);
+  std::vector<Range> level{{0, idx.size()}};
+  while (nth > 1 && level.size() < 4 * (size_t)nth) {
+    std::vector<Range> next;
+    bool any = false;
+    for (const Range& r : level) {
+      if (r.hi - r.lo <= (size_t)leaf) {
+        next.push_back(r);
+        continue;
+      }
+      Range a, b;
+      split(r, a, b);
+      next.push_back(a);
+      next.push_back(b);
+      any = true;
+    }
+    level.swap(next);
+    if (!any) break;
+  }
+  if (nth == 1 || level.size() == 1) {
+    for (const Range& r : level) finish(r);
+  } else {
+    std::vector<std::thread> th;
+    const int nt = (int)std::min<size_t>((size_t)nth, level.size());
+    for (int t = 0; t < nt; ++t)
+      th.emplace_back([&, t] {
+        for (size_t i = (size_t)t; i < level.size(); i += (size_t)nt) finish(level[i]);
+      });
+    for (auto& x : th) x.join();
   }
   idx.insert(idx.end(), none.begin(), none.end());
   return idx;
