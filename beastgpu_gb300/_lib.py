@@ -111,6 +111,8 @@ SIGNATURES = {
     "bgb_assemble_curve": ([C.c_void_p, C.POINTER(Operator2D), C.POINTER(CurveSpace), C.POINTER(CurveSpace),
                             C.POINTER(QuadStrat2D), C.c_int32, C.c_void_p, C.c_int32, C.c_int64, C.c_int64, C.c_int64,
                             C.c_void_p, C.POINTER(Stats)], C.c_int),
+    "bgb_plan_order": ([C.POINTER(Space), C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.POINTER(C.c_int64)],
+                       C.c_int),
     "bgb_local_matrices_curve": ([C.c_void_p, C.POINTER(Operator2D), C.POINTER(CurveSpace), C.POINTER(CurveSpace),
                                   C.POINTER(QuadStrat2D), C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, C.c_int32,
                                   C.c_void_p, C.c_void_p], C.c_int),

@@ -305,6 +305,20 @@ def assemble(operator: Operator, test_functions: Space, trial_functions: Space, 
                         quadstrat=quadstrat, **kw)
 
 
+def tile_order(space: Space, width: int = 64, functions=None):
+    """The far kernel's tiling of one side, computed on the host (no GPU): the order in which tiles
+    of `width` functions take the functions [f0, f1) (`functions`, default all) and the number of
+    (tile, support triangle) slots those tiles stage (the triangles per side the far kernel
+    evaluates, halo included)."""
+    f0, f1 = (0, space.nfun) if functions is None else (int(functions[0]), int(functions[1]))
+    keep = _Keep()
+    order = np.empty(max(0, f1 - f0), dtype=np.int32)
+    slots = C.c_int64(0)
+    _lib.check(_lib.load().bgb_plan_order(C.byref(c_space(space, keep)), f0, f1, int(width), order.ctypes.data,
+                                          C.byref(slots)))
+    return order, int(slots.value)
+
+
 def classify(test_functions: Space, trial_functions: Space, k2: float, block=None, device: int = 0):
     """Pair classes (0 far, 1 CV, 2 CE, 3 CF, 4 near) of a block of triangle pairs on the GPU."""
     t0, t1, s0, s1 = block or (0, test_functions.mesh.nt, 0, trial_functions.mesh.nt)

@@ -588,6 +588,24 @@ int bgb_tile_info(int32_t* ids, int32_t cap) {
   return kNumTileCfgs;
 }
 
+int bgb_plan_order(const bgb_space* s, int32_t f_begin, int32_t f_end, int32_t width, int32_t* order,
+                   int64_t* slots) {
+  int rc;
+  if (!s || !order || !slots || width < 1) { set_error("bgb_plan_order: invalid argument"); return BGB_ERR_INVALID; }
+  if ((rc = validate_space(s, "space"))) return rc;
+  if (f_begin < 0 || f_end < f_begin || f_end > s->nfun) {
+    set_error("bgb_plan_order: function range [%d, %d) outside [0, %d)", f_begin, f_end, s->nfun);
+    return BGB_ERR_INVALID;
+  }
+  const Supports S = build_supports(s);
+  const std::vector<int> ord = order_functions(S, function_centres(s, S), f_begin, f_end, width, planner_threads());
+  HostPlan P;
+  plan_test_side(S, ord, width, 0, P);
+  std::copy(ord.begin(), ord.end(), order);
+  *slots = (int64_t)P.tb_tris.size();
+  return 0;
+}
+
 int bgb_measure_issue_peaks(bgb_handle* h, double* fp32, double* fp64, double* mufu) {
   if (!h || !fp32 || !fp64 || !mufu) { set_error("invalid argument"); return BGB_ERR_INVALID; }
   cudaSetDevice(h->device);

@@ -298,6 +298,15 @@ int bgb_abort(bgb_handle* h);
 /* Tile shapes compiled into the far-pair kernel: fills up to `cap` ids, returns the count. */
 int bgb_tile_info(int32_t* ids, int32_t cap);
 
+/* Far-kernel tiling of one side, on the host (no device needed): the order in which tiles of
+ * `width` functions take the functions [f_begin, f_end) of `s` (order[f_end - f_begin]; each run
+ * of `width` is one tile, a compact patch of a recursive coordinate bisection of the functions'
+ * centres) and, in *slots, the number of (tile, support triangle) entries those tiles stage, i.e.
+ * the triangles per side the far kernel evaluates, halo included.  The tiling replaces the square
+ * tiles of the reference's scheduler (GPU_scheduler.jl:108-129); it does not change any value. */
+int bgb_plan_order(const bgb_space* s, int32_t f_begin, int32_t f_end, int32_t width, int32_t* order,
+                   int64_t* slots);
+
 /* FP32 / FP64 FMA issue peaks and MUFU throughput measured on the handle's device
  * (TFLOP/s, TFLOP/s, Tops/s), for roofline denominators. */
 int bgb_measure_issue_peaks(bgb_handle* h, double* fp32_tflops, double* fp64_tflops, double* mufu_tops);
