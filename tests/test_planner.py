@@ -79,3 +79,35 @@ def test_tile_order_rejects_bad_arguments(spaces):
         tile_order(X, 64, functions=(10, X.nfun + 1))
     with pytest.raises(_lib.BGBError, match="invalid"):
         tile_order(X, 0)
+
+
+def _with(X, vertices=None, triangles=None, fn_index=None, fn_coef=None, nfun=None, refspace=None):
+    m = X.mesh
+    mesh = bg.Mesh(m.vertices if vertices is None else vertices, m.triangles if triangles is None else triangles)
+    return bg.Space(mesh, X.refspace if refspace is None else refspace, X.fn_index if fn_index is None else fn_index,
+                    X.fn_coef if fn_coef is None else fn_coef, X.nfun if nfun is None else nfun)
+
+
+def test_space_validation_on_the_host(spaces):
+    """The library's space checks (the same for every entry point) fail cleanly with a message."""
+    X = spaces["rwg_sphere"]
+    v = X.mesh.vertices.copy()
+    v[5, 1] = np.nan
+    t_bad = X.mesh.triangles.copy()
+    t_bad[7, 2] = X.mesh.vertices.shape[0]
+    t_deg = X.mesh.triangles.copy()
+    t_deg[3, 1] = t_deg[3, 0]
+    f_big = X.fn_index.copy()
+    f_big[2, 0] = X.nfun
+    f_dup = X.fn_index.copy()
+    f_dup[4, 1] = f_dup[4, 0]
+    c_bad = X.fn_coef.copy()
+    c_bad[9, 2] = np.inf
+    cases = [(dict(vertices=v), "non-finite vertex"), (dict(triangles=t_bad), "vertex index"),
+             (dict(triangles=t_deg), "degenerate"), (dict(fn_index=f_big), "function index"),
+             (dict(fn_index=f_dup), "two local shapes"), (dict(fn_coef=c_bad), "non-finite coefficient"),
+             (dict(refspace=7), "refspace")]
+    for kw, msg in cases:
+        with pytest.raises(_lib.BGBError, match=msg):
+            tile_order(_with(X, **kw), 64)
+    tile_order(X, 64)  # the original space still passes
