@@ -15,7 +15,6 @@
 #include "bgb_kernels.cuh"
 
 #include <cmath>
-#include <mutex>
 
 namespace bgb {
 namespace {
@@ -23,25 +22,15 @@ namespace {
 constexpr size_t kNoAllocScratchBytes = (size_t)16 << 20;  // 16 MiB per device
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-void* g_scratch_addr[kMaxDevices] = {};
-
-// Device address of the scratch array on the current device, looked up once per device
-// (with that device current) and cached.
-int scratch_address(int dev, void** out) {
-  if (dev < 0 || dev >= kMaxDevices) {
-    set_error("device ordinal %d not supported by the no-allocation entry point", dev);
-    return BGB_ERR_INVALID;
-  }
-  std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_scratch_addr[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(no-allocation scratch)");
-    g_scratch_addr[dev] = p;
-  }
-  *out = g_scratch_addr[dev];
+// Device address of the scratch array on the current device.  Looked up on every call, with
+// the caller's device current: the address belongs to the device's current context, and a
+// cached address would dangle after the context is reset (cudaDeviceReset, CUDA.jl's
+// device_reset!).  The lookup costs far less than the pair-count read-back of every call.
+int scratch_address(void** out) {
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(no-allocation scratch)");
+  *out = p;
   return 0;
 }
 
@@ -53,10 +42,11 @@ __global__ void k_prepare_geo64_checked(const double* __restrict__ verts, const 
   if (t >= nt) return;
   Geo64 g;
   for (int a = 0; a < 3; ++a) {
-    int vi = tris[3 * t + a];
-    if (vi < 0 || vi >= nv) {
+    const int vi = tris[3 * t + a];
+    if (vi < 0 || vi >= nv) {  // flagged, and no vertex is read: the triangle gets zero coordinates
       atomicOr(err, 2);
-      vi = 0;
+      for (int c = 0; c < 3; ++c) g.v[a][c] = 0.0;
+      continue;
     }
     for (int c = 0; c < 3; ++c) g.v[a][c] = verts[3 * (int64_t)vi + c];
   }
@@ -95,9 +85,14 @@ extern "C" int bgb_classify_csr_noalloc(const double* d_vertices_test, const int
                       up256(sizeof(float4) * (size_t)nt_trial) + up256(sizeof(int) * ((size_t)nt_test + 1));
   if (need > kNoAllocScratchBytes) {
     set_error("bgb_classify_csr_noalloc: %d test + %d trial triangles need %zu bytes of scratch, more than the "
-              "fixed %zu bytes (about 170,000 triangles in total); use bgb_assemble / bgb_classify_block",
+              "fixed %zu bytes (156 bytes per test and 152 per trial triangle: about 54,000 triangles per side "
+              "when both sides are equal); use bgb_assemble / bgb_classify_block",
               nt_test, nt_trial, need, kNoAllocScratchBytes);
     return BGB_ERR_CAPACITY;
+  }
+  if ((nt_test > 0 && nv_test == 0) || (nt_trial > 0 && nv_trial == 0)) {
+    set_error("bgb_classify_csr_noalloc: triangles without vertices (nt > 0 and nv == 0)");
+    return BGB_ERR_INVALID;
   }
   if (!d_offsets || (nt_test > 0 && (!d_vertices_test || !d_triangles_test)) ||
       (nt_trial > 0 && (!d_vertices_trial || !d_triangles_trial))) {
@@ -108,7 +103,7 @@ extern "C" int bgb_classify_csr_noalloc(const double* d_vertices_test, const int
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
   void* base = nullptr;
-  int rc = scratch_address(dev, &base);
+  int rc = scratch_address(&base);
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   int num_sms = 0;

@@ -4,7 +4,7 @@
 //  k_prepare_bounds   FP32 bounding spheres used to skip obviously-far pairs.
 //  k_classify<FILL>   one warp per test triangle sweeps all trial triangles: an FP32 sphere
 //                     test rejects far pairs, the exact FP64 predicate (BEAST quadrule,
-//                     doubleQuadRuleMainCase.jl:324-339) decides the rest; non-far pairs are
+//                     doubleQuadRuleMainCase.jl:187-200) decides the rest; non-far pairs are
 //                     compacted in trial order (ballot/popc), so the list is deterministic.
 //  k_singular<OP>     one warp per non-far pair: Sauter-Schwab CF/CE/CV (SauterSchwab.jl:212-297)
 //                     or the near-pair double quadrature, FP64.  Each point adds a few
@@ -94,7 +94,7 @@ __global__ void k_chunk_bounds(const float4* __restrict__ b, int nb, float4* __r
 }
 
 // ----------------------------------------------------------------------------------------
-// Exact FP64 predicate (doubleQuadRuleMainCase.jl:324-339; codes quadrule_determine.jl:76).
+// Exact FP64 predicate (doubleQuadRuleMainCase.jl:187-200; codes quadrule_determine.jl:76).
 // Rounded like the Julia code: no contraction, IEEE sqrt and division.  *mask (optional)
 // receives the coincident vertex pairs, bit u1 * 3 + u2 (the same test as the reference's
 // vertex matching, pulledback_integrand_gpu.jl:41-51).

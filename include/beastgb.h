@@ -10,7 +10,8 @@
  *
  * Errors: every entry point returns 0 on success or a negative bgb_status; the message of
  * the last failure on the calling thread is bgb_last_error().  Nothing aborts the process
- * and no kernel traps: device-side waits are bounded and report BGB_ERR_TIMEOUT.
+ * and no kernel traps.  No kernel of the library waits on another CTA, stream or device, so
+ * there is no device-side wait to bound: BGB_ERR_TIMEOUT is reserved and never returned.
  *
  * Threading: one handle per host thread (or per CUDA stream); calls on different handles
  * may run concurrently.  A handle owns its device scratch and pinned staging buffers.
@@ -36,7 +37,7 @@ typedef enum {
   BGB_ERR_INVALID = -1,       /* bad argument, inconsistent tables, degenerate geometry */
   BGB_ERR_OOM = -2,           /* device or pinned host allocation failed */
   BGB_ERR_CUDA = -3,          /* CUDA runtime error */
-  BGB_ERR_TIMEOUT = -4,       /* a bounded device wait gave up */
+  BGB_ERR_TIMEOUT = -4,       /* reserved (no entry point returns it: no kernel waits) */
   BGB_ERR_ABORTED = -5,       /* bgb_abort() was called while the call ran */
   BGB_ERR_CAPACITY = -6,      /* a fixed capacity was exceeded */
   BGB_ERR_NOT_SUPPORTED = -7  /* operator / space / rule combination not implemented */
@@ -211,10 +212,14 @@ int bgb_local_matrices(bgb_handle* h, const bgb_operator* op, const bgb_space* t
  * (host) receives the number of non-far pairs; if it exceeds `capacity` the call returns
  * BGB_ERR_CAPACITY after filling d_offsets and *total, so the caller can retry.
  * It calls no cudaMalloc / cudaFree: its scratch is a fixed 16 MiB device array of the
- * library (enough for about 170,000 test + trial triangles; larger inputs are rejected
+ * library, 156 bytes per test triangle plus 152 bytes per trial triangle (about 54,000
+ * triangles per side when test and trial are the same mesh; larger inputs are rejected
  * with BGB_ERR_CAPACITY before any work).  Every device holds that array until the
- * process exits.  The first call on a device looks up the array's address (make that first
- * call before any stream capture).  All calls on a device share the array: calls whose GPU
+ * process exits.  Each call looks up the array's address on the current device (so a reset
+ * context is no problem); the first call on a device may also load the library's device
+ * code there (make that first call before any stream capture).  nt > 0 with nv == 0 is
+ * BGB_ERR_INVALID; a vertex index outside [0, nv) is reported as BGB_ERR_INVALID without
+ * being read.  All calls on a device share the array: calls whose GPU
  * work overlaps race and must be serialised by the caller.  Work is queued on `stream`
  * (a cudaStream_t, NULL = default stream); the call waits for the pair count only. */
 int bgb_classify_csr_noalloc(const double* d_vertices_test, const int32_t* d_triangles_test,

@@ -72,7 +72,7 @@ static inline void cart(const tri_t* T, double u, double v, double x[3]) {
 }
 
 /* ------------------------------------------------------------------------------------ */
-/* Pair classification: the faithful FP64 predicate of doubleQuadRuleMainCase.jl:324-339  */
+/* Pair classification: the faithful FP64 predicate of doubleQuadRuleMainCase.jl:187-200  */
 /* (BEAST quadrule), class codes of quadrule_determine.jl:76: 0 far, 1 CV, 2 CE, 3 CF,     */
 /* 4 near.  Returns -1 for degenerate input (more than three coincident vertex pairs).    */
 /* ------------------------------------------------------------------------------------ */

@@ -16,8 +16,6 @@ import pytest
 import beastgpu_gb300 as bg
 from beastgpu_gb300 import _lib
 
-pytestmark = pytest.mark.gpu
-
 
 def csr_from_dense(cls):
     offsets = np.zeros(cls.shape[0] + 1, dtype=np.int64)
@@ -49,6 +47,7 @@ def call_noalloc(test_mesh, trial_mesh, k2, capacity):
     return rc, n, off.cpu().numpy(), tau[:n].cpu().numpy(), sig[:n].cpu().numpy(), cls[:n].cpu().numpy()
 
 
+@pytest.mark.gpu
 def test_noalloc_matches_classify_block_on_two_calls():
     cases = []
     m = bg.icosphere(3)
@@ -67,6 +66,7 @@ def test_noalloc_matches_classify_block_on_two_calls():
         np.testing.assert_array_equal(cls, r_cls)
 
 
+@pytest.mark.gpu
 def test_noalloc_rejects_oversize_and_short_capacity():
     lib = _lib.load()
     total = C.c_int64(0)
@@ -78,3 +78,31 @@ def test_noalloc_rejects_oversize_and_short_capacity():
     m = bg.icosphere(2)
     rc, n, off, *_ = call_noalloc(m, m, 1.0, capacity=10)
     assert rc == -6 and n > 10 and off[-1] == n
+
+
+@pytest.mark.gpu
+def test_noalloc_reports_a_vertex_index_outside_the_mesh():
+    """A triangle that names vertex nv is flagged on the device, never read; the call fails
+    with BGB_ERR_INVALID and says so, and the next valid call on the same scratch succeeds."""
+    m = bg.icosphere(2)
+    bad = bg.Mesh(m.vertices.copy(), m.triangles.copy())
+    bad.triangles[17, 1] = m.nv  # one past the last vertex
+    rc, *_ = call_noalloc(bad, m, 1.0, capacity=4096)
+    assert rc == -1
+    assert b"vertex index" in _lib.load().bgb_last_error()
+    ref = bg.classify(bg.raviartthomas(m), bg.raviartthomas(m), 1.0)
+    rc, n, off, tau, sig, cls = call_noalloc(m, m, 1.0, capacity=4096)
+    assert rc == 0 and n == np.count_nonzero(ref)
+
+
+def test_noalloc_rejects_triangles_without_vertices():
+    """nt > 0 with nv == 0 is refused on the host, before any CUDA call (runs without a GPU)."""
+    lib = _lib.load()
+    total = C.c_int64(-1)
+    rc = lib.bgb_classify_csr_noalloc(None, None, 0, 5, None, None, 3, 1, 1.0, None, None, None, None, 0,
+                                      C.byref(total), None)
+    assert rc == -1 and total.value == 0
+    assert b"nv == 0" in lib.bgb_last_error()
+    rc = lib.bgb_classify_csr_noalloc(None, None, 3, 1, None, None, 0, 4, 1.0, None, None, None, None, 0,
+                                      C.byref(total), None)
+    assert rc == -1
