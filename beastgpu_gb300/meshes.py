@@ -14,6 +14,11 @@ Workloads:
                                interior vertices jittered in-plane by U(-jitter*h, jitter*h).
   * two_plates(...)         -- the plate plus a coplanar copy shifted along x so the gap
                                between them is `gap`.
+  * meshcuboid(a, b, c, h)  -- the closed surface of the box [0, a] x [0, b] x [0, c] as a
+                               structured grid of step h on each face, 2 triangles per cell:
+                               the mesh of the reference's only test and benchmark
+                               (CompScienceMeshes' meshcuboid(1.0, 1.0, 1.0, 0.5/d),
+                               test/correctness.jl:22, data/graph_data.jl:2-4).
 """
 from __future__ import annotations
 
@@ -167,3 +172,53 @@ def ellipsoid_batch(count: int = 64, seed: int = 2, levels=(1, 4), axis_range=(0
         k = float(rng.uniform(k_range[0], k_range[1]))
         out.append((ellipsoid(lvl, axes), k))
     return out
+
+
+def meshcuboid(width: float, height: float, length: float, delta: float) -> Mesh:
+    """Closed surface of the box [0, width] x [0, height] x [0, length], each face a structured
+    grid of step `delta` (the face extents must be multiples of it), each cell split into two
+    triangles along the same diagonal, normals outward.
+
+    The counts are those of CompScienceMeshes' meshcuboid that the reference tests and times
+    (test/correctness.jl:22; data/graph_data.jl:2-4): for the unit cube and delta = 0.5/d,
+    12 (2d)^2 triangles and 6 (2d)^2 + 2 vertices.  Vertex and face numbering are this
+    generator's: faces are taken in the order z = 0, z = length, y = 0, y = height, x = 0,
+    x = width; a face's vertices are numbered row by row, each lattice point once (the first
+    face that reaches it), and a face's cells in the same order, two triangles per cell.
+    """
+    dims = (float(width), float(height), float(length))
+    h = float(delta)
+    if h <= 0 or min(dims) <= 0:
+        raise ValueError("extents and delta must be positive")
+    n = [int(round(d / h)) for d in dims]
+    for d, k in zip(dims, n):
+        if k < 1 or abs(k * h - d) > 1e-9 * max(1.0, d):
+            raise ValueError("each extent must be a positive multiple of delta")
+    nx, ny, nz = n
+    # (fixed axis, its lattice value, u axis, v axis): u x v is the outward normal
+    faces = [(2, 0, 1, 0), (2, nz, 0, 1), (1, 0, 0, 2), (1, ny, 2, 0), (0, 0, 2, 1), (0, nx, 1, 2)]
+    index = {}
+    verts = []
+    tris = []
+    for fixed, value, ua, va in faces:
+        nu, nv = n[ua], n[va]
+        ids = np.empty((nu + 1, nv + 1), dtype=np.int64)
+        for i in range(nu + 1):
+            for j in range(nv + 1):
+                key = [0, 0, 0]
+                key[fixed], key[ua], key[va] = value, i, j
+                key = tuple(key)
+                k = index.get(key)
+                if k is None:
+                    k = len(verts)
+                    index[key] = k
+                    verts.append(key)
+                ids[i, j] = k
+        for i in range(nu):
+            for j in range(nv):
+                p00, p10, p11, p01 = ids[i, j], ids[i + 1, j], ids[i + 1, j + 1], ids[i, j + 1]
+                tris.append((p00, p10, p11))  # counter-clockwise about u x v: chart normal outward
+                tris.append((p00, p11, p01))
+    lat = np.array(verts, dtype=np.float64)
+    v = lat * np.array([dims[0] / nx, dims[1] / ny, dims[2] / nz])[None, :]
+    return Mesh(v, np.array(tris, dtype=np.int32))

@@ -20,10 +20,14 @@ Other workloads print the same kind of line for their own configuration:
                   plain FP64 assemblies
   --workload c5   EFIE on an icosphere of level 6 (81,920 triangles, 122,880 RWG), k = 2 pi * 8,
                   ComplexF32 output (121 GB) streamed to pinned host memory in output blocks
+  --workload cube  the reference's own benchmark: Helmholtz3D single layer, k = 1, on lagrangec0d1 over
+                  meshcuboid(1, 1, 1, 0.5/d) (--cube-d, default 40: 76,800 triangles, 38,402 functions;
+                  data/graph_data.jl:2-4), mixed and plain FP64, into HBM and end to end into pinned host
+                  memory, beside the reference's recorded full-assemble time for the same d
   --workload curve  Helmholtz2D hypersingular (the operator of the reference's 2-D prototype) on
                   hats over a jittered ellipse of 16,384 segments, k = 2 pi * 100, mixed and FP64
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c2|c3|c4|c5|curve] [--impl reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c2|c3|c4|c5|cube|curve] [--impl reference]
 
 `--impl reference` times the CPU restatement of the reference algorithm (the oracle, OpenMP
 over all host cores) on a bounded row sample of the same workload.
@@ -345,29 +349,36 @@ def run_reference(args):
     import oracle
     if args.workload == "curve":
         return run_reference_curve(args)
-    bg, mesh, X, op, qs = workload()
+    if args.workload == "cube":
+        bg, mesh, X, op, qs = cube_workload(args.cube_d)
+        cfg = cube_config(mesh, X, args.cube_d)
+    else:
+        bg, mesh, X, op, qs = workload()
+        cfg = config_dict(mesh, X)
     rank, world, local = dist_init(args.gpus)
     if rank != 0:
         return 0
     threads = oracle.max_threads()
     nrows = args.ref_rows
     rng = np.random.default_rng(1)
-    pairs_per_row = 2 * mesh.nt
-    vals = []
+    sup = np.bincount(X.fn_index[X.fn_index >= 0], minlength=X.nfun)  # support triangles of each function
+    vals, npairs = [], 0
     for i in range(args.warmup + args.steps):
         rows = np.sort(rng.choice(X.nfun, nrows, replace=False)).astype(np.int32)
+        npairs = int(sup[rows].sum()) * mesh.nt  # triangle pairs the rows' local matrices cover
         t0 = time.perf_counter()
         oracle.assemble_rows(op, X, X, qs, rows, nthreads=threads)
         dt = time.perf_counter() - t0
         if i >= args.warmup:
-            vals.append(nrows * pairs_per_row / dt)
+            vals.append(npairs / dt)
     v = float(np.mean(vals))
-    sample = f"{nrows} random rows per step ({nrows * pairs_per_row} triangle pairs, full local matrices)"
+    sample = f"{nrows} random rows per step ({npairs} triangle pairs, full local matrices)"
+    cfg["parallelism"] = f"OpenMP x{threads} host threads"
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": nrows * pairs_per_row / v * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded icosphere)",
+            "warmup": args.warmup, "ms_per_step": npairs / v * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded meshes)",
             "impl": "reference",
-            "config": config_dict(mesh, X, {"parallelism": f"OpenMP x{threads} host threads"}),
+            "config": cfg,
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -583,6 +594,102 @@ def run_c5(args):
     return 0
 
 
+# The reference's recorded full GPU assemble of this workload (GPU write-back, FP64, ComplexF64 host
+# matrix), median of its logs data/GPU_full/storeGPU/<d>/full_time.txt; its GPU is not named.
+CUBE_REFERENCE_S = {24: 1.208, 40: 9.610}
+
+
+def cube_workload(d):
+    import beastgpu_gb300 as bg
+    mesh = bg.meshcuboid(1.0, 1.0, 1.0, 0.5 / d)
+    return bg, mesh, bg.lagrangec0d1(mesh), bg.Helmholtz3D.singlelayer(wavenumber=1.0), bg.QuadStrat()
+
+
+def cube_config(mesh, X, d, extra=None):
+    c = {"workload": f"Helmholtz3D.singlelayer k=1 on lagrangec0d1, meshcuboid(1,1,1,0.5/{d}) ({mesh.nt} triangles, "
+                     f"{X.nfun} functions), quadstrat far 3x4 / Sauter-Schwab n=4 (the reference's benchmark)",
+         "triangles": mesh.nt, "functions": X.nfun, "pairs_per_step": mesh.nt * mesh.nt,
+         "l2": "outputs > L2; a 256 MiB buffer is written between timed steps"}
+    c.update(extra or {})
+    return c
+
+
+def run_cube(args):
+    """The reference's benchmark workload (data/graph_data.jl:2-4): mixed (value) and plain FP64 into HBM,
+    both end to end into pinned host memory (FP64 into ComplexF64 like the reference's storeGPU path)."""
+    import torch
+    import oracle
+    rank, world, local = dist_init(args.gpus)
+    d = args.cube_d
+    bg, mesh, X, op, qs = cube_workload(d)
+    pairs = mesh.nt * mesh.nt
+    n = X.nfun
+    barrier(world)
+    with ClockSampler(local) as clocks:
+        ms_m, st_m, _, Zm = time_fill(bg, X, op, "mixed", args.steps, args.warmup, local)
+    barrier(world)
+    m = max_over_ranks(float(np.mean(ms_m)), world, local)
+    value = world * pairs / (m * 1e-3)
+    ms_d, st_d, _, Zd = time_fill(bg, X, op, "fp64", args.fp64_steps, 1, local)
+    md = max_over_ranks(float(np.mean(ms_d)), world, local)
+    out = {}
+    if rank == 0:
+        rows = np.sort(np.random.default_rng(ERR_SEED).choice(n, min(n, 200), replace=False)).astype(np.int32)
+        threads = oracle.max_threads()
+        t0 = time.perf_counter()
+        ref = oracle.assemble_rows(op, X, X, qs, rows, nthreads=threads)
+        cpu_s = time.perf_counter() - t0
+        ridx = torch.as_tensor(rows.astype(np.int64), device=Zm.device)
+        out["error_vs_oracle"] = {"mixed": rows_error(Zm[:, ridx].T.cpu().numpy().astype(np.complex128), ref),
+                                  "fp64": rows_error(Zd[:, ridx].T.cpu().numpy(), ref), "rows": int(rows.size),
+                                  "fp64_max_abs": float(np.abs(Zd[:, ridx].T.cpu().numpy() - ref).max()),
+                                  "seed": ERR_SEED}
+        sup = np.bincount(X.fn_index[X.fn_index >= 0], minlength=n)
+        cpu_pairs = int(sup[rows].sum()) * mesh.nt
+        out["cpu_baseline"] = {"value": cpu_pairs / cpu_s, "unit": UNIT, "cores": threads, "kind": "port",
+                               "sample": f"{rows.size} seeded rows ({cpu_pairs} triangle pairs, {cpu_s:.1f} s), FP64 "
+                                         f"oracle with OpenMP"}
+    del Zm, Zd
+    torch.cuda.empty_cache()
+    e2e, e2e64 = None, None
+    h2d = X.mesh.vertices.nbytes + X.mesh.triangles.nbytes + X.fn_index.nbytes + X.fn_coef.nbytes
+    if not args.no_e2e:
+        pinned = torch.empty((n, n), dtype=torch.complex64, pin_memory=True)
+        ms_e, st_e, _, _ = time_fill(bg, X, op, "mixed", max(2, args.steps // 2), 1, local, out="host", pinned=pinned)
+        em = max_over_ranks(float(np.mean(ms_e)), world, local)
+        e2e = {"value": world * pairs / (em * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": n * n * 8, "ms_per_step": em,
+               "ms_copy": float(np.mean([s["ms_copy"] for s in st_e]))}
+        del pinned
+        pinned = torch.empty((n, n), dtype=torch.complex128, pin_memory=True)
+        ms_e64, st_e64, _, _ = time_fill(bg, X, op, "fp64", 1, 0, local, out="host", pinned=pinned)
+        e64 = max_over_ranks(float(np.mean(ms_e64)), world, local)
+        e2e64 = {"value": world * pairs / (e64 * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                 "d2h_bytes_per_step": n * n * 16, "ms_per_step": e64,
+                 "ms_copy": float(np.mean([s["ms_copy"] for s in st_e64]))}
+        del pinned
+    if rank != 0:
+        return 0
+
+    def kernels(st):
+        return {k: float(np.mean([s["ms_" + k] for s in st])) for k in ("far", "singular", "classify")}
+    ref_s = CUBE_REFERENCE_S.get(d)
+    line = line_base(args, world, value, m, "f32 far pairs + double-float (f32 pairs) singular (mixed)",
+                     cube_config(mesh, X, d, {"parallelism": "single GPU" if world == 1 else
+                                              f"{world} independent matrices, one per rank, no collective"}),
+                     fp64_value=world * pairs / (md * 1e-3), fp64_ms_per_step=md, mixed_over_fp64=md / m,
+                     kernels_ms={"mixed": kernels(st_m), "fp64": kernels(st_d)}, pairs_class=st_m[0]["pairs_class"],
+                     halo_redundancy=st_m[0]["pairs_computed"] / pairs, clocks=clocks.summary(),
+                     gpu_launches=int(sum(s["kernel_launches"] for s in st_m)), e2e=e2e, e2e_fp64=e2e64,
+                     reference_recorded=None if ref_s is None else {
+                         "full_assemble_s": ref_s, "pairs_per_s": pairs / ref_s,
+                         "source": f"data/GPU_full/storeGPU/{d}/full_time.txt (median), FP64, GPU write-back, "
+                                   "ComplexF64 host matrix; GPU model not recorded"})
+    line.update(out)
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -593,7 +700,8 @@ def main():
     ap.add_argument("--ref-rows", type=int, default=200)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5", "curve"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5", "cube", "curve"])
+    ap.add_argument("--cube-d", type=int, default=40, help="cube: density d of meshcuboid(1, 1, 1, 0.5/d)")
     ap.add_argument("--hbm-budget", type=int, default=0, help="c5: HBM budget in bytes (0 = 90% of free)")
     ap.add_argument("--curve-segments", type=int, default=CURVE_N, help="curve: segments of the ellipse")
     ap.add_argument("--profile-level", type=int, default=None,
@@ -604,7 +712,7 @@ def main():
     if args.profile_level is not None:
         return run_profile_case(args)
     if args.workload != "c2":
-        return {"c3": run_c3, "c4": run_c4, "c5": run_c5, "curve": run_curve}[args.workload](args)
+        return {"c3": run_c3, "c4": run_c4, "c5": run_c5, "cube": run_cube, "curve": run_curve}[args.workload](args)
 
     import torch
     rank, world, local = dist_init(args.gpus)
