@@ -998,7 +998,10 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
     launch_singular_df(opp.kind, make_opdf(opp), nullptr, nullptr, M, h->df_tab.as<float>(), dgt, dgb,
                        h->ent_tau.as<int>(), h->ent_sigma.as<int>(), h->ent_cls.as<int8_t>(),
                        h->ent_mask.as<int16_t>(), nsing, h->sing_L.as<double2>(), h->abort_dev, h->num_sms, h->stream);
-    launches += 1 + (same ? 0 : 1);
+    // near pairs (singularity extraction: logarithms and arctangents) in FP64
+    launch_singular(opp, qsel, R, test->refspace, trial->refspace, gt, gb, h->ent_tau.as<int>(), h->ent_sigma.as<int>(),
+                    h->ent_cls.as<int8_t>(), nsing, h->sing_L.as<double2>(), h->abort_dev, h->num_sms, h->stream, true);
+    launches += 2 + (same ? 0 : 1);
   } else {
     launch_singular(opp, qsel, R, test->refspace, trial->refspace, gt, gb, h->ent_tau.as<int>(), h->ent_sigma.as<int>(),
                     h->ent_cls.as<int8_t>(), nsing, h->sing_L.as<double2>(), h->abort_dev, h->num_sms, h->stream);

@@ -104,6 +104,9 @@ int enqueue_device_work(bgb_batch* B, cudaStream_t st, bool far_only) {
       launch_singular_df(B->op_kind, OpDf{}, B->opdf.as<OpDf>(), tp_t, B->dfm, B->df_tab.as<float>(), dgt, dgb,
                          B->ent_tau.as<int>(), B->ent_sigma.as<int>(), B->ent_cls.as<int8_t>(),
                          B->ent_mask.as<int16_t>(), B->nsing, B->sing_L.as<double2>(), h->abort_dev, h->num_sms, st);
+      launch_singular_batched(B->op_kind, B->ops.as<OpParams>(), B->qsel, B->rules, gt, gb, tp_t, B->ent_tau.as<int>(),
+                              B->ent_sigma.as<int>(), B->ent_cls.as<int8_t>(), B->nsing, B->sing_L.as<double2>(),
+                              h->abort_dev, h->num_sms, st, true);  // near pairs in FP64
     } else
       launch_singular_batched(B->op_kind, B->ops.as<OpParams>(), B->qsel, B->rules, gt, gb, tp_t, B->ent_tau.as<int>(),
                               B->ent_sigma.as<int>(), B->ent_cls.as<int8_t>(), B->nsing, B->sing_L.as<double2>(),

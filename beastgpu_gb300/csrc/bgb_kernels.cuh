@@ -20,9 +20,10 @@ void launch_classify(bool fill, const float4* tb, const float4* bb, const Geo64*
 void launch_scan(const int* counts, int n, int64_t* offsets, cudaStream_t st);
 void launch_classify_dense(const Geo64* tg, const Geo64* bg, int t0, int t1, int s0, int s1, double k2, int8_t* out,
                            int* err, cudaStream_t st);
+// near_only: integrate only the near pairs of the list (the mixed path's double-float kernel skips them).
 void launch_singular(const OpParams& op, const QuadSel& qs, const RuleTable& rules, int rsA, int rsB, const Geo64* tg,
                      const Geo64* bg, const int* et, const int* es, const int8_t* ec, int64_t n, double2* out,
-                     const volatile int* abort_flag, int num_sms, cudaStream_t st);
+                     const volatile int* abort_flag, int num_sms, cudaStream_t st, bool near_only = false);
 void launch_local_diag64(const OpParams& op, const QuadSel& qs, const RuleTable& rules, int rsA, int rsB,
                          const Geo64* tg, const Geo64* bg, const int* tau, const int* sigma, int64_t n, int force,
                          double2* out, int8_t* cls, int* err, int num_sms, cudaStream_t st, int16_t* mask = nullptr);
@@ -36,7 +37,7 @@ void launch_classify_batched(bool fill, const float4* tb, const float4* bb, cons
 void launch_singular_batched(int op_kind, const OpParams* ops, const QuadSel& qs, const RuleTable& rules,
                              const Geo64* tg, const Geo64* bg, const int* tri_problem, const int* et, const int* es,
                              const int8_t* ec, int64_t n, double2* out, const volatile int* abort_flag, int num_sms,
-                             cudaStream_t st);
+                             cudaStream_t st, bool near_only = false);
 
 // ---- bgb_singular_df.cu ----------------------------------------------------------------
 // Host-built tables of the double-float singular kernel (one float buffer): Sauter-Schwab

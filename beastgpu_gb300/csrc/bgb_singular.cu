@@ -7,9 +7,11 @@
 //                     doubleQuadRuleMainCase.jl:187-200) decides the rest; non-far pairs are
 //                     compacted in trial order (ballot/popc), so the list is deterministic.
 //  k_singular<OP>     one warp per non-far pair: Sauter-Schwab CF/CE/CV (SauterSchwab.jl:212-297)
-//                     or the near-pair double quadrature, FP64.  Each point adds a few
-//                     operator moments (8-10 complex), reduced by warp shuffles; the 3x3
-//                     complex local matrix is formed once per pair (no atomics).
+//                     or the near-pair rule with singularity extraction (BEAST's WiltonSERule:
+//                     closed-form inner integrals of 1/R - gamma + gamma^2 R / 2, the smooth rest
+//                     by the near double rule), FP64.  Each point adds a few operator moments
+//                     (8-10 complex), reduced by warp shuffles; the 3x3 complex local matrix is
+//                     formed once per pair (no atomics).
 //  k_classify_dense   diagnostic: exact class of every pair of a block.
 #include "bgb_kernels.cuh"
 #include "bgb_ss.cuh"
@@ -302,8 +304,33 @@ __device__ inline void make_pair_geo(const Geo64& A, const Geo64& B, const Chart
   }
 }
 
-// Add one point pair with weight w (quadrature weights and Jacobians included).
-template <int OP>
+// e2 = exp(-z) - 1 + z and e3 = e2 - z^2 / 2 for complex z = (zr, zi): the power series for
+// |z| < 1 (Horner, terms to (-z)^20 / 20!), the exponential beyond.
+__device__ inline void exp_tails(double zr, double zi, double2& e2, double2& e3) {
+  const double2 mz = make_double2(-zr, -zi);
+  const double2 z2h = make_double2(0.5 * (zr * zr - zi * zi), zr * zi);
+  if (zr * zr + zi * zi < 1.0) {
+    double2 s = make_double2(1.0, 0.0);
+    for (int n = 20; n >= 4; --n) {
+      const double2 t = cmul(s, mz);
+      s = make_double2(1.0 + t.x / n, t.y / n);
+    }
+    const double2 m3 = cmul(cmul(mz, mz), mz);
+    e3 = cmul(make_double2(m3.x / 6.0, m3.y / 6.0), s);
+    e2 = cadd(e3, z2h);
+    return;
+  }
+  const double er = exp(-zr);
+  double sn, cs;
+  sincos(-zi, &sn, &cs);
+  e2 = make_double2(er * cs - 1.0 + zr, er * sn + zi);
+  e3 = make_double2(e2.x - z2h.x, e2.y - z2h.y);
+}
+
+// Add one point pair with weight w (quadrature weights and Jacobians included).  REG: the
+// regular part of the kernel of a near pair, G_r = (exp(-z) - 1 + z - z^2/2) / (4 pi R), z = gamma R,
+// with grad_x G_r = F (x - y), F = -(z e2 + e3) / (4 pi R^3).
+template <int OP, bool REG = false>
 __device__ __forceinline__ void add_point(const OpParams& op, const double x[3], const double y[3], double bx1,
                                           double bx2, double by1, double by2, const double cA[3],
                                           const double cB[3], const double nA[3], const double nB[3], double w,
@@ -312,11 +339,26 @@ __device__ __forceinline__ void add_point(const OpParams& op, const double x[3],
   const double R2 = d0 * d0 + d1 * d1 + d2 * d2;
   const double rinv = rsqrt(R2);
   const double R = R2 * rinv;
-  double sn = 0.0, cs = 1.0;
-  if (op.gamma[1] != 0.0) sincos(op.gamma[1] * R, &sn, &cs);
-  double amp = w * BGB_INV_4PI_D * rinv;
-  if (op.gamma[0] != 0.0) amp *= exp(-op.gamma[0] * R);
-  const double gr = amp * cs, gi = -amp * sn;
+  double gr, gi, Fr = 0.0, Fi = 0.0;
+  if (REG) {
+    const double zr = op.gamma[0] * R, zi = op.gamma[1] * R;
+    double2 e2, e3;
+    exp_tails(zr, zi, e2, e3);
+    const double a = w * BGB_INV_4PI_D * rinv;
+    gr = a * e3.x;
+    gi = a * e3.y;
+    const double2 c = cadd(cmul(make_double2(zr, zi), e2), e3);
+    const double b = -a * rinv * rinv;
+    Fr = b * c.x;
+    Fi = b * c.y;
+  } else {
+    double sn = 0.0, cs = 1.0;
+    if (op.gamma[1] != 0.0) sincos(op.gamma[1] * R, &sn, &cs);
+    double amp = w * BGB_INV_4PI_D * rinv;
+    if (op.gamma[0] != 0.0) amp *= exp(-op.gamma[0] * R);
+    gr = amp * cs;
+    gi = -amp * sn;
+  }
   if (hat_op(OP)) {
     double hr = gr, hi = gi;
     if (OP == BGB_OP_HELMHOLTZ3D_DL || OP == BGB_OP_HELMHOLTZ3D_DLT) {
@@ -324,9 +366,14 @@ __device__ __forceinline__ void add_point(const OpParams& op, const double x[3],
       const double* nv = OP == BGB_OP_HELMHOLTZ3D_DL ? nB : nA;
       double rn = (d0 * nv[0] + d1 * nv[1] + d2 * nv[2]) * rinv;
       if (OP == BGB_OP_HELMHOLTZ3D_DLT) rn = -rn;
-      const double t = (op.gamma[0] + rinv) * rn, u = op.gamma[1] * rn;
-      hr = t * gr - u * gi;
-      hi = t * gi + u * gr;
+      if (REG) {  // n_y.grad_y G_r = -F (x - y).n_y, n_x.grad_x G_r = F (x - y).n_x: both -F rn R
+        hr = -Fr * rn * R;
+        hi = -Fi * rn * R;
+      } else {
+        const double t = (op.gamma[0] + rinv) * rn, u = op.gamma[1] * rn;
+        hr = t * gr - u * gi;
+        hi = t * gi + u * gr;
+      }
     }
     const double p[3] = {1.0, bx1, bx2}, q[3] = {1.0, by1, by2};
 #pragma unroll
@@ -350,10 +397,10 @@ __device__ __forceinline__ void add_point(const OpParams& op, const double x[3],
     acc[6].x = fma(gr, Y2, acc[6].x); acc[6].y = fma(gi, Y2, acc[6].y);
     acc[7].x += gr; acc[7].y += gi;
   } else {
-    // H = -(gamma + 1/R) G / R
+    // H = -(gamma + 1/R) G / R (F for the regular part)
     const double g2r = gr * rinv, g2i = gi * rinv;
     const double re = op.gamma[0] + rinv;
-    const double Hx = -(re * g2r - op.gamma[1] * g2i), Hy = -(re * g2i + op.gamma[1] * g2r);
+    const double Hx = REG ? Fr : -(re * g2r - op.gamma[1] * g2i), Hy = REG ? Fi : -(re * g2i + op.gamma[1] * g2r);
     const double X0 = x[0] - cA[0], X1 = x[1] - cA[1], X2 = x[2] - cA[2];
     const double Y0 = y[0] - cB[0], Y1 = y[1] - cB[1], Y2 = y[2] - cB[2];
     const double e0 = d1 * Y2 - d2 * Y1, e1 = d2 * Y0 - d0 * Y2, e2 = d0 * Y1 - d1 * Y0;  // d x Y
@@ -364,6 +411,181 @@ __device__ __forceinline__ void add_point(const OpParams& op, const double x[3],
     for (int k = 0; k < 10; ++k) {
       acc[k].x = fma(Hx, v[k], acc[k].x);
       acc[k].y = fma(Hy, v[k], acc[k].y);
+    }
+  }
+}
+
+// ----------------------------------------------------------------------------------------
+// Near pairs: the singular part G_s = (1/R - gamma + gamma^2 R / 2) / (4 pi) integrated in closed
+// form over a flat triangle T at the point x (Wilton et al. 1984; Graglia 1993).  With n the chart
+// normal, d = n.(x - v3), rho = x - d n: Im1 = int 1/R, I1 = int R, Jm1 = int (y - rho)/R,
+// J1 = int (y - rho) R, Om = int d/R^3 (signed solid angle, Van Oosterom & Strackee 1983),
+// Jm3 = int (y - rho)/R^3, from edge sums over a -> b (counter-clockwise about n), unit tangent l,
+// outward normal m = l x n, s+- = (b|a - rho).l, t0 = (a - rho).m, R0^2 = t0^2 + d^2,
+// f = int_e 1/R, K1 = int_e R, K3 = int_e R^3.
+// ----------------------------------------------------------------------------------------
+struct SingPart {
+  double2 S0, D0;    // int G_s, int n.grad_y G_s  (n.grad_y G_s = (d/R^3 - gamma^2 d / (2R)) / (4 pi))
+  double2 Sv[3];     // int G_s (y - rho)
+  double2 Gv[3];     // int grad_x G_s
+  double2 Dv[3];     // int n.grad_y G_s (y - rho)
+  double rho[3];
+};
+
+__device__ inline double dot3d(const double a[3], const double b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+__device__ inline void cross3d(const double a[3], const double b[3], double c[3]) {
+  c[0] = a[1] * b[2] - a[2] * b[1];
+  c[1] = a[2] * b[0] - a[0] * b[2];
+  c[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+__device__ void singular_part(const Geo64& T, const double x[3], const double gam[2], SingPart& S) {
+  double n[3];
+  cross3d(T.t[0], T.t[1], n);
+  const double inn = 1.0 / sqrt(dot3d(n, n));
+  for (int c = 0; c < 3; ++c) n[c] *= inn;
+  double rho[3];
+  const double d = n[0] * (x[0] - T.v[2][0]) + n[1] * (x[1] - T.v[2][1]) + n[2] * (x[2] - T.v[2][2]);
+  for (int c = 0; c < 3; ++c) rho[c] = x[c] - d * n[c];
+  double Jm1[3] = {0, 0, 0}, J1[3] = {0, 0, 0}, Jm3[3] = {0, 0, 0};
+  double sum_tf = 0.0, sum_tk1 = 0.0;
+#pragma unroll 1
+  for (int e = 0; e < 3; ++e) {
+    const double* a = T.v[e];
+    const double* b = T.v[e == 2 ? 0 : e + 1];
+    double l[3], m[3], ar[3], br[3], ax[3], bx[3];
+    for (int c = 0; c < 3; ++c) {
+      l[c] = b[c] - a[c];
+      ar[c] = a[c] - rho[c];
+      br[c] = b[c] - rho[c];
+      ax[c] = x[c] - a[c];
+      bx[c] = x[c] - b[c];
+    }
+    const double il = 1.0 / sqrt(dot3d(l, l));
+    for (int c = 0; c < 3; ++c) l[c] *= il;
+    cross3d(l, n, m);
+    const double sp = dot3d(br, l), sm = dot3d(ar, l), t0 = dot3d(ar, m);
+    const double Rp = sqrt(dot3d(bx, bx)), Rm = sqrt(dot3d(ax, ax));
+    const double R02 = t0 * t0 + d * d;
+    double f;
+    if (sp < 0.0 && sm < 0.0) f = log((Rm - sm) / (Rp - sp));  // beyond a: R0^2 cancels
+    else if (sm >= 0.0) f = log((Rp + sp) / (Rm + sm));         // beyond b
+    else f = log((Rp + sp) * (Rm - sm) / R02);                  // rho abreast of the edge
+    const double K1 = 0.5 * ((sp * Rp - sm * Rm) + R02 * f);
+    const double K3 = 0.25 * (sp * Rp * Rp * Rp - sm * Rm * Rm * Rm) + 0.75 * R02 * K1;
+    sum_tf += t0 * f;
+    sum_tk1 += t0 * K1;
+    for (int c = 0; c < 3; ++c) {
+      Jm1[c] += m[c] * K1;
+      J1[c] += m[c] * K3 / 3.0;
+      Jm3[c] -= m[c] * f;
+    }
+  }
+  double q[3][3], nq[3];
+  for (int i = 0; i < 3; ++i) {
+    for (int c = 0; c < 3; ++c) q[i][c] = T.v[i][c] - x[c];
+    nq[i] = sqrt(dot3d(q[i], q[i]));
+  }
+  double q12[3];
+  cross3d(q[1], q[2], q12);
+  const double trip = dot3d(q[0], q12);
+  const double den = nq[0] * nq[1] * nq[2] + dot3d(q[0], q[1]) * nq[2] + dot3d(q[0], q[2]) * nq[1] + dot3d(q[1], q[2]) * nq[0];
+  const double Om = -2.0 * atan2(trip, den);
+  const double Im1 = sum_tf - d * Om;
+  const double I1 = (d * d * Im1 + sum_tk1) / 3.0;
+  const double i4p = BGB_INV_4PI_D;
+  const double g2hr = 0.5 * (gam[0] * gam[0] - gam[1] * gam[1]), g2hi = gam[0] * gam[1];  // gamma^2 / 2
+  S.S0 = make_double2((Im1 - gam[0] * T.area + g2hr * I1) * i4p, (-gam[1] * T.area + g2hi * I1) * i4p);
+  S.D0 = make_double2((Om - g2hr * d * Im1) * i4p, (-g2hi * d * Im1) * i4p);
+  for (int c = 0; c < 3; ++c) {
+    S.rho[c] = rho[c];
+    const double cen = (T.v[0][c] + T.v[1][c] + T.v[2][c]) / 3.0;
+    const double a0 = T.area * (cen - rho[c]);  // int (y - rho)
+    S.Sv[c] = make_double2((Jm1[c] - gam[0] * a0 + g2hr * J1[c]) * i4p, (-gam[1] * a0 + g2hi * J1[c]) * i4p);
+    const double gR = d * n[c] * Im1 - Jm1[c];  // int grad_x R
+    S.Gv[c] = make_double2((Jm3[c] - n[c] * Om + g2hr * gR) * i4p, (g2hi * gR) * i4p);
+    S.Dv[c] = make_double2((d * Jm3[c] - g2hr * d * Jm1[c]) * i4p, (-g2hi * d * Jm1[c]) * i4p);
+  }
+}
+
+// Hats of T at the in-plane point rho (affine extension) and their gradients.
+__device__ inline void hat_affine(const Geo64& T, const double rho[3], double val[3], double grad[3][3]) {
+  double n[3];
+  cross3d(T.t[0], T.t[1], n);
+  const double inn = 1.0 / sqrt(dot3d(n, n));  // 1 / (2A)
+  for (int c = 0; c < 3; ++c) n[c] *= inn;
+  for (int j = 0; j < 3; ++j) {
+    const int j1 = j == 2 ? 0 : j + 1, j2 = j == 0 ? 2 : j - 1;
+    double e[3], g[3];
+    for (int c = 0; c < 3; ++c) e[c] = T.v[j2][c] - T.v[j1][c];
+    cross3d(n, e, g);
+    double pr = 0.0;
+    for (int c = 0; c < 3; ++c) {
+      grad[j][c] = g[c] * inn;
+      pr += grad[j][c] * (rho[c] - (T.v[0][c] + T.v[1][c] + T.v[2][c]) / 3.0);
+    }
+    val[j] = 1.0 / 3.0 + pr;
+  }
+}
+
+// Moments of the singular part of a near pair at one outer point (weight w): the outer point x
+// lies on the test triangle with chart coordinates (u, v) and T is the trial triangle, except for
+// the transposed double layer, whose outer point lies on the trial triangle and T is the test one.
+template <int OP>
+__device__ void add_singular_part(const OpParams& op, const Geo64& T, const double x[3], double u, double v, double w,
+                                  const double cA[3], const double cB[3], double2* acc) {
+  SingPart S;
+  singular_part(T, x, op.gamma, S);
+  if (hat_op(OP)) {
+    const bool dl = OP == BGB_OP_HELMHOLTZ3D_DL || OP == BGB_OP_HELMHOLTZ3D_DLT;
+    double hv[3], hg[3][3];
+    hat_affine(T, S.rho, hv, hg);
+    const double2 K0 = dl ? S.D0 : S.S0;
+    const double2* Kv = dl ? S.Dv : S.Sv;
+    double2 M[3];  // inner moments against (1, hat 0, hat 1) of T
+    M[0] = K0;
+    for (int h = 0; h < 2; ++h) {
+      double2 t = cscale(K0, hv[h]);
+      for (int c = 0; c < 3; ++c) t = cadd(t, cscale(Kv[c], hg[h][c]));
+      M[h + 1] = t;
+    }
+    const double o[3] = {w, w * u, w * v};  // outer (1, u, v) times the weight
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        // acc[a*3+b]: test moment a, trial moment b; the transposed layer's outer point is on the trial side
+        const double2 m = OP == BGB_OP_HELMHOLTZ3D_DLT ? cscale(M[a], o[b]) : cscale(M[b], o[a]);
+        acc[a * 3 + b] = cadd(acc[a * 3 + b], m);
+      }
+  } else if (OP == BGB_OP_MAXWELL3D_SL) {
+    const double X[3] = {x[0] - cA[0], x[1] - cA[1], x[2] - cA[2]};
+    double2 V[3];
+    for (int c = 0; c < 3; ++c) V[c] = cadd(S.Sv[c], cscale(S.S0, S.rho[c] - cB[c]));  // int G_s (y - cB)
+    double2 xv = make_double2(0.0, 0.0);
+    for (int c = 0; c < 3; ++c) xv = cadd(xv, cscale(V[c], X[c]));
+    acc[0] = cadd(acc[0], cscale(xv, w));
+    for (int c = 0; c < 3; ++c) {
+      acc[1 + c] = cadd(acc[1 + c], cscale(S.S0, w * X[c]));
+      acc[4 + c] = cadd(acc[4 + c], cscale(V[c], w));
+    }
+    acc[7] = cadd(acc[7], cscale(S.S0, w));
+  } else {
+    // Maxwell double layer: int grad_x G_s x (y - cB) = Gv x (x - cB) (grad_x G is parallel to x - y)
+    const double X[3] = {x[0] - cA[0], x[1] - cA[1], x[2] - cA[2]};
+    const double xc[3] = {x[0] - cB[0], x[1] - cB[1], x[2] - cB[2]};
+    const double2* G = S.Gv;
+    const double2 Bv[3] = {cadd(cscale(G[1], xc[2]), cscale(G[2], -xc[1])), cadd(cscale(G[2], xc[0]), cscale(G[0], -xc[2])),
+                           cadd(cscale(G[0], xc[1]), cscale(G[1], -xc[0]))};
+    const double2 Cv[3] = {cadd(cscale(G[2], X[1]), cscale(G[1], -X[2])), cadd(cscale(G[0], X[2]), cscale(G[2], -X[0])),
+                           cadd(cscale(G[1], X[0]), cscale(G[0], -X[1]))};
+    double2 a1 = make_double2(0.0, 0.0);
+    for (int c = 0; c < 3; ++c) a1 = cadd(a1, cscale(Bv[c], X[c]));
+    acc[0] = cadd(acc[0], cscale(a1, w));
+    for (int c = 0; c < 3; ++c) {
+      acc[1 + c] = cadd(acc[1 + c], cscale(Bv[c], w));
+      acc[4 + c] = cadd(acc[4 + c], cscale(Cv[c], w));
+      acc[7 + c] = cadd(acc[7 + c], cscale(G[c], w));
     }
   }
 }
@@ -485,7 +707,20 @@ __device__ void pair_integral64(const OpParams& op, const QuadSel& qs, const Rul
         y[c] = __dadd_rn(__dadd_rn(B.v[2][c], __dmul_rn(B.t[0][c], q[0])), __dmul_rn(B.t[1][c], q[1]));
       }
       const double w = ((p[2] / 2.0) * (A.area * 2.0)) * ((q[2] / 2.0) * (B.area * 2.0));
-      add_point<OP>(op, x, y, p[0], p[1], q[0], q[1], cA, cB, nA, nB, w, acc);
+      if (cls == BGB_CLASS_NEAR) add_point<OP, true>(op, x, y, p[0], p[1], q[0], q[1], cA, cB, nA, nB, w, acc);
+      else add_point<OP>(op, x, y, p[0], p[1], q[0], q[1], cA, cB, nA, nB, w, acc);
+    }
+    if (cls == BGB_CLASS_NEAR) {  // the singular part: closed form inside, one outer point per lane
+      constexpr bool swap = OP == BGB_OP_HELMHOLTZ3D_DLT;
+      const Geo64& O = swap ? B : A;
+      const int ro = swap ? rb : rt;
+      for (int I = lane; I < rules.npoints[ro]; I += 32) {
+        const double* p = rules.uvw[rules.offset[ro] + I];
+        double x[3];
+        for (int c = 0; c < 3; ++c)
+          x[c] = __dadd_rn(__dadd_rn(O.v[2][c], __dmul_rn(O.t[0][c], p[0])), __dmul_rn(O.t[1][c], p[1]));
+        add_singular_part<OP>(op, swap ? A : B, x, p[0], p[1], (p[2] / 2.0) * (O.area * 2.0), cA, cB, acc);
+      }
     }
   } else if (!(flat_face_zero(OP) && cls == BGB_CLASS_CF)) {  // double layers on a flat face are 0
     int I[3], J[3];
@@ -545,11 +780,13 @@ __global__ void __launch_bounds__(256) k_singular(OpParams op1, const OpParams* 
                                                   const Geo64* __restrict__ tg, const Geo64* __restrict__ bg,
                                                   const int* __restrict__ ent_tau, const int* __restrict__ ent_sigma,
                                                   const int8_t* __restrict__ ent_cls, int64_t n,
-                                                  double2* __restrict__ out, const volatile int* abort_flag) {
+                                                  double2* __restrict__ out, const volatile int* abort_flag,
+                                                  int near_only) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < n; e += warps) {
     if (abort_flag && *abort_flag) return;
+    if (near_only && ent_cls[e] != BGB_CLASS_NEAR) continue;  // the others come from the double-float kernel
     const int tau = ent_tau[e];
     const OpParams op = BATCH ? ops[tri_problem[tau]] : op1;
     const Geo64 A = tg[tau], B = bg[ent_sigma[e]];
@@ -687,7 +924,7 @@ void launch_classify_dense(const Geo64* tg, const Geo64* bg, int t0, int t1, int
 }
 void launch_singular(const OpParams& op, const QuadSel& qs, const RuleTable& rules, int rsA, int rsB, const Geo64* tg,
                      const Geo64* bg, const int* et, const int* es, const int8_t* ec, int64_t n, double2* out,
-                     const volatile int* abort_flag, int num_sms, cudaStream_t st) {
+                     const volatile int* abort_flag, int num_sms, cudaStream_t st, bool near_only) {
   (void)rsA;
   (void)rsB;
   if (n <= 0) return;
@@ -695,7 +932,7 @@ void launch_singular(const OpParams& op, const QuadSel& qs, const RuleTable& rul
   if (blocks > (int64_t)num_sms * 32) blocks = (int64_t)num_sms * 32;
 #define BGB_LAUNCH_SING(OPK)                                                                                   \
   k_singular<OPK, false><<<(int)blocks, 256, 0, st>>>(op, nullptr, nullptr, qs, rules, tg, bg, et, es, ec, n, out, \
-                                                      abort_flag)
+                                                      abort_flag, near_only ? 1 : 0)
   switch (op.kind) {
     case BGB_OP_HELMHOLTZ3D_SL: BGB_LAUNCH_SING(BGB_OP_HELMHOLTZ3D_SL); break;
     case BGB_OP_MAXWELL3D_SL: BGB_LAUNCH_SING(BGB_OP_MAXWELL3D_SL); break;
@@ -745,13 +982,13 @@ void launch_classify_batched(bool fill, const float4* tb, const float4* bb, cons
 void launch_singular_batched(int op_kind, const OpParams* ops, const QuadSel& qs, const RuleTable& rules,
                              const Geo64* tg, const Geo64* bg, const int* tri_problem, const int* et, const int* es,
                              const int8_t* ec, int64_t n, double2* out, const volatile int* abort_flag, int num_sms,
-                             cudaStream_t st) {
+                             cudaStream_t st, bool near_only) {
   if (n <= 0) return;
   int64_t blocks = (n + 7) / 8;
   if (blocks > (int64_t)num_sms * 32) blocks = (int64_t)num_sms * 32;
 #define BGB_LAUNCH_SING(OPK)                                                                                  \
   k_singular<OPK, true><<<(int)blocks, 256, 0, st>>>(OpParams{}, ops, tri_problem, qs, rules, tg, bg, et, es, ec, n, \
-                                                     out, abort_flag)
+                                                     out, abort_flag, near_only ? 1 : 0)
   switch (op_kind) {
     case BGB_OP_HELMHOLTZ3D_SL: BGB_LAUNCH_SING(BGB_OP_HELMHOLTZ3D_SL); break;
     case BGB_OP_MAXWELL3D_SL: BGB_LAUNCH_SING(BGB_OP_MAXWELL3D_SL); break;

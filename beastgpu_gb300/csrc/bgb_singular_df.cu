@@ -184,10 +184,11 @@ __global__ void __launch_bounds__(256) k_singular_df(OpDf op1, const OpDf* __res
   const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < n; e += warps) {
     if (abort_flag && *abort_flag) return;
+    const int cls = ent_cls[e];
+    if (cls == BGB_CLASS_NEAR) continue;  // near pairs stay FP64 (k_singular with near_only)
     const int tau = ent_tau[e];
     const OpDf op = BATCH ? ops[tri_problem[tau]] : op1;
     const GeoDf A = tg[tau], B = bg[ent_sigma[e]];
-    const int cls = ent_cls[e];
     DfAcc<OP> acc;
 #pragma unroll
     for (int k = 0; k < NA; ++k) acc.re[k] = acc.im[k] = dfl{0.f, 0.f};

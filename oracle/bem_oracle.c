@@ -298,6 +298,311 @@ static int double_quadrature(const orc_operator* op, const tri_t* A, int32_t rsA
 }
 
 /* ------------------------------------------------------------------------------------ */
+/* Near pairs: singularity extraction.  BEAST integrates pairs of class 4 (close, sharing   */
+/* no vertex) with WiltonSERule, the near rule of DoubleNumWiltonSauterQStrat (the rule its */
+/* quadrule returns in place of the reference's near branch, doubleQuadRuleMainCase.jl:200; */
+/* the reference itself drops the class, quadrule_determine.jl:76).  G = G_s + G_r with     */
+/*   G_s = (1/R - gamma + gamma^2 R / 2) / (4 pi)     the first terms of the Taylor series   */
+/*   G_r = (exp(-z) - 1 + z - z^2/2) / (4 pi R),  z = gamma R   (smooth)                    */
+/* The inner (trial) integral of G_s times a linear shape is in closed form over the flat   */
+/* trial triangle (Wilton et al., IEEE TAP 32(3) 1984; Graglia, IEEE TAP 41(10) 1993) and   */
+/* the outer (test) integral is the near test rule; G_r takes the near double rule.  The    */
+/* transposed double layer swaps the roles (closed form over the test triangle, outer rule  */
+/* over the trial points), since its kernel is the double layer's seen from the trial side. */
+/* ------------------------------------------------------------------------------------ */
+
+/* e2 = exp(-z) - 1 + z and e3 = e2 - z^2 / 2 for complex z: the power series for |z| < 1
+ * (Horner, terms to (-z)^20 / 20!), the exponential beyond. */
+static void exp_tails(cpx z, cpx* e2, cpx* e3) {
+  const cpx mz = mk(-z.re, -z.im);
+  const cpx z2h = cmulr(cmul(z, z), 0.5);
+  if (z.re * z.re + z.im * z.im < 1.0) {
+    cpx sum = mk(1.0, 0.0);
+    for (int n = 20; n >= 4; --n) sum = cadd(mk(1.0, 0.0), cdivr(cmul(sum, mz), (double)n));
+    *e3 = cmul(cdivr(cmul(cmul(mz, mz), mz), 6.0), sum);
+    *e2 = cadd(*e3, z2h);
+    return;
+  }
+  const double er = exp(mz.re);
+  const cpx ez = mk(er * cos(mz.im), er * sin(mz.im));
+  *e2 = cadd(cadd(ez, mk(-1.0, 0.0)), z);
+  *e3 = cadd(*e2, mk(-z2h.re, -z2h.im));
+}
+
+/* Closed-form potentials of a flat triangle T at the point x.  With n the chart normal,
+ * d = n.(x - v3), rho = x - d n and R = |x - y|:
+ *   Im1 = int 1/R,  I1 = int R,  Jm1 = int (y - rho)/R,  J1 = int (y - rho) R,
+ *   Om = int d/R^3 (the signed solid angle, Van Oosterom & Strackee, IEEE TBME 30(2) 1983),
+ *   Jm3 = int (y - rho)/R^3 = -sum_edges m ln((R+ + s+)/(R- + s-))   (x not on T).
+ * Edge sums follow Wilton / Graglia: for the edge a -> b (counter-clockwise about n) with
+ * unit tangent l, outward normal m = l x n, s+- = (b|a - rho).l, t0 = (a - rho).m,
+ * R0^2 = t0^2 + d^2: int_e 1/R = f, int_e R = K1 = (s+R+ - s-R- + R0^2 f)/2,
+ * int_e R^3 = K3 = (s+R+^3 - s-R-^3)/4 + 3 R0^2 K1 / 4, and
+ * Im1 = sum t0 f - d Om,  I1 = (d^2 Im1 + sum t0 K1)/3,  Jm1 = sum m K1,  J1 = sum m K3 / 3. */
+typedef struct {
+  double Im1, I1, Om, d;
+  double Jm1[3], J1[3], Jm3[3], rho[3], n[3];
+} tripot_t;
+
+static inline double dot3(const double a[3], const double b[3]) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
+static inline void cross3(const double a[3], const double b[3], double c[3]) {
+  c[0] = a[1] * b[2] - a[2] * b[1];
+  c[1] = a[2] * b[0] - a[0] * b[2];
+  c[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+static void triangle_potentials(const tri_t* T, const double x[3], tripot_t* P) {
+  double n[3];
+  cross3(T->t[0], T->t[1], n);
+  const double nn = sqrt(dot3(n, n));
+  for (int c = 0; c < 3; ++c) n[c] /= nn;
+  double xv[3];
+  for (int c = 0; c < 3; ++c) xv[c] = x[c] - T->v[2][c];
+  const double d = dot3(n, xv);
+  double rho[3];
+  for (int c = 0; c < 3; ++c) {
+    rho[c] = x[c] - d * n[c];
+    P->rho[c] = rho[c];
+    P->n[c] = n[c];
+    P->Jm1[c] = P->J1[c] = P->Jm3[c] = 0.0;
+  }
+  double sum_tf = 0.0, sum_tk1 = 0.0;
+  for (int e = 0; e < 3; ++e) {
+    const double* a = T->v[e];
+    const double* b = T->v[(e + 1) % 3];
+    double l[3], m[3], ar[3], br[3], ax[3], bx[3];
+    for (int c = 0; c < 3; ++c) {
+      l[c] = b[c] - a[c];
+      ar[c] = a[c] - rho[c];
+      br[c] = b[c] - rho[c];
+      ax[c] = x[c] - a[c];
+      bx[c] = x[c] - b[c];
+    }
+    const double ll = sqrt(dot3(l, l));
+    for (int c = 0; c < 3; ++c) l[c] /= ll;
+    cross3(l, n, m);
+    const double sp = dot3(br, l), sm = dot3(ar, l), t0 = dot3(ar, m);
+    const double Rp = sqrt(dot3(bx, bx)), Rm = sqrt(dot3(ax, ax));
+    const double R02 = t0 * t0 + d * d;
+    double f;
+    if (sp < 0.0 && sm < 0.0) f = log((Rm - sm) / (Rp - sp)); /* beyond a: R0^2 cancels */
+    else if (sm >= 0.0) f = log((Rp + sp) / (Rm + sm));        /* beyond b */
+    else f = log((Rp + sp) * (Rm - sm) / R02);                 /* rho abreast of the edge */
+    const double K1 = 0.5 * ((sp * Rp - sm * Rm) + R02 * f);
+    const double K3 = 0.25 * (sp * Rp * Rp * Rp - sm * Rm * Rm * Rm) + 0.75 * R02 * K1;
+    sum_tf += t0 * f;
+    sum_tk1 += t0 * K1;
+    for (int c = 0; c < 3; ++c) {
+      P->Jm1[c] += m[c] * K1;
+      P->J1[c] += m[c] * K3 / 3.0;
+      P->Jm3[c] -= m[c] * f;
+    }
+  }
+  double q[3][3], nq[3];
+  for (int i = 0; i < 3; ++i) {
+    for (int c = 0; c < 3; ++c) q[i][c] = T->v[i][c] - x[c];
+    nq[i] = sqrt(dot3(q[i], q[i]));
+  }
+  double q12[3];
+  cross3(q[1], q[2], q12);
+  const double trip = dot3(q[0], q12);
+  const double den = nq[0] * nq[1] * nq[2] + dot3(q[0], q[1]) * nq[2] + dot3(q[0], q[2]) * nq[1] + dot3(q[1], q[2]) * nq[0];
+  P->Om = -2.0 * atan2(trip, den);
+  P->d = d;
+  P->Im1 = sum_tf - d * P->Om;
+  P->I1 = (d * d * P->Im1 + sum_tk1) / 3.0;
+}
+
+/* Inner integrals of the singular part over T at x (factor 1/(4 pi) included):
+ *   S0 = int G_s, Sv = int G_s (y - rho), Gv = int grad_x G_s,
+ *   D0 = int (n.grad_y G_s) with n.grad_y G_s = (d/R^3 - gamma^2 d / (2R)) / (4 pi), Dv the same times (y - rho). */
+typedef struct {
+  cpx S0, D0;
+  cpx Sv[3], Gv[3], Dv[3];
+  double rho[3];
+} singpart_t;
+
+static void singular_part(const tri_t* T, const double x[3], const double g[2], singpart_t* S) {
+  tripot_t P;
+  triangle_potentials(T, x, &P);
+  const double i4p = inv4pi();
+  const cpx gam = mk(g[0], g[1]);
+  const cpx g2h = cmulr(cmul(gam, gam), 0.5);
+  double cen[3];
+  for (int c = 0; c < 3; ++c) cen[c] = (T->v[0][c] + T->v[1][c] + T->v[2][c]) / 3.0;
+  /* S0 = (Im1 - gamma A + gamma^2/2 I1) / (4 pi) */
+  S->S0 = cmulr(cadd(cadd(mk(P.Im1, 0.0), cmulr(gam, -T->area)), cmulr(g2h, P.I1)), i4p);
+  S->D0 = cmulr(cadd(mk(P.Om, 0.0), cmulr(g2h, -P.d * P.Im1)), i4p);
+  for (int c = 0; c < 3; ++c) {
+    S->rho[c] = P.rho[c];
+    /* int (y - rho) = A (centroid - rho) */
+    S->Sv[c] = cmulr(cadd(cadd(mk(P.Jm1[c], 0.0), cmulr(gam, -T->area * (cen[c] - P.rho[c]))), cmulr(g2h, P.J1[c])), i4p);
+    /* int grad_x (1/R) = Jm3 - n Om; int grad_x R = d n Im1 - Jm1 */
+    S->Gv[c] = cmulr(cadd(mk(P.Jm3[c] - P.n[c] * P.Om, 0.0), cmulr(g2h, P.d * P.n[c] * P.Im1 - P.Jm1[c])), i4p);
+    S->Dv[c] = cmulr(cadd(mk(P.d * P.Jm3[c], 0.0), cmulr(g2h, -P.d * P.Jm1[c])), i4p);
+  }
+}
+
+/* Hat j of triangle T at the in-plane point rho (affine extension) and its gradient. */
+static void hat_affine(const tri_t* T, const double rho[3], double val[3], double grad[3][3]) {
+  double n[3], cen[3];
+  cross3(T->t[0], T->t[1], n);
+  const double nn = sqrt(dot3(n, n)); /* 2A */
+  for (int c = 0; c < 3; ++c) {
+    n[c] /= nn;
+    cen[c] = (T->v[0][c] + T->v[1][c] + T->v[2][c]) / 3.0;
+  }
+  for (int j = 0; j < 3; ++j) {
+    double e[3], gj[3];
+    for (int c = 0; c < 3; ++c) e[c] = T->v[(j + 2) % 3][c] - T->v[(j + 1) % 3][c];
+    cross3(n, e, gj);
+    double pr = 0.0;
+    for (int c = 0; c < 3; ++c) {
+      grad[j][c] = gj[c] / nn;
+      pr += grad[j][c] * (rho[c] - cen[c]);
+    }
+    val[j] = 1.0 / 3.0 + pr;
+  }
+}
+
+/* One point pair of the regular part G_r, weight w: the operator integrands of accumulate_far
+ * with G_r for G and grad_x G_r = F (x - y). */
+static void accumulate_regular(const orc_operator* op, const shp_t* X, const shp_t* Y, double w, cpx L[3][3]) {
+  const double r[3] = {X->x[0] - Y->x[0], X->x[1] - Y->x[1], X->x[2] - Y->x[2]};
+  const double R = sqrt(dot3(r, r));
+  const cpx z = cmulr(mk(op->gamma[0], op->gamma[1]), R);
+  cpx e2, e3;
+  exp_tails(z, &e2, &e3);
+  const cpx G = cmulr(e3, w * inv4pi() / R);                                       /* G_r */
+  const cpx F = cmulr(cadd(cmul(z, e2), e3), -w * inv4pi() / (R * R * R));          /* G_r' / R */
+  const cpx alpha = mk(op->alpha[0], op->alpha[1]);
+  const cpx beta = mk(op->beta[0], op->beta[1]);
+  switch (op->kind) {
+    case ORC_OP_HELMHOLTZ3D_SL:
+    case ORC_OP_HELMHOLTZ3D_DL:
+    case ORC_OP_HELMHOLTZ3D_DLT: {
+      cpx k = cmul(alpha, G);
+      if (op->kind == ORC_OP_HELMHOLTZ3D_DL) k = cmul(alpha, cmulr(F, -dot3(r, Y->n))); /* n_y.grad_y G = -F r.n_y */
+      if (op->kind == ORC_OP_HELMHOLTZ3D_DLT) k = cmul(alpha, cmulr(F, dot3(r, X->n))); /* n_x.grad_x G = F r.n_x */
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) L[i][j] = cadd(L[i][j], cmulr(k, X->val[i] * Y->val[j]));
+      return;
+    }
+    case ORC_OP_HELMHOLTZ3D_HS: {
+      const cpx a = cmulr(cmul(alpha, G), dot3(X->n, Y->n)), b = cmul(beta, G);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+          L[i][j] = cadd(L[i][j], cadd(cmulr(a, X->val[i] * Y->val[j]), cmulr(b, dot3(X->curl[i], Y->curl[j]))));
+      return;
+    }
+    case ORC_OP_MAXWELL3D_SL: {
+      const cpx a = cmul(alpha, G), b = cmul(beta, G);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+          L[i][j] = cadd(L[i][j], cadd(cmulr(a, dot3(X->vec[i], Y->vec[j])), cmulr(b, X->div * Y->div)));
+      return;
+    }
+    default: { /* Maxwell double layer: f . (F r x g) */
+      const cpx H = cmul(alpha, F);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          double c[3];
+          cross3(r, Y->vec[j], c);
+          L[i][j] = cadd(L[i][j], cmulr(H, dot3(X->vec[i], c)));
+        }
+      return;
+    }
+  }
+}
+
+static inline cpx cdot3(const double a[3], const cpx b[3]) {
+  return cadd(cadd(cmulr(b[0], a[0]), cmulr(b[1], a[1])), cmulr(b[2], a[2]));
+}
+
+static int near_extraction(const orc_operator* op, const tri_t* A, int32_t rsA, const tri_t* B, int32_t rsB, int qt,
+                           int qb, cpx L[3][3]) {
+  int rt = trirule_index(qt), rb = trirule_index(qb);
+  if (rt < 0 || rb < 0) return -1;
+  shp_t X[16], Y[16];
+  double wx[16], wy[16];
+  for (int I = 0; I < qt; ++I) {
+    const double* q = orc_trirule_uvw[orc_trirule_offset[rt] + I];
+    eval_shapes(A, rsA, q[0], q[1], &X[I]);
+    wx[I] = (q[2] / 2.0) * (A->area * 2.0);
+  }
+  for (int J = 0; J < qb; ++J) {
+    const double* q = orc_trirule_uvw[orc_trirule_offset[rb] + J];
+    eval_shapes(B, rsB, q[0], q[1], &Y[J]);
+    wy[J] = (q[2] / 2.0) * (B->area * 2.0);
+  }
+  for (int I = 0; I < qt; ++I)
+    for (int J = 0; J < qb; ++J) accumulate_regular(op, &X[I], &Y[J], wx[I] * wy[J], L);
+  const cpx alpha = mk(op->alpha[0], op->alpha[1]);
+  const cpx beta = mk(op->beta[0], op->beta[1]);
+  if (op->kind == ORC_OP_HELMHOLTZ3D_DLT) { /* outer rule over the trial points, closed form over the test triangle */
+    for (int J = 0; J < qb; ++J) {
+      singpart_t S;
+      singular_part(A, Y[J].x, op->gamma, &S);
+      double hv[3], hg[3][3];
+      hat_affine(A, S.rho, hv, hg);
+      for (int i = 0; i < 3; ++i) {
+        const cpx in = cmul(alpha, cadd(cmulr(S.D0, hv[i]), cdot3(hg[i], S.Dv)));
+        for (int j = 0; j < 3; ++j) L[i][j] = cadd(L[i][j], cmulr(in, wy[J] * Y[J].val[j]));
+      }
+    }
+    return 0;
+  }
+  for (int I = 0; I < qt; ++I) {
+    singpart_t S;
+    singular_part(B, X[I].x, op->gamma, &S);
+    const double w = wx[I];
+    double hv[3], hg[3][3];
+    hat_affine(B, S.rho, hv, hg);
+    for (int j = 0; j < 3; ++j) {
+      cpx in_j = mk(0.0, 0.0); /* the singular part's inner integral against trial shape j, times the test shapes below */
+      switch (op->kind) {
+        case ORC_OP_HELMHOLTZ3D_SL:
+          in_j = cmul(alpha, cadd(cmulr(S.S0, hv[j]), cdot3(hg[j], S.Sv)));
+          for (int i = 0; i < 3; ++i) L[i][j] = cadd(L[i][j], cmulr(in_j, w * X[I].val[i]));
+          break;
+        case ORC_OP_HELMHOLTZ3D_DL:
+          in_j = cmul(alpha, cadd(cmulr(S.D0, hv[j]), cdot3(hg[j], S.Dv)));
+          for (int i = 0; i < 3; ++i) L[i][j] = cadd(L[i][j], cmulr(in_j, w * X[I].val[i]));
+          break;
+        case ORC_OP_HELMHOLTZ3D_HS: {
+          const cpx sl = cmul(cmulr(alpha, dot3(X[I].n, Y[0].n)), cadd(cmulr(S.S0, hv[j]), cdot3(hg[j], S.Sv)));
+          const cpx cc = cmul(beta, S.S0);
+          for (int i = 0; i < 3; ++i)
+            L[i][j] = cadd(L[i][j], cmulr(cadd(cmulr(sl, X[I].val[i]), cmulr(cc, dot3(X[I].curl[i], Y[0].curl[j]))), w));
+          break;
+        }
+        case ORC_OP_MAXWELL3D_SL: {
+          /* int G_s g_j = (Sv + (rho - w_j) S0) / (2 A_sigma) */
+          cpx gj[3];
+          for (int c = 0; c < 3; ++c)
+            gj[c] = cmulr(cadd(S.Sv[c], cmulr(S.S0, S.rho[c] - B->v[j][c])), 1.0 / (2.0 * B->area));
+          const cpx dd = cmul(beta, cmulr(S.S0, X[I].div * Y[0].div));
+          for (int i = 0; i < 3; ++i)
+            L[i][j] = cadd(L[i][j], cmulr(cadd(cmul(alpha, cdot3(X[I].vec[i], gj)), dd), w));
+          break;
+        }
+        default: { /* Maxwell double layer: int grad_x G_s x g_j = Gv x (x - w_j) / (2 A_sigma) */
+          double xw[3];
+          for (int c = 0; c < 3; ++c) xw[c] = (X[I].x[c] - B->v[j][c]) / (2.0 * B->area);
+          cpx cr[3];
+          cr[0] = cadd(cmulr(S.Gv[1], xw[2]), cmulr(S.Gv[2], -xw[1]));
+          cr[1] = cadd(cmulr(S.Gv[2], xw[0]), cmulr(S.Gv[0], -xw[2]));
+          cr[2] = cadd(cmulr(S.Gv[0], xw[1]), cmulr(S.Gv[1], -xw[0]));
+          for (int i = 0; i < 3; ++i) L[i][j] = cadd(L[i][j], cmulr(cmul(alpha, cdot3(X[I].vec[i], cr)), w));
+          break;
+        }
+      }
+    }
+  }
+  return 0;
+}
+
+/* ------------------------------------------------------------------------------------ */
 /* Sauter-Schwab singular rules                                                            */
 /* ------------------------------------------------------------------------------------ */
 
@@ -506,7 +811,7 @@ static int local_matrix(const orc_operator* op, const orc_space* test, const orc
     case ORC_CLASS_FAR:
       return double_quadrature(op, A, test->refspace, B, trial->refspace, qs->far_test, qs->far_trial, L);
     case ORC_CLASS_NEAR:
-      return double_quadrature(op, A, test->refspace, B, trial->refspace, qs->near_test, qs->near_trial, L);
+      return near_extraction(op, A, test->refspace, B, trial->refspace, qs->near_test, qs->near_trial, L);
     case ORC_CLASS_CV:
       return sauter_schwab(op, cls, A, test->refspace, B, trial->refspace, qs->ss_cv, L);
     case ORC_CLASS_CE:

@@ -8,6 +8,7 @@ For a test triangle tau and trial triangle sigma the local matrices are
   MWb  L_ij = 1/(4 pi) int_tau int_sigma div psi_i div psi_j / |x - y|           (RWG divergence part)
   DL   L_ij = 1/(4 pi) int_tau int_sigma lambda_i(x) lambda_j(y) (x - y).n_sigma / |x - y|^3
   DLT  L_ij = DL of the swapped pair, transposed (the kernel of the transposed double layer)
+  MDL  L_ij = 1/(4 pi) int_tau int_sigma psi_i(x) . (grad_x(1/|x - y|) x psi_j(y))      (RWG, MFIE)
 
 with lambda_i the barycentric coordinate of chart vertex i, psi_i(x) = (x - v_i) / (2 A) and
 div psi_i = 1 / A (BEAST's RT reference shapes).  The inner integrals over sigma are the closed
@@ -26,7 +27,9 @@ integrand loses smoothness).  Checked against the closed-form self term of a tri
 
 The mesh is an ellipsoid (icosphere of level 1 scaled by 1, 0.8, 0.6); the pairs cover common
 face, common edge and common vertex in several local positions, and four far pairs.  Near pairs
-come from two jittered coplanar 4 x 4 plates 0.01 apart.  Run from the repository root:
+come from two jittered coplanar 4 x 4 plates 0.01 apart and, not coplanar, from a plate and a copy
+tilted by 60 degrees 0.02 beside it.  The Maxwell double layer (MFIE) is pinned through the
+gradient of the flat-triangle potential.  Run from the repository root:
 
     python tests/golden/make_static_fixtures.py
 """
@@ -104,7 +107,11 @@ def dl_potentials(V, r):
 
 def local_static_dl(Vt, Vs, n=40, p=3):
     """DL_ij = 1/(4 pi) int_tau lambda_i(x) int_sigma lambda_j(y) (x - y) . n_sigma / |x - y|^3."""
-    x, w = graded_rule(Vt, n, p)
+    return local_static_dl_at(Vt, Vs, *graded_rule(Vt, n, p))
+
+
+def local_static_dl_at(Vt, Vs, x, w):
+    """local_static_dl with the outer integral taken as the sum over the points x (N, 3) with weights w."""
     W0, W1, d = dl_potentials(Vs, x)
     lam_t = barycentric(Vt, x)
     lam_s = barycentric(Vs, x)
@@ -115,6 +122,32 @@ def local_static_dl(Vt, Vs, n=40, p=3):
             inner = lam_s[:, j] * W0 + d * (W1 @ gs[j])
             dl[i, j] = np.sum(w * lam_t[:, i] * inner) / (4 * np.pi)
     return dl
+
+
+def local_static_mfie(Vt, Vs, n=40, p=3):
+    """MFIE_ij = 1/(4 pi) int_tau psi_i(x) . (int_sigma grad_x(1/|x - y|) x psi_j(y) dy) with the RWG
+    shapes psi = (x - v) / (2 A).  grad_x(1/R) is parallel to x - y, so the inner integral is
+    (int_sigma grad_x(1/R)) x (x - w_j) / (2 A_sigma), and int_sigma grad_x(1/R) = W1 - n W0 from the
+    double-layer potentials (Graglia 1993)."""
+    return local_static_mfie_at(Vt, Vs, *graded_rule(Vt, n, p))
+
+
+def local_static_mfie_at(Vt, Vs, x, w):
+    """local_static_mfie with the outer integral taken as the sum over the points x with weights w."""
+    W0, W1, d = dl_potentials(Vs, x)
+    v1, v2, v3 = Vs
+    nrm = np.cross(v2 - v1, v3 - v1)
+    nrm /= np.linalg.norm(nrm)
+    grad = W1 - nrm[None, :] * W0[:, None]
+    At = 0.5 * np.linalg.norm(np.cross(Vt[1] - Vt[0], Vt[2] - Vt[0]))
+    As = 0.5 * np.linalg.norm(np.cross(Vs[1] - Vs[0], Vs[2] - Vs[0]))
+    out = np.zeros((3, 3))
+    for i in range(3):
+        psi_i = (x - Vt[i]) / (2 * At)
+        for j in range(3):
+            inner = np.cross(grad, (x - Vs[j]) / (2 * As))
+            out[i, j] = np.sum(w * np.einsum("kc,kc->k", psi_i, inner)) / (4 * np.pi)
+    return out
 
 
 def graded_rule(V, n=40, p=3):
@@ -159,7 +192,11 @@ def grad_barycentric(V):
 
 
 def local_static(Vt, Vs, n=40, p=3):
-    x, w = graded_rule(Vt, n, p)
+    return local_static_at(Vt, Vs, *graded_rule(Vt, n, p))
+
+
+def local_static_at(Vt, Vs, x, w):
+    """(HH, MW alpha part, MW beta part) with the outer integral as the sum over the points x, weights w."""
     P0, P1 = tri_potentials(Vs, x)
     At = 0.5 * np.linalg.norm(np.cross(Vt[1] - Vt[0], Vt[2] - Vt[0]))
     As = 0.5 * np.linalg.norm(np.cross(Vs[1] - Vs[0], Vs[2] - Vs[0]))
@@ -199,7 +236,7 @@ def pick_pairs(tris):
 
 
 def tables(V, T, pairs):
-    hh, mwa, mwb, dl, dlt, err = [], [], [], [], [], []
+    hh, mwa, mwb, dl, dlt, mdl, err = [], [], [], [], [], [], []
     for a, b in pairs:
         A, B = V[T[a]], V[T[b]]
         r40 = local_static(A, B, 40)
@@ -207,13 +244,30 @@ def tables(V, T, pairs):
         hh.append(r60[0]), mwa.append(r60[1]), mwb.append(r60[2])
         err.append(max(np.abs(x - y).max() / np.abs(y).max() for x, y in zip(r40, r60)))
         if a == b:  # the double layers vanish on a flat common face
-            dl.append(np.zeros((3, 3))), dlt.append(np.zeros((3, 3)))
+            dl.append(np.zeros((3, 3))), dlt.append(np.zeros((3, 3))), mdl.append(np.zeros((3, 3)))
             continue
         d40, d60 = local_static_dl(A, B, 40), local_static_dl(A, B, 60)
         t60 = local_static_dl(B, A, 60).T  # transposed double layer: DL with the roles swapped
-        dl.append(d60), dlt.append(t60)
-        err.append(np.abs(d40 - d60).max() / max(np.abs(d60).max(), 1e-300))
-    return np.array(hh), np.array(mwa), np.array(mwb), np.array(dl), np.array(dlt), np.array(err)
+        # the MFIE's outer integrand has a logarithmic edge singularity on common-edge pairs: more points
+        m80, m100 = local_static_mfie(A, B, 80), local_static_mfie(A, B, 100)
+        dl.append(d60), dlt.append(t60), mdl.append(m100)
+        for x, y in ((d40, d60), (m80, m100)):
+            sc = np.abs(y).max()
+            if sc > 1e-14 * np.abs(r60[0]).max():  # coplanar pairs: the double layers vanish
+                err.append(np.abs(x - y).max() / sc)
+    return (np.array(hh), np.array(mwa), np.array(mwb), np.array(dl), np.array(dlt), np.array(mdl), np.array(err))
+
+
+def tilted_plates(n=4, jitter=0.3, seed=1, gap=0.02, angle=np.pi / 3):
+    """A jittered n x n plate in z = 0 and a copy turned by `angle` about the x axis, lifted so that
+    its lower edge runs `gap` above and beside the first plate's edge y = 1: near pairs that are
+    not coplanar (the double layers do not vanish)."""
+    import beastgpu_gb300 as bg
+    p = bg.plate(n, jitter, seed)
+    v = p.vertices.copy()
+    c, s = np.cos(angle), np.sin(angle)
+    q = np.stack([v[:, 0], 1.0 + gap + c * v[:, 1], gap + s * v[:, 1]], axis=1)
+    return np.concatenate([v, q]), np.concatenate([p.triangles, p.triangles + p.nv]).astype(np.int32)
 
 
 def main():
@@ -224,12 +278,16 @@ def main():
     assert len(pairs) == 15, len(pairs)
     # far pairs: the three closest non-touching pairs and the farthest one
     pairs += [(67, 69), (40, 55), (3, 12), (19, 59)]
-    hh, mwa, mwb, dl, dlt, err = tables(V, T, pairs)
+    hh, mwa, mwb, dl, dlt, mdl, err = tables(V, T, pairs)
     # near pairs (class 4 at k = 0) of two jittered coplanar 4 x 4 plates 0.01 apart
     p = bg.two_plates(4, jitter=0.3, seed=1, gap=0.01)
     PV, PT = p.vertices.astype(np.float64), p.triangles.astype(np.int32)
     near = [(24, 32), (25, 34), (26, 37), (24, 35)]
-    nhh, nmwa, nmwb, ndl, ndlt, nerr = tables(PV, PT, near)
+    nhh, nmwa, nmwb, ndl, ndlt, nmdl, nerr = tables(PV, PT, near)
+    # near pairs across a plate and a tilted copy (not coplanar), at gaps 0.02 .. 0.1 of the plate
+    tv, tt = tilted_plates()
+    tilted = [(6, 32), (7, 33), (14, 48), (15, 41), (23, 56), (31, 57)]
+    thh, tmwa, tmwb, tdl, tdlt, tmdl, terr = tables(tv, tt, tilted)
     # the CF self term of the outer rule against its closed form
     Vt = V[T[0]]
     x, w = graded_rule(Vt, 60)
@@ -238,11 +296,15 @@ def main():
     out = os.path.join(HERE, "static_singular.npz")
     np.savez(out, vertices=V, triangles=T, tau=np.array([q[0] for q in pairs], dtype=np.int32),
              sigma=np.array([q[1] for q in pairs], dtype=np.int32), hh=hh, mw_alpha=mwa, mw_beta=mwb, dl=dl, dlt=dlt,
-             plate_vertices=PV, plate_triangles=PT, near_tau=np.array([q[0] for q in near], dtype=np.int32),
+             mw_dl=mdl, plate_vertices=PV, plate_triangles=PT, near_tau=np.array([q[0] for q in near], dtype=np.int32),
              near_sigma=np.array([q[1] for q in near], dtype=np.int32), near_hh=nhh, near_mw_alpha=nmwa,
-             near_mw_beta=nmwb, near_dl=ndl, near_dlt=ndlt, rule_change=np.concatenate([err, nerr]), self_term_error=np.array(self_err))
-    print(f"wrote {out}: {len(pairs)} + {len(near)} pairs, max change 40 -> 60 points per dimension "
-          f"{max(err.max(), nerr.max()):.2e}, self-term error {self_err:.2e}")
+             near_mw_beta=nmwb, near_dl=ndl, near_dlt=ndlt, near_mw_dl=nmdl, tilted_vertices=tv, tilted_triangles=tt,
+             tilted_tau=np.array([q[0] for q in tilted], dtype=np.int32),
+             tilted_sigma=np.array([q[1] for q in tilted], dtype=np.int32), tilted_hh=thh, tilted_mw_alpha=tmwa,
+             tilted_mw_beta=tmwb, tilted_dl=tdl, tilted_dlt=tdlt, tilted_mw_dl=tmdl,
+             rule_change=np.concatenate([err, nerr, terr]), self_term_error=np.array(self_err))
+    print(f"wrote {out}: {len(pairs)} + {len(near)} + {len(tilted)} pairs, max change 40 -> 60 (MFIE 80 -> 100) points per dimension "
+          f"{max(err.max(), nerr.max(), terr.max()):.2e}, self-term error {self_err:.2e}")
 
 
 if __name__ == "__main__":

@@ -87,12 +87,13 @@ def test_noalloc_reports_a_vertex_index_outside_the_mesh():
     m = bg.icosphere(2)
     bad = bg.Mesh(m.vertices.copy(), m.triangles.copy())
     bad.triangles[17, 1] = m.nv  # one past the last vertex
-    rc, *_ = call_noalloc(bad, m, 1.0, capacity=4096)
+    rc, *_ = call_noalloc(bad, m, 1.0, capacity=16384)
     assert rc == -1
     assert b"vertex index" in _lib.load().bgb_last_error()
     ref = bg.classify(bg.raviartthomas(m), bg.raviartthomas(m), 1.0)
-    rc, n, off, tau, sig, cls = call_noalloc(m, m, 1.0, capacity=4096)
+    rc, n, off, tau, sig, cls = call_noalloc(m, m, 1.0, capacity=int(np.count_nonzero(ref)) + 5)
     assert rc == 0 and n == np.count_nonzero(ref)
+    np.testing.assert_array_equal(cls, ref[tau, sig])
 
 
 def test_noalloc_rejects_triangles_without_vertices():
