@@ -53,8 +53,12 @@ class GPUConfiguration:
     """The fields of the reference's GPUConfiguration (utils/configuration.jl:11-26) that mean
     something on one GB300, plus the precision mode and tile choice.
 
+    floatType: the reference's field; np.float64 (or float) selects the plain FP64 kernels and
+    np.float32 the mixed ones, overriding `precision` when given.
+    amount_of_gpus: the reference's chunk count (assamble_chunk_gpu.jl:123-130): the matrix is
+    assembled in that many row windows, one after the other; the result is the same.
     precision: "fp64" (plain all-FP64 kernels, the drop-in) or "mixed" (FP32 far pairs with
-    double-float phase base, FP64 singular and near pairs).
+    double-float phase base, FP64-accurate singular and near pairs).
     total_GPU_budget: HBM bytes the call may use for the output staging (0 = 90% of free);
     host outputs are produced in blocks of columns of at most a quarter of it (two device
     staging buffers), and large outputs in about 16 blocks so that copies overlap the fill.
@@ -70,12 +74,21 @@ class GPUConfiguration:
     makeCompexWithGPU: bool = True
     pinned_ring_bytes: int = 0
     pageable_via_ring: bool = False
+    floatType: type = None
+    amount_of_gpus: int = 1
 
     def __post_init__(self):
         if self.writeBackStrategy is None:
             self.writeBackStrategy = GpuWriteBackTrueInstance()
+        if self.floatType is not None:
+            ft = np.dtype(self.floatType)
+            if ft not in (np.float64, np.float32):
+                raise ValueError("floatType must be Float64 or Float32")
+            self.precision = "fp64" if ft == np.float64 else "mixed"
         if self.precision not in ("fp64", "mixed"):
             raise ValueError("precision must be 'fp64' or 'mixed'")
+        if self.amount_of_gpus < 1:
+            raise ValueError("amount_of_gpus must be at least 1")
 
 
 _handles = {}
@@ -167,17 +180,26 @@ def _precision(p):
 
 
 def assemble_gpu(operator: Operator, test_functions: Space, trial_functions: Space, config: GPUConfiguration = None,
-                 writeBackStrategy: GpuWriteBack = None, *, quadstrat: QuadStrat = None, out: str = "host",
-                 dtype=None, rows=None, out_buffer=None, stream=None, return_stats: bool = False):
+                 writeBackStrategy: GpuWriteBack = None, *, storage_policy=None, threading=None,
+                 quadstrat: QuadStrat = None, out: str = "host", dtype=None, rows=None, out_buffer=None, stream=None,
+                 return_stats: bool = False):
     """Dense Galerkin matrix Z[m, n] = <f_m, op g_n> (test rows, trial columns).
 
-    out="host": numpy array in Fortran (column-major) order, complex128 for precision "fp64"
-    and complex64 for "mixed" unless `dtype` says otherwise.  out="device": a torch CUDA
+    The reference's signature, assemble_gpu(operator, test_functions, trial_functions, config,
+    writeBackStrategy; storage_policy, threading, quadstrat) (assamble_gpu.jl:8,25): both
+    write-back strategies give the same matrix; storage_policy and threading are accepted and
+    ignored (the matrix is dense, the threads are the library's); quadstrat defaults to
+    defaultquadstrat(operator, test_functions, trial_functions).  The keywords after it are this
+    binding's: out="host": numpy array in Fortran (column-major) order, complex128 for precision
+    "fp64" and complex64 for "mixed" unless `dtype` says otherwise.  out="device": a torch CUDA
     tensor view of shape (rows, cols) with column-major strides.  rows=(row0, nrows) assembles
     a row window.  out_buffer: a preallocated host (numpy or pinned torch) or device (torch)
     buffer of the right shape/dtype to write into.
     """
     config = config or GPUConfiguration()
+    if config.amount_of_gpus > 1 and rows is None and out == "host" and out_buffer is None \
+            and not isinstance(test_functions, CurveSpace):
+        return _assemble_chunks(operator, test_functions, trial_functions, config, quadstrat, dtype, return_stats)
     if isinstance(test_functions, CurveSpace):
         return _assemble_curve(operator, test_functions, trial_functions, config, quadstrat, out, dtype, rows,
                                out_buffer, stream, return_stats)
@@ -224,6 +246,28 @@ def assemble_gpu(operator: Operator, test_functions: Space, trial_functions: Spa
     else:
         raise ValueError("out must be 'host' or 'device'")
     return (Z, stats.as_dict()) if return_stats else Z
+
+
+def _assemble_chunks(operator, X, Y, config, quadstrat, dtype, return_stats):
+    """config.amount_of_gpus row windows of one host matrix, assembled one after the other (the
+    reference's chunks, assamble_chunk_gpu.jl:123-130)."""
+    prec = _precision(config.precision)
+    dtype = np.dtype(dtype or (np.complex128 if prec == _lib.PREC_FP64 else np.complex64))
+    Z = np.empty((X.nfun, Y.nfun), dtype=dtype, order="F")
+    one = GPUConfiguration(writeBackStrategy=config.writeBackStrategy, precision=config.precision,
+                           device=config.device, total_GPU_budget=config.total_GPU_budget,
+                           tile_config=config.tile_config, pinned_ring_bytes=config.pinned_ring_bytes,
+                           pageable_via_ring=config.pageable_via_ring)
+    stats = []
+    for c in range(config.amount_of_gpus):
+        r0, n = row_shard(X.nfun, c, config.amount_of_gpus)
+        if n == 0:
+            continue
+        part, st = assemble_gpu(operator, X, Y, one, quadstrat=quadstrat, dtype=dtype, rows=(r0, n),
+                                return_stats=True)
+        Z[r0:r0 + n, :] = part
+        stats.append(st)
+    return (Z, stats) if return_stats else Z
 
 
 def _assemble_curve(operator, X, Y, config, quadstrat, out, dtype, rows, out_buffer, stream, return_stats):

@@ -68,9 +68,10 @@ def cube1():
 def test_reference_correctness_case_fp64(cube1, wb, chunks):
     X, op, ref = cube1
     strat = bg.GpuWriteBackTrueInstance() if wb == "true" else bg.GpuWriteBackFalseInstance()
-    cfg = bg.GPUConfiguration(writeBackStrategy=strat, precision="fp64")
-    parts = [bg.assemble_gpu(op, X, X, cfg, strat, rows=bg.row_shard(X.nfun, r, chunks)) for r in range(chunks)]
-    Z = np.concatenate(parts, axis=0)
+    # the reference's configuration fields (test/configers.jl:31-43) and call (test/correctness.jl:36)
+    cfg = bg.GPUConfiguration(writeBackStrategy=strat, amount_of_gpus=chunks, total_GPU_budget=3 * 2 ** 30,
+                              floatType=np.float64)
+    Z = bg.assemble_gpu(op, X, X, cfg, cfg.writeBackStrategy)
     assert Z.shape == (26, 26) and Z.dtype == np.complex128
     assert np.abs(Z - ref).max() < REF_TOL
     assert np.abs(Z - ref).max() < 1e-12 * np.abs(ref).max()

@@ -370,3 +370,89 @@ def test_distinct_test_and_trial_spaces(name):
         assert rel(zmx.astype(np.complex128), ref) < MIXED_TOL
         part = bg.assemble_gpu(op, X, Y, bg.GPUConfiguration(precision="fp64"), rows=(3, X.nfun - 5))
         np.testing.assert_array_equal(part, z64[3:X.nfun - 2])
+
+
+def _nonfar_pairs(X, k2, rows_per_block=2048):
+    """(tau, sigma) of every non-far triangle pair, from the GPU classifier in row blocks."""
+    nt = X.mesh.nt
+    taus, sigmas = [], []
+    for t0 in range(0, nt, rows_per_block):
+        c = bg.classify(X, X, k2, block=(t0, min(nt, t0 + rows_per_block), 0, nt))
+        t, s = np.nonzero(c)
+        taus.append(t + t0)
+        sigmas.append(s)
+    return np.concatenate(taus).astype(np.int32), np.concatenate(sigmas).astype(np.int32)
+
+
+def _per_pair_rel(a, b):
+    """Error of each local matrix relative to its own norm; pairs whose matrix vanishes up to rounding
+    (the Maxwell double layer on coplanar pairs) are measured against 1e-6 of the largest pair's norm."""
+    num = np.linalg.norm((a - b).reshape(len(a), -1), axis=1)
+    den = np.linalg.norm(b.reshape(len(b), -1), axis=1)
+    return num / np.maximum(np.maximum(den, 1e-6 * den.max()), 1e-300)
+
+
+def test_c2_every_singular_entry_of_the_mixed_path_within_1e_12():
+    """The EFIE at the benchmark size (icosphere level 5, k = 8 pi): every common-face, -edge and
+    -vertex local matrix of the mixed path (double-float Sauter-Schwab) within 1e-12 of the plain
+    FP64 kernel, pair by pair (not in aggregate)."""
+    m = bg.icosphere(5)
+    X = bg.raviartthomas(m)
+    k = 2 * np.pi * 4
+    op = bg.Maxwell3D.singlelayer(wavenumber=k)
+    tau, sigma = _nonfar_pairs(X, k * k)
+    L64, c64 = bg.local_matrices(op, X, X, tau, sigma)
+    Lmx, cmx = bg.local_matrices(op, X, X, tau, sigma, precision="mixed")
+    np.testing.assert_array_equal(c64, cmx)
+    assert set(np.unique(c64)) == {1, 2, 3}
+    assert tau.size == 20480 * (1 + 3) + int(np.count_nonzero(c64 == 1))  # CF + 3 CE per triangle + CV
+    assert _per_pair_rel(Lmx, L64).max() < 1e-12
+
+
+@pytest.mark.parametrize("name", ["hh", "mfie", "efie"])
+def test_near_entries_are_fp64_in_the_mixed_path(name):
+    """Near pairs (singularity extraction) run in FP64 in both precisions: identical local matrices;
+    the mixed path's singular pairs within 1e-12 of FP64, pair by pair, on jittered and folded plates."""
+    make, which = OPS[name]
+    k = 4 * np.pi
+    op = make(k)
+    p = bg.two_plates(16, jitter=0.3, seed=1, gap=0.01)
+    v = p.vertices.copy()
+    half = v[:, 0] > 1.0  # fold the second plate up by 30 degrees about its edge x = 1.01
+    v[half, 2] = (v[half, 0] - 1.01) * np.sin(np.pi / 6)
+    v[half, 0] = 1.01 + (v[half, 0] - 1.01) * np.cos(np.pi / 6)
+    # the Maxwell double layer vanishes on coplanar pairs: only the tilted plates give it values
+    meshes = (p, bg.Mesh(v, p.triangles)) if name != "mfie" else (bg.Mesh(v, p.triangles),)
+    for mesh in meshes:
+        sp = (mesh, bg.raviartthomas(mesh), bg.lagrangec0d1(mesh))[which]
+        tau, sigma = _nonfar_pairs(sp, k * k)
+        L64, c = bg.local_matrices(op, sp, sp, tau, sigma)
+        Lmx, _ = bg.local_matrices(op, sp, sp, tau, sigma, precision="mixed")
+        near = c == 4
+        assert near.sum() > 0
+        np.testing.assert_array_equal(Lmx[near], L64[near])
+        # each singular pair against its own norm; the Maxwell double layer's singular pairs here are all
+        # coplanar, i.e. zero up to rounding, so they are measured against the largest local matrix
+        num = np.linalg.norm((Lmx - L64)[~near].reshape(-1, 9), axis=1)
+        den = np.linalg.norm(L64.reshape(-1, 9), axis=1)
+        floor = den.max() if name == "mfie" else 1e-6 * den.max()
+        tol = 1e-11 if name == "mfie" else 1e-12  # double-float rounding on entries that vanish analytically
+        assert (num / np.maximum(den[~near], floor)).max() < tol
+
+
+def test_double_float_fallback_for_large_wavenumbers():
+    """k (edge_test + edge_trial) 2 >= 350 is beyond the double-float sine table: the mixed path's
+    singular pairs fall back to the FP64 kernel (bit-identical local matrices) and the assembly
+    still meets the mixed tolerance against the oracle."""
+    m = bg.icosphere(1)
+    X = bg.raviartthomas(m)
+    e = np.linalg.norm(m.vertices[m.triangles[:, 0]] - m.vertices[m.triangles[:, 1]], axis=1).max()
+    k = 400.0 / (4 * e)  # k (2 e) 2 = 400 > 350
+    op = bg.Maxwell3D.singlelayer(wavenumber=k)
+    tau, sigma = _nonfar_pairs(X, k * k)
+    L64, _ = bg.local_matrices(op, X, X, tau, sigma)
+    Lmx, _ = bg.local_matrices(op, X, X, tau, sigma, precision="mixed")
+    np.testing.assert_array_equal(Lmx, L64)
+    ref = oracle.assemble(op, X, X, bg.QuadStrat())
+    assert rel(bg.assemble_gpu(op, X, X, bg.GPUConfiguration(precision="mixed")).astype(np.complex128), ref) < MIXED_TOL
+    assert rel(bg.assemble_gpu(op, X, X, bg.GPUConfiguration(precision="fp64")), ref) < FP64_TOL
