@@ -141,8 +141,8 @@ def _near(local, fx, name, qt, qb, pre="near_", op=None, **kw):
     return L, _errors(L, d[pre + name]).max()
 
 
-def _oracle(op, X, Y, qs, tau, sigma):
-    return oracle.local_matrices(op, X, Y, qs, tau, sigma)
+def _oracle(op, X, Y, qs, tau, sigma, force_class=-1):
+    return oracle.local_matrices(op, X, Y, qs, tau, sigma, force_class=force_class)
 
 
 @pytest.mark.parametrize("name", ALL)
@@ -218,8 +218,8 @@ def test_oracle_near_rule_is_outer_rule_times_closed_form(fx, name, pre, qt, qb)
 
 
 def _gpu(precision):
-    def local(op, X, Y, qs, tau, sigma):
-        return bg.local_matrices(op, X, Y, tau, sigma, quadstrat=qs, precision=precision)
+    def local(op, X, Y, qs, tau, sigma, force_class=-1):
+        return bg.local_matrices(op, X, Y, tau, sigma, quadstrat=qs, precision=precision, force_class=force_class)
     return local
 
 
@@ -257,7 +257,11 @@ def test_gpu_near_rule_matches_oracle_at_wavenumbers(fx, name, precision, k):
     base = fx[3][name]
     op = Operator(base.kind, base.alpha, 1j * k, base.beta)
     local = _gpu(precision)
+    # at k = 25 these pairs classify as far and the near rule is forced: |gamma R| reaches 7, where the
+    # extracted gamma^2 R / 2 term and the smooth rest cancel to a few percent, so rounding differences
+    # between the two FP64 implementations grow to ~1e-12
+    tol = 1e-12 if k < 10 else 5e-12
     for pre in NEAR_SETS:
-        L, _ = _near(local, fx, name, 12, 13, pre, op=op)
-        ref, _ = _near(_oracle, fx, name, 12, 13, pre, op=op)
-        assert _errors(L, ref).max() < 1e-12
+        L, _ = _near(local, fx, name, 12, 13, pre, op=op, force_class=4)
+        ref, _ = _near(_oracle, fx, name, 12, 13, pre, op=op, force_class=4)
+        assert _errors(L, ref).max() < tol
