@@ -784,9 +784,8 @@ __global__ void __launch_bounds__(256) k_singular(OpParams op1, const OpParams* 
                                                   int near_only) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < n; e += warps) {
-    if (abort_flag && *abort_flag) return;
-    if (near_only && ent_cls[e] != BGB_CLASS_NEAR) continue;  // the others come from the double-float kernel
+  const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  auto entry = [&](int64_t e) {
     const int tau = ent_tau[e];
     const OpParams op = BATCH ? ops[tri_problem[tau]] : op1;
     const Geo64 A = tg[tau], B = bg[ent_sigma[e]];
@@ -799,6 +798,25 @@ __global__ void __launch_bounds__(256) k_singular(OpParams op1, const OpParams* 
         if (lane == q) v = L[q / 3][q % 3];
       out[e * 9 + lane] = v;
     }
+  };
+  if (near_only) {
+    // near pairs only (the others come from the double-float kernel): a warp reads the classes of
+    // 32 entries at once and integrates the near ones among them
+    for (int64_t e0 = warp0 * 32; e0 < n; e0 += warps * 32) {
+      if (abort_flag && *abort_flag) return;
+      const int64_t e = e0 + lane;
+      unsigned near = __ballot_sync(0xffffffffu, e < n && ent_cls[e] == BGB_CLASS_NEAR);
+      while (near) {
+        const int l = __ffs(near) - 1;
+        near &= near - 1;
+        entry(e0 + l);
+      }
+    }
+    return;
+  }
+  for (int64_t e = warp0; e < n; e += warps) {
+    if (abort_flag && *abort_flag) return;
+    entry(e);
   }
 }
 

@@ -82,8 +82,9 @@ def dist_init(ngpus):
     if world > 1:
         import torch
         import torch.distributed as dist
-        backend = "nccl" if torch.cuda.is_available() else "gloo"
-        dist.init_process_group(backend=backend)
+        if not dist.is_initialized():
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            dist.init_process_group(backend=backend)
         if torch.cuda.is_available():
             torch.cuda.set_device(local)
     return rank, world, local
@@ -159,23 +160,26 @@ def flush_l2(buf):
     buf.add_(1)
 
 
-def time_fill(bg, X, op, prec, steps, warmup, local, out="device", pinned=None, cfg=None):
-    """Per-step device time (CUDA events on the launching stream) of full assemblies."""
+def time_fill(bg, X, op, prec, steps, warmup, local, out="device", pinned=None, cfg=None, rows=None):
+    """Per-step device time (CUDA events on the launching stream) of full assemblies, or of the row
+    window rows = (row0, nrows)."""
     import torch
     cfg = cfg or bg.GPUConfiguration(precision=prec, device=local)
     scratch = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")
     dt = np.complex64 if prec == "mixed" else np.complex128
+    nr = X.nfun if rows is None else int(rows[1])
     Zbuf = None
     if out == "device":
         tdt = torch.complex64 if prec == "mixed" else torch.complex128
-        Zbuf = torch.empty((X.nfun, X.nfun), dtype=tdt, device=f"cuda:{local}")
+        Zbuf = torch.empty((X.nfun, nr), dtype=tdt, device=f"cuda:{local}")
     stats = []
 
     def one():
         if out == "device":
-            _, st = bg.assemble_gpu(op, X, X, cfg, out="device", out_buffer=Zbuf, return_stats=True)
+            _, st = bg.assemble_gpu(op, X, X, cfg, out="device", out_buffer=Zbuf, rows=rows, return_stats=True)
         else:
-            _, st = bg.assemble_gpu(op, X, X, cfg, out="host", out_buffer=pinned, dtype=dt, return_stats=True)
+            _, st = bg.assemble_gpu(op, X, X, cfg, out="host", out_buffer=pinned, dtype=dt, rows=rows,
+                                    return_stats=True)
         return st
 
     for _ in range(warmup):
@@ -416,8 +420,9 @@ def oracle_rows_error(op, X, Zrows, rows, qs=None):
     return rows_error(np.asarray(Zrows, dtype=np.complex128), ref)
 
 
-def run_c3(args):
-    """Near-singular stress: MFIE (RWG) and Helmholtz single layer (Lagrange) on two plates."""
+def run_c3(args, emit=True):
+    """Near-singular stress: MFIE (RWG) and Helmholtz single layer (Lagrange) on two plates.  Returns
+    the line (rank 0; None elsewhere) and prints it when `emit`."""
     import torch
     import beastgpu_gb300 as bg
     rank, world, local = dist_init(args.gpus)
@@ -435,7 +440,8 @@ def run_c3(args):
             rows = np.sort(np.random.default_rng(3).choice(X.nfun, 200, replace=False)).astype(np.int32)
             r = {"functions": X.nfun}
             for prec in ("mixed", "fp64"):
-                ms, st, _, Z = time_fill(bg, X, op, prec, args.steps, args.warmup, local)
+                steps = args.steps if prec == "mixed" else args.fp64_steps
+                ms, st, _, Z = time_fill(bg, X, op, prec, steps, args.warmup, local)
                 m = max_over_ranks(float(np.mean(ms)), world, local)
                 tot_ms[prec] += m
                 launches += sum(x["kernel_launches"] for x in st) if prec == "mixed" else 0
@@ -450,19 +456,22 @@ def run_c3(args):
                 torch.cuda.empty_cache()
             res[name] = r
     if rank != 0:
-        return 0
+        return None
     value = world * 2 * pairs / (tot_ms["mixed"] * 1e-3)
     cfg = {"workload": "MFIE (RWG) + Helmholtz SL (Lagrange, interior vertices) on two jittered 96x96 plates, "
                        "gap 0.01, k=2*pi*2", "triangles": mesh.nt, "pairs_per_step": 2 * pairs,
            "l2": "outputs > L2; a 256 MiB buffer is written between timed steps"}
-    print(json.dumps(line_base(args, world, value, tot_ms["mixed"], "f32 far pairs + double-float (f32 pairs) singular/near (mixed)",
-                               cfg, fp64_value=world * 2 * pairs / (tot_ms["fp64"] * 1e-3), cases=res,
-                               clocks=clocks.summary(), gpu_launches=launches)))
-    return 0
+    line = line_base(args, world, value, tot_ms["mixed"], "f32 far pairs + double-float singular, FP64 near (mixed)",
+                     cfg, fp64_value=world * 2 * pairs / (tot_ms["fp64"] * 1e-3), cases=res,
+                     clocks=clocks.summary(), gpu_launches=launches)
+    if emit:
+        print(json.dumps(line))
+    return line
 
 
-def run_c4(args):
-    """64 uneven ellipsoids: one batched persistent launch (CUDA graph) vs 64 sequential assemblies."""
+def run_c4(args, emit=True):
+    """64 uneven ellipsoids: one batched persistent launch (CUDA graph) vs 64 sequential assemblies.
+    Returns the line (rank 0; None elsewhere) and prints it when `emit`."""
     import torch
     import beastgpu_gb300 as bg
     rank, world, local = dist_init(args.gpus)
@@ -476,11 +485,13 @@ def run_c4(args):
     out = {}
     with ClockSampler(local) as clocks:
         for prec in ("mixed", "fp64"):
-            B = bg.Batch(probs, bg.GPUConfiguration(precision=prec, device=local), out="device", autotune=True)
+            steps = args.steps if prec == "mixed" else args.fp64_steps
+            B = bg.Batch(probs, bg.GPUConfiguration(precision=prec, device=local), out="device",
+                         autotune=prec == "mixed" or not getattr(args, "c4_fp64_default_tiles", False))
             for _ in range(args.warmup):
                 B.run()
             torch.cuda.synchronize()
-            ms = [B.run()["ms_total"] for _ in range(args.steps)]
+            ms = [B.run()["ms_total"] for _ in range(steps)]
             graph_ms = max_over_ranks(float(np.mean(ms)), world, local)
             # 64 sequential single assemblies (one bgb_assemble each), device outputs
             bufs = [torch.empty((X.nfun, X.nfun), dtype=torch.complex64 if prec == "mixed" else torch.complex128,
@@ -495,11 +506,11 @@ def run_c4(args):
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            for _ in range(args.steps):
+            for _ in range(steps):
                 seq()
             e1.record(stream)
             torch.cuda.synchronize()
-            seq_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, world, local)
+            seq_ms = max_over_ranks(e0.elapsed_time(e1) / steps, world, local)
             same = all(bool(torch.equal(a.T, b)) for a, b in zip(bufs, B.outputs))
             errs = []
             if rank == 0:
@@ -517,16 +528,18 @@ def run_c4(args):
             del bufs
             torch.cuda.empty_cache()
     if rank != 0:
-        return 0
+        return None
     value = world * pairs / (out["mixed"]["graph_ms_per_step"] * 1e-3)
     cfg = {"workload": "64 seeded ellipsoids (icosphere levels 1-4, axes U[0.5,2], k U[1,10]), EFIE on RWG, "
                        "one persistent CUDA-graph launch, autotuned tiles and schedule",
            "problems": 64, "triangles": sum(m.nt for m, _ in batch), "pairs_per_step": pairs}
-    print(json.dumps(line_base(args, world, value, out["mixed"]["graph_ms_per_step"],
-                               "f32 far pairs + double-float (f32 pairs) singular/near (mixed)", cfg,
-                               vs_sequential_fp64=out["fp64"]["sequential_ms_per_step"] / out["mixed"]["graph_ms_per_step"],
-                               results=out, clocks=clocks.summary(), gpu_launches=3 * (args.steps + args.warmup))))
-    return 0
+    line = line_base(args, world, value, out["mixed"]["graph_ms_per_step"],
+                     "f32 far pairs + double-float singular, FP64 near (mixed)", cfg,
+                     vs_sequential_fp64=out["fp64"]["sequential_ms_per_step"] / out["mixed"]["graph_ms_per_step"],
+                     results=out, clocks=clocks.summary(), gpu_launches=3 * (args.steps + args.warmup))
+    if emit:
+        print(json.dumps(line))
+    return line
 
 
 def run_c5(args):
@@ -614,9 +627,10 @@ def cube_config(mesh, X, d, extra=None):
     return c
 
 
-def run_cube(args):
+def run_cube(args, emit=True):
     """The reference's benchmark workload (data/graph_data.jl:2-4): mixed (value) and plain FP64 into HBM,
-    both end to end into pinned host memory (FP64 into ComplexF64 like the reference's storeGPU path)."""
+    both end to end into pinned host memory (FP64 into ComplexF64 like the reference's storeGPU path).
+    Returns the line (rank 0; None elsewhere) and prints it when `emit`."""
     import torch
     import oracle
     rank, world, local = dist_init(args.gpus)
@@ -661,15 +675,16 @@ def run_cube(args):
                "d2h_bytes_per_step": n * n * 8, "ms_per_step": em,
                "ms_copy": float(np.mean([s["ms_copy"] for s in st_e]))}
         del pinned
-        pinned = torch.empty((n, n), dtype=torch.complex128, pin_memory=True)
-        ms_e64, st_e64, _, _ = time_fill(bg, X, op, "fp64", 1, 0, local, out="host", pinned=pinned)
-        e64 = max_over_ranks(float(np.mean(ms_e64)), world, local)
-        e2e64 = {"value": world * pairs / (e64 * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                 "d2h_bytes_per_step": n * n * 16, "ms_per_step": e64,
-                 "ms_copy": float(np.mean([s["ms_copy"] for s in st_e64]))}
-        del pinned
+        if not getattr(args, "cube_no_fp64_e2e", False):
+            pinned = torch.empty((n, n), dtype=torch.complex128, pin_memory=True)
+            ms_e64, st_e64, _, _ = time_fill(bg, X, op, "fp64", 1, 0, local, out="host", pinned=pinned)
+            e64 = max_over_ranks(float(np.mean(ms_e64)), world, local)
+            e2e64 = {"value": world * pairs / (e64 * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                     "d2h_bytes_per_step": n * n * 16, "ms_per_step": e64,
+                     "ms_copy": float(np.mean([s["ms_copy"] for s in st_e64]))}
+            del pinned
     if rank != 0:
-        return 0
+        return None
 
     def kernels(st):
         return {k: float(np.mean([s["ms_" + k] for s in st])) for k in ("far", "singular", "classify")}
@@ -686,8 +701,33 @@ def run_cube(args):
                          "source": f"data/GPU_full/storeGPU/{d}/full_time.txt (median), FP64, GPU write-back, "
                                    "ComplexF64 host matrix; GPU model not recorded"})
     line.update(out)
-    print(json.dumps(line))
-    return 0
+    if emit:
+        print(json.dumps(line))
+    return line
+
+
+def extra_workloads(args):
+    """Short runs of the other workloads for the default line (one GPU): the two-plate near-singular
+    stress, the 64-ellipsoid batch and the reference's cube benchmark at d = 40, each with its own
+    error against the oracle.  Each is also a workload of its own (--workload c3 | c4 | cube)."""
+    import copy
+    import torch
+    sub = copy.copy(args)
+    sub.steps, sub.warmup, sub.fp64_steps = 3, 1, 1
+    sub.cube_d, sub.no_e2e, sub.cube_no_fp64_e2e, sub.c4_fp64_default_tiles = 40, False, True, True
+    out = {}
+    for name, fn in (("c3", run_c3), ("c4", run_c4), ("cube_d40", run_cube)):
+        t0 = time.perf_counter()
+        line = fn(sub, emit=False)
+        torch.cuda.empty_cache()
+        if line is None:
+            continue
+        keep = ("value", "unit", "ms_per_step", "fp64_value", "fp64_ms_per_step", "mixed_over_fp64", "config",
+                "error_vs_oracle", "cases", "results", "vs_sequential_fp64", "e2e", "reference_recorded",
+                "kernels_ms", "halo_redundancy", "cpu_baseline", "clocks")
+        out[name] = {k: line[k] for k in keep if k in line}
+        out[name]["wall_s"] = time.perf_counter() - t0
+    return out
 
 
 def main():
@@ -700,6 +740,7 @@ def main():
     ap.add_argument("--ref-rows", type=int, default=200)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="default workload: leave out the c3 / c4 / cube sub-results")
     ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5", "cube", "curve"])
     ap.add_argument("--cube-d", type=int, default=40, help="cube: density d of meshcuboid(1, 1, 1, 0.5/d)")
     ap.add_argument("--hbm-budget", type=int, default=0, help="c5: HBM budget in bytes (0 = 90% of free)")
@@ -712,40 +753,46 @@ def main():
     if args.profile_level is not None:
         return run_profile_case(args)
     if args.workload != "c2":
-        return {"c3": run_c3, "c4": run_c4, "c5": run_c5, "cube": run_cube, "curve": run_curve}[args.workload](args)
+        rc = {"c3": run_c3, "c4": run_c4, "c5": run_c5, "cube": run_cube, "curve": run_curve}[args.workload](args)
+        return rc if isinstance(rc, int) else 0
 
     import torch
     rank, world, local = dist_init(args.gpus)
     bg, mesh, X, op, qs = workload()
     pairs = mesh.nt * mesh.nt
+    # N ranks: one matrix, cut into N balanced row windows (each rank assembles its rows against all
+    # trial functions; no data exchange); value = the whole matrix's pairs / the slowest rank's time
+    win = None if world == 1 else bg.row_shard(X.nfun, rank, world)
+    r0, nr = (0, X.nfun) if win is None else win
     # the caller's pinned output of the end-to-end leg, allocated once up front (as an application
     # holds its output buffer), before the CPU oracle's allocations
-    pinned = None if args.no_e2e else torch.empty((X.nfun, X.nfun), dtype=torch.complex64, pin_memory=True)
+    pinned = None if args.no_e2e else torch.empty((X.nfun, nr), dtype=torch.complex64, pin_memory=True)
 
     # roofline denominators measured live (FP32 / FP64 FMA issue, MUFU)
     fp32_peak, fp64_peak, mufu_peak = bg.measure_issue_peaks(local)
 
     barrier(world)
     with ClockSampler(local) as clocks:
-        ms_mixed, st_mixed, wall_mixed, Zm = time_fill(bg, X, op, "mixed", args.steps, args.warmup, local)
+        ms_mixed, st_mixed, wall_mixed, Zm = time_fill(bg, X, op, "mixed", args.steps, args.warmup, local, rows=win)
     barrier(world)
     ms_step = max_over_ranks(float(np.mean(ms_mixed)), world, local)
-    value = world * pairs / (ms_step * 1e-3)
+    value = pairs / (ms_step * 1e-3)
 
-    ms_fp64, st_fp64, _, Zd = time_fill(bg, X, op, "fp64", args.fp64_steps, min(args.warmup, 3), local)
+    ms_fp64, st_fp64, _, Zd = time_fill(bg, X, op, "fp64", args.fp64_steps, min(args.warmup, 3), local, rows=win)
     fp64_ms = max_over_ranks(float(np.mean(ms_fp64)), world, local)
-    fp64_value = world * pairs / (fp64_ms * 1e-3)
+    fp64_value = pairs / (fp64_ms * 1e-3)
 
     out = {}
     if rank == 0:
-        # accuracy on 1000 seeded rows against the FP64 CPU oracle (also the CPU baseline sample)
+        # accuracy on 1000 seeded rows (of rank 0's window) against the FP64 CPU oracle (also the CPU
+        # baseline sample)
         import oracle
-        rows = np.sort(np.random.default_rng(ERR_SEED).choice(X.nfun, ERR_ROWS, replace=False)).astype(np.int32)
+        rows = (r0 + np.sort(np.random.default_rng(ERR_SEED).choice(nr, min(nr, ERR_ROWS), replace=False))).astype(np.int32)
         threads = oracle.max_threads()
         t0 = time.perf_counter()
         ref = oracle.assemble_rows(op, X, X, qs, rows, nthreads=threads)
         cpu_s = time.perf_counter() - t0
-        ridx = torch.as_tensor(rows.astype(np.int64), device=Zm.device)
+        ridx = torch.as_tensor((rows - r0).astype(np.int64), device=Zm.device)
         # Zbuf is (cols, rows) storage of the column-major matrix: row r of Z is column r of Zbuf
         err_mixed = rows_error(Zm[:, ridx].T.cpu().numpy().astype(np.complex128), ref)
         err_fp64 = rows_error(Zd[:, ridx].T.cpu().numpy(), ref)
@@ -761,11 +808,11 @@ def main():
         del Zm
         torch.cuda.empty_cache()
         ms_e2e, st_e2e, wall_e2e, _ = time_fill(bg, X, op, "mixed", max(3, args.steps // 2), 1, local, out="host",
-                                                pinned=pinned)
+                                                pinned=pinned, rows=win)
         e2e_ms = max_over_ranks(float(np.mean(ms_e2e)), world, local)
         h2d = X.mesh.vertices.nbytes + X.mesh.triangles.nbytes + X.fn_index.nbytes + X.fn_coef.nbytes
-        e2e = {"value": world * pairs / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(X.nfun) * int(X.nfun) * 8, "ms_per_step": e2e_ms,
+        e2e = {"value": pairs / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(X.nfun) * int(nr) * 8, "ms_per_step": e2e_ms,
                "ms_copy": float(np.mean([s["ms_copy"] for s in st_e2e]))}
         del pinned
 
@@ -804,18 +851,21 @@ def main():
                                 "classify": float(np.mean([s["ms_classify"] for s in st_mixed]))},
                  "far_tflops": far_tf, "singular_tflops": sing_tf,
                  "fp64_peak_tflops": fp64_peak, "mufu_peak_tops": mufu_peak,
-                 "halo_redundancy": st_mixed[0]["pairs_computed"] / pairs})
+                 "halo_redundancy": st_mixed[0]["pairs_computed"] / st_mixed[0]["pairs_total"]})
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+            "scaling": "strong" if world > 1 else "weak",
             "vs_baseline": None, "dtype": "f32 far pairs + double-float (f32 pairs) singular/near (mixed)",
             "data": "synthetic (seeded icosphere, built in-process)",
-            "config": config_dict(mesh, X, {"parallelism": f"{world} independent matrices, one per rank, no collective"
-                                            if world > 1 else "single GPU"}),
+            "config": config_dict(mesh, X, {"parallelism": f"one matrix in {world} row windows, one per rank, no "
+                                            "collective on the data path" if world > 1 else "single GPU"}),
             "fp64_value": fp64_value, "fp64_ms_per_step": fp64_ms, "mixed_over_fp64": value / fp64_value,
             "roofline": roof, "clocks": clocks.summary(),
             "gpu_launches": int(sum(s["kernel_launches"] for s in st_mixed)),
             "e2e": e2e}
     line.update(out)
+    if world == 1 and not args.no_extra:
+        line["workloads"] = extra_workloads(args)
     print(json.dumps(line))
     return 0
 

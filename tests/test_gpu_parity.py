@@ -456,3 +456,39 @@ def test_double_float_fallback_for_large_wavenumbers():
     ref = oracle.assemble(op, X, X, bg.QuadStrat())
     assert rel(bg.assemble_gpu(op, X, X, bg.GPUConfiguration(precision="mixed")).astype(np.complex128), ref) < MIXED_TOL
     assert rel(bg.assemble_gpu(op, X, X, bg.GPUConfiguration(precision="fp64")), ref) < FP64_TOL
+
+
+def test_mixed_far_pairs_hold_the_bound_without_compensated_sums():
+    """The mixed far kernel accumulates its moments in plain FP32 (no Kahan compensation): its error
+    comes from the phase and from cancellation in the bilinear forms, which the double-float phase
+    base and the centroid-relative coordinates remove, not from summation.  Shown where summation
+    and phase are hardest: (a) the 13 x 13 far rule, 169 point pairs summed per pair; (b) k times the
+    meshes' diameter at 2.9e5, just inside the 3e5 range of the exact phase reduction (two small plates
+    29 apart, k h ~ 1); beyond the range the call is refused."""
+    m = bg.icosphere(2)
+    X = bg.raviartthomas(m)
+    op = bg.Maxwell3D.singlelayer(wavenumber=K1)
+    c = oracle.classify_block(X, X, K1 * K1)
+    t, s = np.nonzero(c == 0)
+    sel = np.random.default_rng(5).choice(t.size, 400, replace=False)
+    qs = bg.QuadStrat(far_test=13, far_trial=13)
+    L64, _ = bg.local_matrices(op, X, X, t[sel], s[sel], quadstrat=qs, force_class=0)
+    Lmx, _ = bg.local_matrices(op, X, X, t[sel], s[sel], quadstrat=qs, force_class=0, precision="mixed")
+    assert _per_pair_rel(Lmx, L64).max() < 1e-5
+
+    p = bg.plate(4, jitter=0.3, seed=4)
+    v = p.vertices * 4e-4  # h = 1e-4
+    w = v.copy()
+    w[:, 0] += 29.0
+    mesh = bg.Mesh(np.concatenate([v, w]), np.concatenate([p.triangles, p.triangles + p.nv]))
+    Y = bg.raviartthomas(mesh)
+    k = 1.0e4  # k * diameter = 2.9e5, k h = 1
+    op = bg.Maxwell3D.singlelayer(wavenumber=k)
+    tau = np.repeat(np.arange(p.nt), p.nt).astype(np.int32)
+    sig = (p.nt + np.tile(np.arange(p.nt), p.nt)).astype(np.int32)
+    L64, c64 = bg.local_matrices(op, Y, Y, tau, sig)
+    Lmx, _ = bg.local_matrices(op, Y, Y, tau, sig, precision="mixed")
+    assert np.all(c64 == 0)
+    assert _per_pair_rel(Lmx, L64).max() < 1e-5
+    with pytest.raises(Exception, match="3e5"):
+        bg.local_matrices(bg.Maxwell3D.singlelayer(wavenumber=1.1e4), Y, Y, tau, sig, precision="mixed")

@@ -1,9 +1,10 @@
-"""The multi-process path on CPU with gloo, world size 2 (no GPU involved).
+"""The multi-process path with gloo, world size 2.
 
-Each rank takes its row window of one matrix (beastgpu_gb300.row_shard), computes it with the
-FP64 oracle as the stand-in for its GPU, and the ranks check that the windows tile the matrix
-exactly and agree with a single-process assembly; the bench's barrier and max-over-ranks
-reduction run under the same process group.
+Each rank takes its row window of one matrix (beastgpu_gb300.row_shard) and the ranks check that
+the windows tile the matrix exactly and agree with a single-process assembly.  On the CPU the FP64
+oracle stands in for each rank's GPU, and the bench's barrier and max-over-ranks reduction run
+under the same process group; with a GPU both ranks drive libbeastgb's row windows (on the one
+GPU of this machine: independent launches, no kernel waits on another rank).
 """
 import os
 import socket
@@ -75,3 +76,46 @@ def test_row_shard_partitions(n, world):
     for (a0, an), (b0, _) in zip(spans, spans[1:]):
         assert a0 + an == b0
     assert max(s[1] for s in spans) - min(s[1] for s in spans) <= 1
+
+
+def _rank_main_gpu(rank, world, port, out_dir):
+    os.environ.update({"MASTER_ADDR": "127.0.0.1", "MASTER_PORT": str(port)})
+    sys.path.insert(0, ROOT)
+    import beastgpu_gb300 as bg
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    m = bg.icosphere(3)
+    X = bg.raviartthomas(m)
+    op = bg.Maxwell3D.singlelayer(wavenumber=2 * np.pi * 2)
+    row0, nrows = bg.row_shard(X.nfun, rank, world)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        Z = bg.assemble_gpu(op, X, X, bg.GPUConfiguration(precision=prec), rows=(row0, nrows))
+        t = torch.from_numpy(np.ascontiguousarray(np.stack([Z.real, Z.imag], -1)).astype(np.float64)).reshape(-1)
+        sizes = [torch.zeros(1, dtype=torch.int64) for _ in range(world)]
+        dist.all_gather(sizes, torch.tensor([t.numel()], dtype=torch.int64))
+        bufs = [torch.zeros(int(s.item()), dtype=t.dtype) for s in sizes]
+        dist.all_gather(bufs, t)
+        out[prec] = bufs
+    if rank == 0:
+        for prec, bufs in out.items():
+            parts = [b.reshape(-1, X.nfun, 2).numpy() for b in bufs]
+            np.save(os.path.join(out_dir, f"gathered_{prec}.npy"),
+                    np.concatenate([p[..., 0] + 1j * p[..., 1] for p in parts]))
+    dist.destroy_process_group()
+
+
+@pytest.mark.gpu
+def test_row_windows_through_the_library_on_two_gloo_ranks(tmp_path):
+    """Two ranks assemble their row windows of one EFIE matrix with libbeastgb: the gathered windows
+    equal the single-process matrix bit for bit, in both precisions (results do not depend on the
+    tiling, which the windows change)."""
+    import beastgpu_gb300 as bg
+    world = 2
+    mp.start_processes(_rank_main_gpu, args=(world, _free_port(), str(tmp_path)), nprocs=world, start_method="spawn")
+    m = bg.icosphere(3)
+    X = bg.raviartthomas(m)
+    op = bg.Maxwell3D.singlelayer(wavenumber=2 * np.pi * 2)
+    for prec in ("fp64", "mixed"):
+        full = bg.assemble_gpu(op, X, X, bg.GPUConfiguration(precision=prec))
+        gathered = np.load(tmp_path / f"gathered_{prec}.npy")
+        np.testing.assert_array_equal(gathered, full.astype(np.complex128))
