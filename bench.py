@@ -14,7 +14,9 @@ kernels against the FP64 CPU oracle are measured on 1000 seeded rows.
 
 Other workloads print the same kind of line for their own configuration:
   --workload c3   MFIE on RWG and Helmholtz single layer on Lagrange over two jittered
-                  96 x 96 coplanar plates 0.01 apart (36,864 triangles), k = 2 pi * 2
+                  96 x 96 coplanar plates 0.01 apart (36,864 triangles), k = 2 pi * 2; beside it the MFIE
+                  on the same plates 0.003 apart with the second one turned up by 30 degrees (near pairs
+                  across the fold with values)
   --workload c4   64 seeded ellipsoids (icosphere levels 1-4, axes U[0.5, 2], k U[1, 10]), EFIE,
                   one batched persistent launch replayed from a CUDA graph vs 64 sequential
                   plain FP64 assemblies
@@ -390,16 +392,34 @@ def run_reference(args):
 
 
 def run_profile_case(args):
-    """Small case for ncu captures: EFIE on an icosphere of the given level, device output."""
+    """Small cases for ncu captures, device output: EFIE on an icosphere of level --profile-level
+    (mixed, then FP64); with --profile-cube D also the Helmholtz single layer on meshcuboid(1,1,1,0.5/D)
+    (the Lagrange instances); with --profile-batch also one run of the 64-ellipsoid batch (mixed, no
+    autotuning: its persistent far launch)."""
     import torch
     import beastgpu_gb300 as bg
-    mesh = bg.icosphere(args.profile_level)
-    X = bg.raviartthomas(mesh)
-    op = bg.Maxwell3D.singlelayer(wavenumber=KWAVE)
-    for prec in ("mixed", "fp64"):
-        ms, st, _, _ = time_fill(bg, X, op, prec, args.steps, args.warmup, 0)
-        print(json.dumps({"profile_case": f"icosphere level {args.profile_level}", "precision": prec,
-                          "ms_per_step": float(np.mean(ms)), "stats": st[-1]}))
+    cases = []
+    if args.profile_level > 0:
+        mesh = bg.icosphere(args.profile_level)
+        cases.append((f"icosphere level {args.profile_level}", bg.raviartthomas(mesh),
+                      bg.Maxwell3D.singlelayer(wavenumber=KWAVE)))
+    if args.profile_cube:
+        mesh = bg.meshcuboid(1.0, 1.0, 1.0, 0.5 / args.profile_cube)
+        cases.append((f"meshcuboid(1,1,1,0.5/{args.profile_cube})", bg.lagrangec0d1(mesh),
+                      bg.Helmholtz3D.singlelayer(wavenumber=1.0)))
+    for name, X, op in cases:
+        for prec in ("mixed", "fp64"):
+            ms, st, _, _ = time_fill(bg, X, op, prec, args.steps, args.warmup, 0)
+            print(json.dumps({"profile_case": name, "precision": prec, "ms_per_step": float(np.mean(ms)),
+                              "stats": st[-1]}))
+    if args.profile_batch:
+        probs = []
+        for mesh, k in bg.ellipsoid_batch(64, seed=2):
+            X = bg.raviartthomas(mesh)
+            probs.append((bg.Maxwell3D.singlelayer(wavenumber=k), X, X))
+        B = bg.Batch(probs, bg.GPUConfiguration(precision="mixed"), out="device", autotune=False)
+        print(json.dumps({"profile_case": "64-ellipsoid batch", "precision": "mixed", "stats": B.create_stats}))
+        B.close()
     torch.cuda.synchronize()
     return 0
 
@@ -429,8 +449,18 @@ def run_c3(args, emit=True):
     mesh = bg.two_plates(96, jitter=0.3, seed=1, gap=0.01)
     k = 2 * np.pi * 2
     R, L = bg.raviartthomas(mesh), bg.lagrangec0d1(mesh)
+    # the Maxwell double layer vanishes on coplanar plates: two such plates 0.003 apart (0.3 h) with the
+    # second one turned up by 30 degrees about its edge give it near pairs with values across the fold
+    # (reported beside, not in `value`)
+    fp = bg.two_plates(96, jitter=0.3, seed=1, gap=0.003)
+    v = fp.vertices.copy()
+    up = v[:, 0] > 1.0
+    v[up, 2] = (v[up, 0] - 1.003) * np.sin(np.pi / 6)
+    v[up, 0] = 1.003 + (v[up, 0] - 1.003) * np.cos(np.pi / 6)
+    folded = bg.Mesh(v, fp.triangles)
     cases = [("mfie_rwg", bg.Maxwell3D.doublelayer(wavenumber=k), R),
-             ("helmholtz_sl_lagrange", bg.Helmholtz3D.singlelayer(wavenumber=k), L)]
+             ("helmholtz_sl_lagrange", bg.Helmholtz3D.singlelayer(wavenumber=k), L),
+             ("mfie_rwg_folded", bg.Maxwell3D.doublelayer(wavenumber=k), bg.raviartthomas(folded))]
     pairs = mesh.nt * mesh.nt
     res = {}
     tot_ms = {"mixed": 0.0, "fp64": 0.0}
@@ -443,12 +473,13 @@ def run_c3(args, emit=True):
                 steps = args.steps if prec == "mixed" else args.fp64_steps
                 ms, st, _, Z = time_fill(bg, X, op, prec, steps, args.warmup, local)
                 m = max_over_ranks(float(np.mean(ms)), world, local)
-                tot_ms[prec] += m
+                if name != "mfie_rwg_folded":
+                    tot_ms[prec] += m
                 launches += sum(x["kernel_launches"] for x in st) if prec == "mixed" else 0
                 Zr = Z[:, torch.as_tensor(rows.astype(np.int64), device=Z.device)].T.cpu().numpy()
                 r[prec] = {"ms_per_step": m, "pairs_per_s": pairs / (m * 1e-3), "stats": st[-1]}
                 if rank == 0:
-                    if name.startswith("mfie"):
+                    if name == "mfie_rwg":
                         r[prec]["max_abs_entry"] = float(np.abs(Zr).max())  # coplanar plates: exactly zero
                     else:
                         r[prec]["error_vs_oracle_200_rows"] = oracle_rows_error(op, X, Zr, rows)
@@ -743,10 +774,13 @@ def main():
     ap.add_argument("--no-extra", action="store_true", help="default workload: leave out the c3 / c4 / cube sub-results")
     ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5", "cube", "curve"])
     ap.add_argument("--cube-d", type=int, default=40, help="cube: density d of meshcuboid(1, 1, 1, 0.5/d)")
-    ap.add_argument("--hbm-budget", type=int, default=0, help="c5: HBM budget in bytes (0 = 90% of free)")
+    ap.add_argument("--hbm-budget", type=int, default=0, help="c5: HBM budget in bytes (0 = 90%% of free)")
     ap.add_argument("--curve-segments", type=int, default=CURVE_N, help="curve: segments of the ellipse")
     ap.add_argument("--profile-level", type=int, default=None,
-                    help="profiling case: run W + K mixed and FP64 fills of an icosphere of this level and exit")
+                    help="profiling case: run W + K mixed and FP64 fills of an icosphere of this level and exit "
+                         "(0: none, with --profile-cube / --profile-batch)")
+    ap.add_argument("--profile-cube", type=int, default=0, help="profiling case: also the cube at this density d")
+    ap.add_argument("--profile-batch", action="store_true", help="profiling case: also one 64-ellipsoid batch")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
