@@ -224,6 +224,37 @@ FarConst make_farconst(const OpParams& op, const RuleTable& R, const QuadSel& qs
     double h[3] = {p[0], p[1], 1.0 - p[0] - p[1]};
     for (int i = 0; i < 3; ++i) { k.shpB64[J][i] = h[i]; k.shpB[J][i] = (float)h[i]; }
   }
+  // plain FP64 kernel: series for exp(-i k (R - R0)) when |k (R - R0)| <= k (r_test + r_trial) is small
+  k.tay_n = 0;
+  if (test && trial && op.gamma[1] != 0.0) {
+    const double xmax = std::fabs(op.gamma[1]) * (max_centroid_radius(test) + max_centroid_radius(trial));
+    if (xmax <= 2.0) {
+      double fs = 1.0, fc = 1.0;  // (2j+1)!, (2j)!
+      int n = 1;
+      for (; n <= BGB_TAYLOR_MAX; ++n) {
+        // terms j < n kept: the first dropped terms are x^(2n) / (2n)! (cos) and x^(2n+1) / (2n+1)! (sin)
+        double tc = 1.0, ts = xmax;
+        for (int q = 1; q <= 2 * n; ++q) tc *= xmax / q;
+        for (int q = 2; q <= 2 * n + 1; ++q) ts *= xmax / q;
+        if (tc <= 0x1p-55 && ts <= 0x1p-55) break;
+      }
+      // measured on GB300: FP64 sincos of these small arguments costs about as much as 8 series terms
+      // (cube of the reference's benchmark, 4 terms: far stage 16.0 -> 14.4 s; icosphere level 5 at
+      // k = 8 pi, 11 terms: 1.13 -> 1.15 s), so the series is kept for short series only
+      if (n <= 6) {
+        k.tay_n = n;
+        for (int j = 0; j < n; ++j) {
+          if (j > 0) {
+            fc *= (2.0 * j - 1.0) * (2.0 * j);
+            fs *= (2.0 * j) * (2.0 * j + 1.0);
+          }
+          const double sg = (j & 1) ? -1.0 : 1.0;
+          k.tay_c[j] = sg / fc;
+          k.tay_s[j] = sg / fs;
+        }
+      }
+    }
+  }
   return k;
 }
 
@@ -304,6 +335,24 @@ double max_edge(const bgb_space* s) {
       m = std::max(m, d);
     }
   return m;
+}
+
+// Largest distance of a vertex from its triangle's centroid: bounds |x - c| for every rule point x.
+double max_centroid_radius(const bgb_space* s) {
+  double m = 0.0;
+  for (int64_t t = 0; t < s->nt; ++t) {
+    const double* v[3];
+    for (int a = 0; a < 3; ++a) v[a] = s->vertices + 3 * (int64_t)s->triangles[3 * t + a];
+    for (int a = 0; a < 3; ++a) {
+      double d2 = 0.0;
+      for (int c = 0; c < 3; ++c) {
+        const double d = v[a][c] - (v[0][c] + v[1][c] + v[2][c]) / 3.0;
+        d2 += d * d;
+      }
+      m = std::max(m, std::sqrt(d2));
+    }
+  }
+  return m * (1.0 + 1e-12);
 }
 
 bool df_singular_ok(const OpParams& op, double edge_t, double edge_b) {

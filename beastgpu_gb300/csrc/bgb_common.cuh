@@ -15,6 +15,7 @@
 
 #define BGB_MAXQ 13        // largest triangle rule (points)
 #define BGB_MAX_SS 16      // largest Gauss-Legendre order for Sauter-Schwab
+#define BGB_TAYLOR_MAX 16  // series terms of the plain FP64 far kernel's point-pair phase
 
 namespace bgb {
 

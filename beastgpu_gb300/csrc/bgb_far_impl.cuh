@@ -443,13 +443,22 @@ __device__ __forceinline__ void far_pair_mixed(const FarScalars& K, const float 
 // ----------------------------------------------------------------------------------------
 template <int OP, int QT, int QB>
 __device__ __forceinline__ void far_pair_fp64(const FarScalars& K, const double (*__restrict__ shpT)[3],
-                                              const double (*__restrict__ shpB)[3], const double* __restrict__ a,
+                                              const double (*__restrict__ shpB)[3], const double* __restrict__ tay_s,
+                                              const double* __restrict__ tay_c, const double* __restrict__ a,
                                               const double* __restrict__ b, double2 L[9]) {
   using OA = Off64<QT>;
   using OB = Off64<QB>;
   constexpr bool kHH = is_lagrange_op(OP);
   const double Dx = a[OA::C] - b[OB::C], Dy = a[OA::C + 1] - b[OB::C + 1], Dz = a[OA::C + 2] - b[OB::C + 2];
   const double gre = K.gamma[0], gim = K.gamma[1];
+  // Phase k R = k R0 + k (R - R0) with R0 the centroid distance: sin / cos of k R0 once per pair, and
+  // of the small k (R - R0) (|.| <= 2) from K.tay_n series terms per point pair (sincos otherwise).
+  const int tn = gim != 0.0 ? K.tay_n : 0;
+  double R0 = 0.0, s0 = 0.0, c0 = 1.0;
+  if (tn > 0) {
+    R0 = sqrt(Dx * Dx + Dy * Dy + Dz * Dz);
+    sincos(gim * R0, &s0, &c0);
+  }
   double nA[3] = {0, 0, 0}, nB[3] = {0, 0, 0};
   if (OP == BGB_OP_HELMHOLTZ3D_DLT || OP == BGB_OP_HELMHOLTZ3D_HS) tri_normal(a + OA::VO, a[OA::INV2A], nA);
   if (OP == BGB_OP_HELMHOLTZ3D_DL || OP == BGB_OP_HELMHOLTZ3D_HS) tri_normal(b + OB::VO, b[OB::INV2A], nB);
@@ -482,7 +491,19 @@ __device__ __forceinline__ void far_pair_fp64(const FarScalars& K, const double 
       const double rinv = rsqrt(R2);
       const double R = R2 * rinv;
       double sn = 0.0, cs = 1.0;
-      if (gim != 0.0) sincos(gim * R, &sn, &cs);
+      if (tn > 0) {
+        const double x = gim * (R - R0), x2 = x * x;
+        double ps = tay_s[tn - 1], pc = tay_c[tn - 1];
+        for (int j = tn - 2; j >= 0; --j) {
+          ps = fma(ps, x2, tay_s[j]);
+          pc = fma(pc, x2, tay_c[j]);
+        }
+        const double s1 = x * ps;
+        sn = fma(s0, pc, c0 * s1);  // sin(k R0 + x)
+        cs = fma(c0, pc, -s0 * s1); // cos(k R0 + x)
+      } else if (gim != 0.0) {
+        sincos(gim * R, &sn, &cs);
+      }
       double amp = wI * b[OB::W + J] * rinv;
       if (gre != 0.0) amp *= exp(-gre * R);
       const double gr = amp * cs, gi = -amp * sn;
@@ -648,6 +669,7 @@ __device__ __forceinline__ FarScalars far_scalars(const FarConst& K) {
   S.qb = K.qb;
   S.lossy = K.lossy;
   S.phase_direct = K.phase_direct;
+  S.tay_n = K.tay_n;
   S.k_hi = K.k_hi;
   S.k_lo = K.k_lo;
   S.gre = K.gre;
@@ -667,7 +689,7 @@ __device__ __forceinline__ void far_pair(const FarScalars& S, const FarConst& K,
   if constexpr (sizeof(typename P::R) == 4)
     far_pair_mixed<OP, QT, QB>(S, K.shpT, K.shpB, a, b, L);
   else
-    far_pair_fp64<OP, QT, QB>(S, K.shpT64, K.shpB64, a, b, L);
+    far_pair_fp64<OP, QT, QB>(S, K.shpT64, K.shpB64, K.tay_s, K.tay_c, a, b, L);
 }
 
 __device__ __forceinline__ int64_t find_sigma(const int64_t* __restrict__ off, const int* __restrict__ sig, int tau,

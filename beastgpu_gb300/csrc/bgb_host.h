@@ -139,6 +139,7 @@ int planner_threads();
 bool same_space(const bgb_space* a, const bgb_space* b);
 // Largest triangle edge of a space (host), for the argument range of the double-float sincos.
 double max_edge(const bgb_space* s);
+double max_centroid_radius(const bgb_space* s);
 // True when the mixed path may integrate singular / near pairs in double-float: no lossy
 // wave number and k R below the range of the df sin / cos.
 bool df_singular_ok(const OpParams& op, double edge_t, double edge_b);

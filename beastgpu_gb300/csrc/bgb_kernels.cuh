@@ -80,11 +80,17 @@ struct FarConst {
   float k_hi, k_lo, gre;       // gamma_im as double-float, gamma_re
   float shpT[BGB_MAXQ][3], shpB[BGB_MAXQ][3];     // Lagrange hats at rule points
   double shpT64[BGB_MAXQ][3], shpB64[BGB_MAXQ][3];
+  // Plain FP64 kernel: with tay_n > 0 the phase of a point pair is k R = k R0 + k (R - R0), R0 the
+  // centroid distance, and exp(-i k (R - R0)) comes from the first tay_n <= 6 terms of the series of
+  // sin and cos (|k (R - R0)| <= k (r_test + r_trial), truncation below 2^-55); tay_s[j] =
+  // (-1)^j / (2j + 1)!, tay_c[j] = (-1)^j / (2j)!.  tay_n = 0: sincos at every point pair.
+  int tay_n;
+  double tay_s[BGB_TAYLOR_MAX], tay_c[BGB_TAYLOR_MAX];
 };
 
 // The scalar constants of a far launch, copied into registers per tile.
 struct FarScalars {
-  int qt, qb, lossy, phase_direct;
+  int qt, qb, lossy, phase_direct, tay_n;
   float k_hi, k_lo, gre;
   float alpha32[2], beta32[2];
   double alpha[2], beta[2], gamma[2];
