@@ -563,7 +563,8 @@ int bgb_create(bgb_handle** out, const bgb_config* cfg) {
   int rc = 0;
   if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess ||
       (e = cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking)) != cudaSuccess ||
-      (e = cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking)) != cudaSuccess) {
+      (e = cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaStreamCreateWithFlags(&h->stream_sing, cudaStreamNonBlocking)) != cudaSuccess) {
     rc = cuda_fail(e, "cudaStreamCreate");
   }
   for (int i = 0; i < 8 && !rc; ++i)
@@ -599,10 +600,11 @@ int bgb_destroy(bgb_handle* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
   if (h->stream2) cudaStreamSynchronize(h->stream2);
+  if (h->stream_sing) cudaStreamSynchronize(h->stream_sing);
   DevBuf* bufs[] = {&h->verts_t, &h->tris_t, &h->verts_b, &h->tris_b, &h->geo_t, &h->geo_b, &h->bnd_t, &h->bnd_b, &h->bnd_c,
                     &h->rec_t, &h->rec_b, &h->cls_count, &h->cls_off, &h->ent_tau, &h->ent_sigma, &h->ent_cls, &h->ent_mask, &h->geodf_t, &h->geodf_b,
                     &h->sing_L, &h->err, &h->df_tab, &h->tplan_i, &h->tplan_l, &h->tplan_d, &h->tplan_f,
-                    &h->diag_a, &h->diag_b, &h->diag_c, &h->diag_d};
+                    &h->diag_a, &h->diag_b, &h->diag_c, &h->diag_d, &h->grp_tri, &h->grp_cnt, &h->grp_off, &h->grp_perm};
   for (DevBuf* b : bufs) b->release();
   h->curve.release();
   for (int k = 0; k < bgb_handle::kSlots; ++k) {
@@ -614,12 +616,14 @@ int bgb_destroy(bgb_handle* h) {
     if (h->ev[i]) cudaEventDestroy(h->ev[i]);
   for (int i = 0; i < 4 * bgb_handle::kSlots; ++i)
     if (h->ev2[i]) cudaEventDestroy(h->ev2[i]);
+  for (cudaEvent_t x : h->grp_ev) cudaEventDestroy(x);
   for (int i = 0; i < 2; ++i)
     if (h->ring_ev[i]) cudaEventDestroy(h->ring_ev[i]);
   if (h->ring) cudaFreeHost(h->ring);
   if (h->stream) cudaStreamDestroy(h->stream);
   if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
   if (h->stream2) cudaStreamDestroy(h->stream2);
+  if (h->stream_sing) cudaStreamDestroy(h->stream_sing);
   if (h->abort_host) cudaFreeHost((void*)h->abort_host);
   delete h;
   return 0;
@@ -1032,8 +1036,57 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
   if ((rc = h->sing_L.ensure(sizeof(double2) * 9 * std::max<int64_t>(1, nsing)))) return rc;
   const bool use_df = precision == BGB_PREC_MIXED && df_singular_ok(opp, max_edge(test), same ? max_edge(test) : max_edge(trial));
   std::vector<float> df_host;  // uploaded asynchronously: lives until the end of the call
+  DfTables M{};
+  const GeoDf* dgt = nullptr;
+  const GeoDf* dgb = nullptr;
+  // the singular kernels over all entries (perm null) or over the entries perm[range[0] .. range[1])
+  auto launch_sing = [&](const int* perm, const int64_t* range, cudaStream_t st) {
+    if (use_df) {
+      launch_singular_df(opp.kind, make_opdf(opp), nullptr, nullptr, M, h->df_tab.as<float>(), dgt, dgb,
+                         h->ent_tau.as<int>(), h->ent_sigma.as<int>(), h->ent_cls.as<int8_t>(),
+                         h->ent_mask.as<int16_t>(), nsing, h->sing_L.as<double2>(), h->abort_dev, h->num_sms, st, perm,
+                         range);
+      // near pairs (singularity extraction: logarithms and arctangents) in FP64
+      launch_singular(opp, qsel, R, test->refspace, trial->refspace, gt, gb, h->ent_tau.as<int>(),
+                      h->ent_sigma.as<int>(), h->ent_cls.as<int8_t>(), nsing, h->sing_L.as<double2>(), h->abort_dev,
+                      h->num_sms, st, true, perm, range);
+      return 2;
+    }
+    launch_singular(opp, qsel, R, test->refspace, trial->refspace, gt, gb, h->ent_tau.as<int>(), h->ent_sigma.as<int>(),
+                    h->ent_cls.as<int8_t>(), nsing, h->sing_L.as<double2>(), h->abort_dev, h->num_sms, st, false, perm,
+                    range);
+    return 1;
+  };
+  // A host output in several blocks integrates its singular entries in groups on a stream of their
+  // own: group b holds the entries whose trial triangle first appears in block b, the groups run in
+  // block order from the end of the classification on (while the host still plans the tiles), and
+  // block b's far kernel waits for group b only.  Block 0's far kernel and copy then start after a
+  // fraction of the singular stage instead of all of it.
+  const bool grouped = host_out && nblocks > 1 && nsing > 0;
+  std::vector<int> tri_group;  // uploaded asynchronously: lives until the end of the call
+  if (grouped) {
+    tri_group.assign((size_t)std::max(1, trial->nt), nblocks - 1);
+    for (int t = 0; t < trial->nt; ++t)
+      for (int i = 0; i < 3; ++i) {
+        const int f = trial->fn_index[3 * t + i];
+        if (f < 0) continue;
+        const int g = (int)(std::upper_bound(col_start.begin(), col_start.end(), (int64_t)f) - col_start.begin()) - 1;
+        tri_group[(size_t)t] = std::min(tri_group[(size_t)t], std::max(0, g));
+      }
+    if ((rc = h->grp_tri.ensure(sizeof(int) * tri_group.size())) || (rc = h->grp_cnt.ensure(sizeof(int) * nblocks)) ||
+        (rc = h->grp_off.ensure(sizeof(int64_t) * (nblocks + 1))) || (rc = h->grp_perm.ensure(sizeof(int) * nsing)))
+      return rc;
+    if ((rc = upload(h, h->grp_tri, tri_group, 0))) return rc;
+    launch_group_entries(h->ent_sigma.as<int>(), nsing, h->grp_tri.as<int>(), nblocks, h->grp_cnt.as<int>(),
+                         h->grp_off.as<int64_t>(), h->grp_perm.as<int>(), h->num_sms, h->stream);
+    launches += 3;
+    while ((int)h->grp_ev.size() < nblocks) {
+      cudaEvent_t x = nullptr;
+      BGB_CUDA(cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
+      h->grp_ev.push_back(x);
+    }
+  }
   if (use_df) {
-    DfTables M;
     build_df_tables(qsel, R, df_host, M);
     if ((rc = h->df_tab.ensure(sizeof(float) * df_host.size()))) return rc;
     BGB_CUDA(cudaMemcpyAsync(h->df_tab.p, df_host.data(), sizeof(float) * df_host.size(), cudaMemcpyHostToDevice, h->stream));
@@ -1042,18 +1095,26 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
       return rc;
     launch_prepare_geodf(gt, test->nt, h->geodf_t.as<GeoDf>(), h->stream);
     if (!same) launch_prepare_geodf(gb, trial->nt, h->geodf_b.as<GeoDf>(), h->stream);
-    const GeoDf* dgt = h->geodf_t.as<GeoDf>();
-    const GeoDf* dgb = same ? dgt : h->geodf_b.as<GeoDf>();
-    launch_singular_df(opp.kind, make_opdf(opp), nullptr, nullptr, M, h->df_tab.as<float>(), dgt, dgb,
-                       h->ent_tau.as<int>(), h->ent_sigma.as<int>(), h->ent_cls.as<int8_t>(),
-                       h->ent_mask.as<int16_t>(), nsing, h->sing_L.as<double2>(), h->abort_dev, h->num_sms, h->stream);
-    // near pairs (singularity extraction: logarithms and arctangents) in FP64
-    launch_singular(opp, qsel, R, test->refspace, trial->refspace, gt, gb, h->ent_tau.as<int>(), h->ent_sigma.as<int>(),
-                    h->ent_cls.as<int8_t>(), nsing, h->sing_L.as<double2>(), h->abort_dev, h->num_sms, h->stream, true);
-    launches += 2 + (same ? 0 : 1);
+    dgt = h->geodf_t.as<GeoDf>();
+    dgb = same ? dgt : h->geodf_b.as<GeoDf>();
+    launches += 1 + (same ? 0 : 1);
+  }
+  struct SyncOnExit {  // singular groups still in flight when the call returns early
+    cudaStream_t st;
+    ~SyncOnExit() {
+      if (st) cudaStreamSynchronize(st);
+    }
+  } sync_sing{grouped ? h->stream_sing : nullptr};
+  if (grouped) {
+    BGB_CUDA(cudaEventRecord(h->ev[4], h->stream));
+    BGB_CUDA(cudaStreamWaitEvent(h->stream_sing, h->ev[4], 0));
+    for (int b = 0; b < nblocks; ++b) {
+      launches += launch_sing(h->grp_perm.as<int>(), h->grp_off.as<int64_t>() + b, h->stream_sing);
+      BGB_CUDA(cudaEventRecord(h->grp_ev[(size_t)b], h->stream_sing));
+    }
+    BGB_CUDA(cudaEventRecord(h->ev[5], h->stream_sing));
   } else {
-    launch_singular(opp, qsel, R, test->refspace, trial->refspace, gt, gb, h->ent_tau.as<int>(), h->ent_sigma.as<int>(),
-                    h->ent_cls.as<int8_t>(), nsing, h->sing_L.as<double2>(), h->abort_dev, h->num_sms, h->stream);
+    launches += launch_sing(nullptr, nullptr, h->stream);
   }
   BGB_CUDA(cudaGetLastError());
   cudaEventRecord(h->ev[2], h->stream);
@@ -1222,6 +1283,7 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
                                cudaMemcpyHostToDevice, cst));
     BGB_CUDA(cudaMemsetAsync(dctr, 0, sizeof(int), cst));
     const int ctas = (int)std::min<int64_t>((int64_t)H.items.size(), (int64_t)std::max(1, per_sm) * h->num_sms);
+    if (grouped) BGB_CUDA(cudaStreamWaitEvent(cst, h->grp_ev[(size_t)b], 0));  // singular groups 0 .. b
     BGB_CUDA(cudaEventRecord(h->ev2[slot * 4 + 0], cst));
     if ((rc2 = launch_far_persistent(precision, K.op_kind, gen, dK, dT, (const int4*)h->far_items[slot].p,
                                      (int)H.items.size(), dctr, smem, std::max(1, ctas), h->abort_dev, cst)))
@@ -1288,6 +1350,7 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
   auto drain = [&](int code) {  // the slots' host tables must outlive uploads still in flight
     cudaStreamSynchronize(h->stream);
     cudaStreamSynchronize(h->stream2);
+    cudaStreamSynchronize(h->stream_sing);
     cudaStreamSynchronize(h->copy_stream);
     return code;
   };
@@ -1299,6 +1362,7 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
   }
   BGB_CUDA(cudaStreamSynchronize(h->stream));
   BGB_CUDA(cudaStreamSynchronize(h->stream2));
+  BGB_CUDA(cudaStreamSynchronize(h->stream_sing));
   BGB_CUDA(cudaStreamSynchronize(h->copy_stream));
   for (int k = 0; k < NS; ++k) harvest(k);
   const double ms_pipe = std::chrono::duration<double, std::milli>(clk::now() - t_pipe).count();
@@ -1316,9 +1380,10 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
   st.ms_classify = event_ms(h->ev[0], h->ev[1]);
   if (trace)
     fprintf(stderr, "bgb trace: classify end %.3f, singular end %.3f, pipeline start %.3f (host) ms\n",
-            event_ms(h->ev[0], h->ev[1]), event_ms(h->ev[0], h->ev[2]),
+            event_ms(h->ev[0], h->ev[1]), event_ms(h->ev[0], grouped ? h->ev[5] : h->ev[2]),
             std::chrono::duration<double, std::milli>(t_pipe - t_start).count());
-  st.ms_singular = event_ms(h->ev[1], h->ev[2]);
+  // grouped: the classification-side preparation plus the span of the groups (beside far kernels)
+  st.ms_singular = event_ms(h->ev[1], h->ev[2]) + (grouped ? event_ms(h->ev[4], h->ev[5]) : 0.0);
   st.ms_far = ms_far;
   if (stats) {
     std::vector<int8_t> cls((size_t)nsing);

@@ -71,6 +71,7 @@ struct bgb_handle {
   // buffers
   bgb::DevBuf verts_t, tris_t, verts_b, tris_b, geo_t, geo_b, bnd_t, bnd_b, bnd_c, rec_t, rec_b;
   bgb::DevBuf cls_count, cls_off, ent_tau, ent_sigma, ent_cls, ent_mask, sing_L, err, geodf_t, geodf_b;
+  bgb::DevBuf grp_tri, grp_cnt, grp_off, grp_perm;  // singular entries grouped by output block
   static constexpr int kSlots = 3;  // output-block slots in flight (staging, plan tables, events)
   bgb::DevBuf plan_i[kSlots], plan_l[kSlots], plan_d[kSlots], plan_f[kSlots], far_items[kSlots], far_const[kSlots], df_tab;
   bgb::DevBuf tplan_i, tplan_l, tplan_d, tplan_f;  // test-side tile tables (shared by all output blocks)
@@ -79,6 +80,8 @@ struct bgb_handle {
   bgb::CurveBufs curve;
   cudaEvent_t ev[8] = {};
   cudaEvent_t ev2[4 * kSlots] = {};  // per output-block slot: far start / end, copy start / end
+  cudaStream_t stream_sing = nullptr;  // singular groups of a host output in blocks
+  std::vector<cudaEvent_t> grp_ev;     // end of each singular group (grown on demand)
   cudaEvent_t ring_ev[2] = {};
   void* ring = nullptr;      // pinned host staging ring
   size_t ring_bytes = 0;

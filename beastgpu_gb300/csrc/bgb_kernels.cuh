@@ -18,12 +18,18 @@ void launch_classify(bool fill, const float4* tb, const float4* bb, const Geo64*
                      double k2, int* count, const int64_t* offset, int* out_tau, int* out_sigma, int8_t* out_cls,
                      int* err, int num_sms, cudaStream_t st, int16_t* out_mask = nullptr, const float4* cb = nullptr);
 void launch_scan(const int* counts, int n, int64_t* offsets, cudaStream_t st);
+// Singular entries sorted by group: perm[off[g] .. off[g + 1]) are the entries e with
+// tri_group[sigma[e]] == g (out of range: the last group).  counts: ngroups ints, off: ngroups + 1.
+void launch_group_entries(const int* sigma, int64_t n, const int* tri_group, int ngroups, int* counts, int64_t* off,
+                          int* perm, int num_sms, cudaStream_t st);
 void launch_classify_dense(const Geo64* tg, const Geo64* bg, int t0, int t1, int s0, int s1, double k2, int8_t* out,
                            int* err, cudaStream_t st);
 // near_only: integrate only the near pairs of the list (the mixed path's double-float kernel skips them).
+// perm (device, optional): integrate only the entries perm[range[0] .. range[1]) (range: device int64[2]).
 void launch_singular(const OpParams& op, const QuadSel& qs, const RuleTable& rules, int rsA, int rsB, const Geo64* tg,
                      const Geo64* bg, const int* et, const int* es, const int8_t* ec, int64_t n, double2* out,
-                     const volatile int* abort_flag, int num_sms, cudaStream_t st, bool near_only = false);
+                     const volatile int* abort_flag, int num_sms, cudaStream_t st, bool near_only = false,
+                     const int* perm = nullptr, const int64_t* range = nullptr);
 void launch_local_diag64(const OpParams& op, const QuadSel& qs, const RuleTable& rules, int rsA, int rsB,
                          const Geo64* tg, const Geo64* bg, const int* tau, const int* sigma, int64_t n, int force,
                          double2* out, int8_t* cls, int* err, int num_sms, cudaStream_t st, int16_t* mask = nullptr);
@@ -66,7 +72,8 @@ OpDf make_opdf(const OpParams& op);
 void launch_singular_df(int op_kind, const OpDf& op, const OpDf* opdf_array, const int* tri_problem,
                         const DfTables& M, const float* dtab, const GeoDf* tg, const GeoDf* bg, const int* et,
                         const int* es, const int8_t* ec, const int16_t* emask, int64_t n, double2* out,
-                        const volatile int* abort_flag, int num_sms, cudaStream_t st);
+                        const volatile int* abort_flag, int num_sms, cudaStream_t st, const int* perm = nullptr,
+                        const int64_t* range = nullptr);
 
 // ---- bgb_far.cu ------------------------------------------------------------------------
 // Constants of the far-pair kernels (passed by value).

@@ -228,6 +228,41 @@ __global__ void k_scan_counts(const int* __restrict__ counts, int n, int64_t* __
   if (threadIdx.x == T - 1) offsets[n] = part[T - 1];
 }
 
+// Singular entries in groups: entry e belongs to group tri_group[ent_sigma[e]] (clamped to
+// [0, ngroups)).  Count per group (a shared histogram when the groups fit), scan, then place each
+// entry at the next free position of its group.  The order inside a group depends on the atomics;
+// each entry writes only its own local matrix, so the results do not.
+constexpr int kGroupHist = 2048;
+__device__ __forceinline__ int entry_group(const int* __restrict__ sigma, const int* __restrict__ tri_group, int64_t e,
+                                           int ngroups) {
+  const int g = tri_group[sigma[e]];
+  return (g < 0 || g >= ngroups) ? ngroups - 1 : g;
+}
+__global__ void k_group_count(const int* __restrict__ sigma, int64_t n, const int* __restrict__ tri_group, int ngroups,
+                              int* __restrict__ counts) {
+  __shared__ int hist[kGroupHist];
+  const bool sh = ngroups <= kGroupHist;
+  if (sh)
+    for (int i = threadIdx.x; i < ngroups; i += blockDim.x) hist[i] = 0;
+  __syncthreads();
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    const int g = entry_group(sigma, tri_group, e, ngroups);
+    if (sh) atomicAdd(&hist[g], 1);
+    else atomicAdd(&counts[g], 1);
+  }
+  __syncthreads();
+  if (sh)
+    for (int i = threadIdx.x; i < ngroups; i += blockDim.x)
+      if (hist[i]) atomicAdd(&counts[i], hist[i]);
+}
+__global__ void k_group_fill(const int* __restrict__ sigma, int64_t n, const int* __restrict__ tri_group, int ngroups,
+                             const int64_t* __restrict__ off, int* __restrict__ cursor, int* __restrict__ perm) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    const int g = entry_group(sigma, tri_group, e, ngroups);
+    perm[off[g] + atomicAdd(&cursor[g], 1)] = (int)e;
+  }
+}
+
 __global__ void k_classify_dense(const Geo64* __restrict__ tg, const Geo64* __restrict__ bg, int t0, int t1,
                                  int s0, int s1, double k2, int8_t* __restrict__ out, int* __restrict__ err) {
   int64_t ns = s1 - s0;
@@ -781,10 +816,14 @@ __global__ void __launch_bounds__(256) k_singular(OpParams op1, const OpParams* 
                                                   const int* __restrict__ ent_tau, const int* __restrict__ ent_sigma,
                                                   const int8_t* __restrict__ ent_cls, int64_t n,
                                                   double2* __restrict__ out, const volatile int* abort_flag,
-                                                  int near_only) {
+                                                  int near_only, const int* __restrict__ perm,
+                                                  const int64_t* __restrict__ range) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  // perm: the entries perm[range[0] .. range[1]) (one output block's group); otherwise 0 .. n
+  const int64_t i0 = perm ? range[0] : 0, i1 = perm ? range[1] : n;
+  auto ent_at = [&](int64_t i) -> int64_t { return perm ? (int64_t)perm[i] : i; };
   auto entry = [&](int64_t e) {
     const int tau = ent_tau[e];
     const OpParams op = BATCH ? ops[tri_problem[tau]] : op1;
@@ -802,21 +841,21 @@ __global__ void __launch_bounds__(256) k_singular(OpParams op1, const OpParams* 
   if (near_only) {
     // near pairs only (the others come from the double-float kernel): a warp reads the classes of
     // 32 entries at once and integrates the near ones among them
-    for (int64_t e0 = warp0 * 32; e0 < n; e0 += warps * 32) {
+    for (int64_t b = i0 + warp0 * 32; b < i1; b += warps * 32) {
       if (abort_flag && *abort_flag) return;
-      const int64_t e = e0 + lane;
-      unsigned near = __ballot_sync(0xffffffffu, e < n && ent_cls[e] == BGB_CLASS_NEAR);
+      const int64_t i = b + lane;
+      unsigned near = __ballot_sync(0xffffffffu, i < i1 && ent_cls[ent_at(i)] == BGB_CLASS_NEAR);
       while (near) {
         const int l = __ffs(near) - 1;
         near &= near - 1;
-        entry(e0 + l);
+        entry(ent_at(b + l));
       }
     }
     return;
   }
-  for (int64_t e = warp0; e < n; e += warps) {
+  for (int64_t i = i0 + warp0; i < i1; i += warps) {
     if (abort_flag && *abort_flag) return;
-    entry(e);
+    entry(ent_at(i));
   }
 }
 
@@ -932,6 +971,16 @@ void launch_classify(bool fill, const float4* tb, const float4* bb, const Geo64*
 void launch_scan(const int* counts, int n, int64_t* offsets, cudaStream_t st) {
   k_scan_counts<<<1, 1024, 0, st>>>(counts, n, offsets);
 }
+void launch_group_entries(const int* sigma, int64_t n, const int* tri_group, int ngroups, int* counts, int64_t* off,
+                          int* perm, int num_sms, cudaStream_t st) {
+  cudaMemsetAsync(counts, 0, sizeof(int) * (size_t)ngroups, st);
+  int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)num_sms * 4);
+  if (blocks < 1) blocks = 1;
+  if (n > 0) k_group_count<<<blocks, 256, 0, st>>>(sigma, n, tri_group, ngroups, counts);
+  k_scan_counts<<<1, 1024, 0, st>>>(counts, ngroups, off);
+  cudaMemsetAsync(counts, 0, sizeof(int) * (size_t)ngroups, st);
+  if (n > 0) k_group_fill<<<blocks, 256, 0, st>>>(sigma, n, tri_group, ngroups, off, counts, perm);
+}
 void launch_classify_dense(const Geo64* tg, const Geo64* bg, int t0, int t1, int s0, int s1, double k2, int8_t* out,
                            int* err, cudaStream_t st) {
   int64_t total = (int64_t)(t1 - t0) * (s1 - s0);
@@ -942,15 +991,17 @@ void launch_classify_dense(const Geo64* tg, const Geo64* bg, int t0, int t1, int
 }
 void launch_singular(const OpParams& op, const QuadSel& qs, const RuleTable& rules, int rsA, int rsB, const Geo64* tg,
                      const Geo64* bg, const int* et, const int* es, const int8_t* ec, int64_t n, double2* out,
-                     const volatile int* abort_flag, int num_sms, cudaStream_t st, bool near_only) {
+                     const volatile int* abort_flag, int num_sms, cudaStream_t st, bool near_only, const int* perm,
+                     const int64_t* range) {
   (void)rsA;
   (void)rsB;
   if (n <= 0) return;
   int64_t blocks = (n + 7) / 8;
-  if (blocks > (int64_t)num_sms * 32) blocks = (int64_t)num_sms * 32;
+  const int64_t cap = (int64_t)num_sms * (perm ? 2 : 32);  // a group: about one wave beside a far kernel
+  if (blocks > cap) blocks = cap;
 #define BGB_LAUNCH_SING(OPK)                                                                                   \
   k_singular<OPK, false><<<(int)blocks, 256, 0, st>>>(op, nullptr, nullptr, qs, rules, tg, bg, et, es, ec, n, out, \
-                                                      abort_flag, near_only ? 1 : 0)
+                                                      abort_flag, near_only ? 1 : 0, perm, range)
   switch (op.kind) {
     case BGB_OP_HELMHOLTZ3D_SL: BGB_LAUNCH_SING(BGB_OP_HELMHOLTZ3D_SL); break;
     case BGB_OP_MAXWELL3D_SL: BGB_LAUNCH_SING(BGB_OP_MAXWELL3D_SL); break;
@@ -1006,7 +1057,7 @@ void launch_singular_batched(int op_kind, const OpParams* ops, const QuadSel& qs
   if (blocks > (int64_t)num_sms * 32) blocks = (int64_t)num_sms * 32;
 #define BGB_LAUNCH_SING(OPK)                                                                                  \
   k_singular<OPK, true><<<(int)blocks, 256, 0, st>>>(OpParams{}, ops, tri_problem, qs, rules, tg, bg, et, es, ec, n, \
-                                                     out, abort_flag, near_only ? 1 : 0)
+                                                     out, abort_flag, near_only ? 1 : 0, nullptr, nullptr)
   switch (op_kind) {
     case BGB_OP_HELMHOLTZ3D_SL: BGB_LAUNCH_SING(BGB_OP_HELMHOLTZ3D_SL); break;
     case BGB_OP_MAXWELL3D_SL: BGB_LAUNCH_SING(BGB_OP_MAXWELL3D_SL); break;

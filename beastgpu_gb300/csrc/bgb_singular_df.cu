@@ -175,15 +175,19 @@ __global__ void __launch_bounds__(256) k_singular_df(OpDf op1, const OpDf* __res
                                                      const GeoDf* __restrict__ bg, const int* __restrict__ ent_tau,
                                                      const int* __restrict__ ent_sigma, const int8_t* __restrict__ ent_cls,
                                                      const int16_t* __restrict__ ent_mask, int64_t n,
-                                                     double2* __restrict__ out, const volatile int* abort_flag) {
+                                                     double2* __restrict__ out, const volatile int* abort_flag,
+                                                     const int* __restrict__ perm, const int64_t* __restrict__ range) {
   __shared__ float4 trig[128];
   for (int i = threadIdx.x; i < 128; i += blockDim.x) trig[i] = ((const float4*)(tab + M.trig_off))[i];
   __syncthreads();
   constexpr int NA = DfAcc<OP>::N;
   const int lane = threadIdx.x & 31;
   const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < n; e += warps) {
+  // perm: the entries perm[range[0] .. range[1]) (one output block's group); otherwise 0 .. n
+  const int64_t i0 = perm ? range[0] : 0, i1 = perm ? range[1] : n;
+  for (int64_t i = i0 + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); i < i1; i += warps) {
     if (abort_flag && *abort_flag) return;
+    const int64_t e = perm ? (int64_t)perm[i] : i;
     const int cls = ent_cls[e];
     if (cls == BGB_CLASS_NEAR) continue;  // near pairs stay FP64 (k_singular with near_only)
     const int tau = ent_tau[e];
@@ -420,18 +424,20 @@ OpDf make_opdf(const OpParams& op) {
 void launch_singular_df(int op_kind, const OpDf& op, const OpDf* opdf_array, const int* tri_problem,
                         const DfTables& M, const float* dtab, const GeoDf* tg, const GeoDf* bg, const int* et,
                         const int* es, const int8_t* ec, const int16_t* emask, int64_t n, double2* out,
-                        const volatile int* abort_flag, int num_sms, cudaStream_t st) {
+                        const volatile int* abort_flag, int num_sms, cudaStream_t st, const int* perm,
+                        const int64_t* range) {
   if (n <= 0) return;
   int64_t blocks = (n + 7) / 8;
-  if (blocks > (int64_t)num_sms * 32) blocks = (int64_t)num_sms * 32;
+  const int64_t cap = (int64_t)num_sms * (perm ? 2 : 32);  // a group: about one wave beside a far kernel
+  if (blocks > cap) blocks = cap;
   const bool batch = opdf_array != nullptr;
 #define BGB_LAUNCH_DF(OPK)                                                                                        \
   if (batch)                                                                                                      \
     k_singular_df<OPK, true><<<(int)blocks, 256, 0, st>>>(op, opdf_array, tri_problem, M, dtab, tg, bg, et, es, ec, \
-                                                          emask, n, out, abort_flag);                             \
+                                                          emask, n, out, abort_flag, perm, range);               \
   else                                                                                                            \
     k_singular_df<OPK, false><<<(int)blocks, 256, 0, st>>>(op, opdf_array, tri_problem, M, dtab, tg, bg, et, es, ec, \
-                                                           emask, n, out, abort_flag);
+                                                           emask, n, out, abort_flag, perm, range);
   if (op_kind == BGB_OP_HELMHOLTZ3D_SL) {
     BGB_LAUNCH_DF(BGB_OP_HELMHOLTZ3D_SL)
   } else if (op_kind == BGB_OP_MAXWELL3D_SL) {

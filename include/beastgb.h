@@ -116,7 +116,9 @@ typedef struct {
   int64_t pairs_total;          /* nt_test * nt_trial over the assembled rows */
   int64_t pairs_class[5];       /* far, CV, CE, CF, near */
   int64_t pairs_computed;       /* triangle pairs evaluated by the far kernel (incl. halo) */
-  double ms_classify, ms_singular; /* device time of the classification / singular stages */
+  double ms_classify, ms_singular; /* device time of the classification / singular stages (a host
+                                      output in several blocks integrates its singular entries in
+                                      groups beside the far kernels: ms_singular spans them) */
   double ms_far;                /* device time of the far kernels (sum over output blocks; blocks on
                                    the two compute streams may overlap) */
   double ms_copy;               /* device-to-host copy time (sum over output blocks) */

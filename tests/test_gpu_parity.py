@@ -370,6 +370,12 @@ def test_distinct_test_and_trial_spaces(name):
         assert rel(zmx.astype(np.complex128), ref) < MIXED_TOL
         part = bg.assemble_gpu(op, X, Y, bg.GPUConfiguration(precision="fp64"), rows=(3, X.nfun - 5))
         np.testing.assert_array_equal(part, z64[3:X.nfun - 2])
+        # a host output in column blocks of 7: the singular entries in groups by the trial side's blocks
+        for prec, esz, want in (("fp64", 16, z64), ("mixed", 8, zmx)):
+            Zb, st = bg.assemble_gpu(op, X, Y, bg.GPUConfiguration(precision=prec, total_GPU_budget=4 * 7 * X.nfun * esz),
+                                     return_stats=True)
+            assert st["out_blocks"] >= Y.nfun // 7
+            np.testing.assert_array_equal(Zb, want)
 
 
 def _nonfar_pairs(X, k2, rows_per_block=2048):
