@@ -94,7 +94,7 @@ int far_target_ctas_per_sm(int precision) {
 
 int rec_stride(int precision, int q, int generic) {
   const int Q = generic ? BGB_MAXQ : q;
-  return precision == BGB_PREC_MIXED ? 17 + 4 * Q : 13 + 4 * Q;
+  return precision == BGB_PREC_MIXED ? farimpl::off32_size(Q) : 13 + 4 * Q;
 }
 
 size_t far_smem_bytes(int precision, int qt, int qb, const TilePlan& p) {

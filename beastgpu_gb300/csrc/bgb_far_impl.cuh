@@ -63,10 +63,16 @@ __device__ __forceinline__ void tri_curls(const T* vo, T inv2a, T c[3][3]) {
     for (int k = 0; k < 3; ++k) c[i][k] = (vo[3 * ((i + 1) % 3) + k] - vo[3 * ((i + 2) % 3) + k]) * inv2a;
 }
 
+// FP32 record of a triangle, in 16-byte groups read with 128-bit shared-memory loads:
+// [CH.xyz CL.x] [CL.yz - -] [x y z w] per quadrature point [VO (9) INV2A - -]; the stride is an odd
+// number of groups, so the records of different triangles start in different bank groups.
 template <int Q>
 struct Off32 {
-  static constexpr int CH = 0, CL = 3, RAD = 6, INV2A = 7, X = 8, W = 8 + 3 * Q, VO = 8 + 4 * Q, SIZE = 17 + 4 * Q;
+  static constexpr int CH = 0, CL = 3, X = 8, PS = 4, VO = 8 + 4 * Q, INV2A = VO + 9, SIZE = 4 * ((5 + Q) | 1);
+  static constexpr int px(int I) { return X + PS * I; }      // point I: x, y, z
+  static constexpr int pw(int I) { return X + PS * I + 3; }  // point I: weight
 };
+__host__ __device__ constexpr int off32_size(int Q) { return 4 * ((5 + Q) | 1); }
 template <int Q>
 struct Off64 {
   static constexpr int C = 0, X = 3, W = 3 + 3 * Q, VO = 3 + 4 * Q, INV2A = 12 + 4 * Q, SIZE = 13 + 4 * Q;
@@ -92,19 +98,34 @@ struct PFp64 {
 // ----------------------------------------------------------------------------------------
 // Mixed FP32 far pair
 // ----------------------------------------------------------------------------------------
+// the 9 vertex offsets of an FP32 record (three 16-byte groups)
+__device__ __forceinline__ void load_vo(const float4* __restrict__ g, float V[3][3]) {
+  const float4 v0 = g[0], v1 = g[1], v2 = g[2];
+  V[0][0] = v0.x; V[0][1] = v0.y; V[0][2] = v0.z;
+  V[1][0] = v0.w; V[1][1] = v1.x; V[1][2] = v1.y;
+  V[2][0] = v1.z; V[2][1] = v1.w; V[2][2] = v2.x;
+}
+
 template <int OP, int QT, int QB>
 __device__ __forceinline__ void far_pair_mixed(const FarScalars& K, const float (*__restrict__ shpT)[3],
                                                const float (*__restrict__ shpB)[3], const float* __restrict__ a,
                                                const float* __restrict__ b, float2 L[9]) {
   using OA = Off32<QT>;
   using OB = Off32<QB>;
+  const float4* __restrict__ a4 = reinterpret_cast<const float4*>(a);
+  const float4* __restrict__ b4 = reinterpret_cast<const float4*>(b);
   float Dh[3], Dl[3];
+  {
+    const float4 a0 = a4[0], a1 = a4[1], b0 = b4[0], b1 = b4[1];
+    const float ach[3] = {a0.x, a0.y, a0.z}, acl[3] = {a0.w, a1.x, a1.y};
+    const float bch[3] = {b0.x, b0.y, b0.z}, bcl[3] = {b0.w, b1.x, b1.y};
 #pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    float s, e;
-    two_sum(a[OA::CH + c], -b[OB::CH + c], s, e);
-    e = __fadd_rn(e, __fsub_rn(a[OA::CL + c], b[OB::CL + c]));
-    fast_two_sum(s, e, Dh[c], Dl[c]);
+    for (int c = 0; c < 3; ++c) {
+      float s, e;
+      two_sum(ach[c], -bch[c], s, e);
+      e = __fadd_rn(e, __fsub_rn(acl[c], bcl[c]));
+      fast_two_sum(s, e, Dh[c], Dl[c]);
+    }
   }
   const float n2 = fmaf(Dh[0], Dh[0], fmaf(Dh[1], Dh[1], Dh[2] * Dh[2]));
   const float R0 = n2 * rsqrtf(n2);
@@ -152,23 +173,23 @@ __device__ __forceinline__ void far_pair_mixed(const FarScalars& K, const float 
     // (per test point, per trial point, per point pair): 5 operations per point pair.
     // trial points of the pair in registers when the rule is small (shared-memory loads otherwise)
     constexpr int QY = QB <= 4 ? QB : 1;
-    float Y[QY][3], MJ[QY];
+    float MJ[QY];
     if constexpr (QB <= 4) {
 #pragma unroll
       for (int J = 0; J < QB; ++J) {
         if (J >= qb) break;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) Y[J][c] = b[OB::X + 3 * J + c];
-        MJ[J] = fmaf(Y[J][0], Y[J][0] - D2x, fmaf(Y[J][1], Y[J][1] - D2y, Y[J][2] * (Y[J][2] - D2z)));
+        const float4 y = b4[OB::px(J) / 4];
+        MJ[J] = fmaf(y.x, y.x - D2x, fmaf(y.y, y.y - D2y, y.z * (y.z - D2z)));
       }
     }
 #pragma unroll
     for (int I = 0; I < QT; ++I) {
       if (I >= qt) break;
-      const float Xx = a[OA::X + 3 * I], Xy = a[OA::X + 3 * I + 1], Xz = a[OA::X + 3 * I + 2];
+      const float4 XI = a4[OA::px(I) / 4];
+      const float Xx = XI.x, Xy = XI.y, Xz = XI.z;
       const float ax = Dl[0] + Xx, ay = Dl[1] + Xy, az = Dl[2] + Xz;
       const float KI = fmaf(ax, ax + D2x, fmaf(ay, ay + D2y, fmaf(az, az + D2z, c0)));
-      const float wI = a[OA::W + I];
+      const float wI = XI.w;
       // double layer: (x - y) . n_y = (D + X_I) . n_y, constant over the trial points
       const float cI = OP == BGB_OP_HELMHOLTZ3D_DL
                            ? fmaf(Dh[0] + ax, nB[0], fmaf(Dh[1] + ay, nB[1], (Dh[2] + az) * nB[2]))
@@ -180,13 +201,11 @@ __device__ __forceinline__ void far_pair_mixed(const FarScalars& K, const float 
 #pragma unroll
       for (int J = 0; J < QB; ++J) {
         if (J >= qb) break;
-        float yx, yy, yz, mj;
-        if constexpr (QB <= 4) {
-          yx = Y[J][0], yy = Y[J][1], yz = Y[J][2], mj = MJ[J];
-        } else {
-          yx = b[OB::X + 3 * J], yy = b[OB::X + 3 * J + 1], yz = b[OB::X + 3 * J + 2];
-          mj = fmaf(yx, yx - D2x, fmaf(yy, yy - D2y, yz * (yz - D2z)));
-        }
+        const float4 YJ = b4[OB::px(J) / 4];
+        const float yx = YJ.x, yy = YJ.y, yz = YJ.z;
+        float mj;
+        if constexpr (QB <= 4) mj = MJ[J];
+        else mj = fmaf(yx, yx - D2x, fmaf(yy, yy - D2y, yz * (yz - D2z)));
         const float dot = fmaf(ax, yx, fmaf(ay, yy, az * yz));
         const float q = fmaf(-2.f, dot, KI + mj);
         const float R2 = R0sq + q;
@@ -200,7 +219,7 @@ __device__ __forceinline__ void far_pair_mixed(const FarScalars& K, const float 
         }
         float sn, cs;
         __sincosf(psi, &sn, &cs);
-        float amp = (wI * b[OB::W + J]) * rs;
+        float amp = (wI * YJ.w) * rs;
         if (K.lossy) amp *= amp0 * __expf(-K.gre * delta);
         const float gr = amp * cs, gi = -amp * sn;
         if (kHH) {
@@ -256,9 +275,10 @@ __device__ __forceinline__ void far_pair_mixed(const FarScalars& K, const float 
 #pragma unroll
   for (int I = 0; I < QT; ++I) {
     if (I >= qt) break;
-    const float Xx = a[OA::X + 3 * I], Xy = a[OA::X + 3 * I + 1], Xz = a[OA::X + 3 * I + 2];
+    const float4 XI = a4[OA::px(I) / 4];
+    const float Xx = XI.x, Xy = XI.y, Xz = XI.z;
     const float ax = Dl[0] + Xx, ay = Dl[1] + Xy, az = Dl[2] + Xz;
-    const float wI = a[OA::W + I];
+    const float wI = XI.w;
     float2 TI = make_float2(0.f, 0.f);
     float2 UI[3], EI[3], BI[3];
 #pragma unroll
@@ -269,7 +289,8 @@ __device__ __forceinline__ void far_pair_mixed(const FarScalars& K, const float 
 #pragma unroll
     for (int J = 0; J < QB; ++J) {
       if (J >= qb) break;
-      const float Yx = b[OB::X + 3 * J], Yy = b[OB::X + 3 * J + 1], Yz = b[OB::X + 3 * J + 2];
+      const float4 YJ = b4[OB::px(J) / 4];
+      const float Yx = YJ.x, Yy = YJ.y, Yz = YJ.z;
       const float sx = ax - Yx, sy = ay - Yy, sz = az - Yz;
       const float q = fmaf(sx, D2x + sx, fmaf(sy, D2y + sy, fmaf(sz, D2z + sz, c0)));
       const float R2 = R0sq + q;
@@ -282,7 +303,7 @@ __device__ __forceinline__ void far_pair_mixed(const FarScalars& K, const float 
       psi = fmaf(-nn, kPiB, psi);
       float sn, cs;
       __sincosf(psi, &sn, &cs);
-      float amp = wI * b[OB::W + J] * rs;
+      float amp = wI * YJ.w * rs;
       if (K.lossy) amp *= amp0 * __expf(-K.gre * delta);
       const float gr = amp * cs, gi = -amp * sn;
       if (OP == BGB_OP_HELMHOLTZ3D_SL) {
@@ -384,14 +405,11 @@ __device__ __forceinline__ void far_pair_mixed(const FarScalars& K, const float 
     const float2 cb = make_float2(K.beta32[0] * invAA, K.beta32[1] * invAA);
     const float2 tb = cmulf(cb, P0);
     float V[3][3], W[3][3];
+    load_vo(a4 + OA::VO / 4, V);
+    load_vo(b4 + OB::VO / 4, W);
     float2 Ai[3], Bj[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        V[i][c] = a[OA::VO + 3 * i + c];
-        W[i][c] = b[OB::VO + 3 * i + c];
-      }
       Ai[i].x = S.x - fmaf(V[i][0], Py[0].x, fmaf(V[i][1], Py[1].x, V[i][2] * Py[2].x));
       Ai[i].y = S.y - fmaf(V[i][0], Py[0].y, fmaf(V[i][1], Py[1].y, V[i][2] * Py[2].y));
       Bj[i].x = fmaf(W[i][0], Px[0].x, fmaf(W[i][1], Px[1].x, W[i][2] * Px[2].x));
@@ -793,13 +811,27 @@ __device__ __forceinline__ void tile_body(const FarConst& K, const TilePlan& p, 
     s.triB[i] = t;
     s.bndB[i] = p.bnd_b[t];
   }
-  for (int i = tid; i < tm * RT; i += kThreads) {
-    const int r = i / RT, c = i - r * RT;
-    s.recT[i] = gRT[(int64_t)p.tb_tris[t0 + r] * RT + c];
-  }
-  for (int i = tid; i < nbk * RB; i += kThreads) {
-    const int r = i / RB, c = i - r * RB;
-    s.recB[i] = gRB[(int64_t)p.bb_tris[b0 + r] * RB + c];
+  if constexpr (sizeof(R) == 4) {  // FP32 records: whole 16-byte groups
+    constexpr int RT4 = RT / 4, RB4 = RB / 4;
+    const float4* __restrict__ gT4 = reinterpret_cast<const float4*>(gRT);
+    const float4* __restrict__ gB4 = reinterpret_cast<const float4*>(gRB);
+    for (int i = tid; i < tm * RT4; i += kThreads) {
+      const int r = i / RT4, c = i - r * RT4;
+      reinterpret_cast<float4*>(s.recT)[i] = gT4[(int64_t)p.tb_tris[t0 + r] * RT4 + c];
+    }
+    for (int i = tid; i < nbk * RB4; i += kThreads) {
+      const int r = i / RB4, c = i - r * RB4;
+      reinterpret_cast<float4*>(s.recB)[i] = gB4[(int64_t)p.bb_tris[b0 + r] * RB4 + c];
+    }
+  } else {
+    for (int i = tid; i < tm * RT; i += kThreads) {
+      const int r = i / RT, c = i - r * RT;
+      s.recT[i] = gRT[(int64_t)p.tb_tris[t0 + r] * RT + c];
+    }
+    for (int i = tid; i < nbk * RB; i += kThreads) {
+      const int r = i / RB, c = i - r * RB;
+      s.recB[i] = gRB[(int64_t)p.bb_tris[b0 + r] * RB + c];
+    }
   }
   const bool f32 = sizeof(R) == 4;
   for (int m = tid; m < fm; m += kThreads) {
@@ -984,12 +1016,12 @@ __global__ void k_prepare_rec32(const Geo64* __restrict__ g, int nt, const __gri
   double c[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) c[k] = (T.v[0][k] + T.v[1][k] + T.v[2][k]) / 3.0;
+  for (int k = 0; k < O::SIZE; ++k) r[k] = 0.f;  // spare slots
   for (int k = 0; k < 3; ++k) {
     const float hi = (float)c[k];
     r[O::CH + k] = hi;
     r[O::CL + k] = (float)(c[k] - (double)hi);
   }
-  r[O::RAD] = 0.f;
   r[O::INV2A] = (float)(1.0 / (2.0 * T.area));
   const int q = rules.npoints[rule];
   for (int I = 0; I < Q; ++I) {
@@ -1001,9 +1033,9 @@ __global__ void k_prepare_rec32(const Geo64* __restrict__ g, int nt, const __gri
     }
     for (int k = 0; k < 3; ++k) {
       const double x = (T.v[2][k] + T.t[0][k] * u) + T.t[1][k] * v;
-      r[O::X + 3 * I + k] = (float)(x - c[k]);
+      r[O::px(I) + k] = (float)(x - c[k]);
     }
-    r[O::W + I] = (float)((w / 2.0) * (2.0 * T.area) * wscale);
+    r[O::pw(I)] = (float)((w / 2.0) * (2.0 * T.area) * wscale);
   }
   for (int i = 0; i < 3; ++i)
     for (int k = 0; k < 3; ++k) r[O::VO + 3 * i + k] = (float)(T.v[i][k] - c[k]);
