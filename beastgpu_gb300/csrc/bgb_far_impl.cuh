@@ -39,6 +39,30 @@ constexpr float kPiC = (float)(kTwoPi - 6.28125 - (double)(float)(kTwoPi - 6.281
 constexpr float kInv2Pi = (float)(1.0 / kTwoPi);
 constexpr int kThreads = 256;
 
+// Hardware approximations (PTX .approx with flush-to-zero).  Their arguments in the FP32 pair loop
+// are normal numbers (squared distances, sums of distances, phases within a few pi), so the
+// denormal handling that the non-flushing forms add to each call is dead weight there.
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float rcp_ftz(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ void sincos_ftz(float x, float* s, float* c) {
+  asm("sin.approx.ftz.f32 %0, %1;" : "=f"(*s) : "f"(x));
+  asm("cos.approx.ftz.f32 %0, %1;" : "=f"(*c) : "f"(x));
+}
+// e^x = 2^(x log2 e)
+__device__ __forceinline__ float exp_ftz(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x * 1.4426950408889634f));
+  return y;
+}
+
 // Operators on Lagrange hats: Helmholtz single layer, double layer, transposed double layer,
 // hypersingular.  They share the hat accumulation of the single layer.
 __host__ __device__ constexpr bool is_lagrange_op(int op) {
@@ -128,7 +152,7 @@ __device__ __forceinline__ void far_pair_mixed(const FarScalars& K, const float 
     }
   }
   const float n2 = fmaf(Dh[0], Dh[0], fmaf(Dh[1], Dh[1], Dh[2] * Dh[2]));
-  const float R0 = n2 * rsqrtf(n2);
+  const float R0 = n2 * rsqrt_ftz(n2);
   // c0 = |D_hi|^2 - R0^2, exact to double-float accuracy
   float p0, e0, p1, e1, p2, e2, s1, f1, s2, f2, r2h, r2l;
   two_prod(Dh[0], Dh[0], p0, e0);
@@ -151,7 +175,7 @@ __device__ __forceinline__ void far_pair_mixed(const FarScalars& K, const float 
   const float R0sq = R0 * R0;
   const float D2x = 2.f * Dh[0], D2y = 2.f * Dh[1], D2z = 2.f * Dh[2];
   const float kh = K.k_hi;
-  const float amp0 = K.lossy ? __expf(-K.gre * R0) : 1.f;
+  const float amp0 = K.lossy ? exp_ftz(-K.gre * R0) : 1.f;
   constexpr bool kHH = is_lagrange_op(OP);
   float nA[3] = {0.f, 0.f, 0.f}, nB[3] = {0.f, 0.f, 0.f};
   if (OP == BGB_OP_HELMHOLTZ3D_DLT || OP == BGB_OP_HELMHOLTZ3D_HS) tri_normal(a + OA::VO, a[OA::INV2A], nA);
@@ -209,8 +233,8 @@ __device__ __forceinline__ void far_pair_mixed(const FarScalars& K, const float 
         const float dot = fmaf(ax, yx, fmaf(ay, yy, az * yz));
         const float q = fmaf(-2.f, dot, KI + mj);
         const float R2 = R0sq + q;
-        const float rs = rsqrtf(R2);
-        const float delta = __fdividef(q, fmaf(R2, rs, R0));
+        const float rs = rsqrt_ftz(R2);
+        const float delta = q * rcp_ftz(fmaf(R2, rs, R0));
         float psi = fmaf(kh, delta, phi0);
         if (!K.phase_direct) {  // |psi| may exceed 2 pi: reduce again
           const float nn = rintf(psi * kInv2Pi);
@@ -218,9 +242,9 @@ __device__ __forceinline__ void far_pair_mixed(const FarScalars& K, const float 
           psi = fmaf(-nn, kPiB, psi);
         }
         float sn, cs;
-        __sincosf(psi, &sn, &cs);
+        sincos_ftz(psi, &sn, &cs);
         float amp = (wI * YJ.w) * rs;
-        if (K.lossy) amp *= amp0 * __expf(-K.gre * delta);
+        if (K.lossy) amp *= amp0 * exp_ftz(-K.gre * delta);
         const float gr = amp * cs, gi = -amp * sn;
         if (kHH) {
           float hr = gr, hi = gi;
@@ -294,17 +318,17 @@ __device__ __forceinline__ void far_pair_mixed(const FarScalars& K, const float 
       const float sx = ax - Yx, sy = ay - Yy, sz = az - Yz;
       const float q = fmaf(sx, D2x + sx, fmaf(sy, D2y + sy, fmaf(sz, D2z + sz, c0)));
       const float R2 = R0sq + q;
-      const float rs = rsqrtf(R2);
+      const float rs = rsqrt_ftz(R2);
       const float Rr = R2 * rs;
-      const float delta = __fdividef(q, Rr + R0);
+      const float delta = q * rcp_ftz(Rr + R0);
       float psi = fmaf(kh, delta, phi0);
       const float nn = rintf(psi * kInv2Pi);
       psi = fmaf(-nn, kPiA, psi);
       psi = fmaf(-nn, kPiB, psi);
       float sn, cs;
-      __sincosf(psi, &sn, &cs);
+      sincos_ftz(psi, &sn, &cs);
       float amp = wI * YJ.w * rs;
-      if (K.lossy) amp *= amp0 * __expf(-K.gre * delta);
+      if (K.lossy) amp *= amp0 * exp_ftz(-K.gre * delta);
       const float gr = amp * cs, gi = -amp * sn;
       if (OP == BGB_OP_HELMHOLTZ3D_SL) {
 #pragma unroll
