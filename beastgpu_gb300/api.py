@@ -179,6 +179,34 @@ def _precision(p):
     return {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED}[p]
 
 
+def _out_ptr(buf, dtype, nelem: int, on_device: bool, device: int) -> int:
+    """Address of a caller-provided output buffer, after the checks that keep every write of the
+    library inside it: the element type of the output, contiguous storage of at least `nelem`
+    elements, and host memory for a host output / a tensor on `device` for a device output."""
+    if hasattr(buf, "data_ptr"):  # torch tensor
+        import torch
+        want = torch.complex128 if dtype == np.complex128 else torch.complex64
+        if buf.dtype != want:
+            raise ValueError(f"out_buffer has dtype {buf.dtype}; this output is {want}")
+        if not buf.is_contiguous():
+            raise ValueError("out_buffer must be contiguous")
+        if buf.is_cuda != on_device or (on_device and buf.device.index != device):
+            raise ValueError(f"out_buffer is on {buf.device}; this output goes to "
+                             f"{'cuda:%d' % device if on_device else 'host memory'}")
+        n, ptr = buf.numel(), buf.data_ptr()
+    else:
+        if on_device:
+            raise ValueError("a device output needs a torch CUDA tensor as out_buffer")
+        if not isinstance(buf, np.ndarray) or buf.dtype != dtype:
+            raise ValueError(f"out_buffer must be a numpy array of {np.dtype(dtype)}")
+        if not (buf.flags.f_contiguous or buf.flags.c_contiguous) or not buf.flags.writeable:
+            raise ValueError("out_buffer must be contiguous and writeable")
+        n, ptr = buf.size, buf.ctypes.data
+    if n < nelem:
+        raise ValueError(f"out_buffer holds {n} elements; the output needs {nelem}")
+    return ptr
+
+
 def assemble_gpu(operator: Operator, test_functions: Space, trial_functions: Space, config: GPUConfiguration = None,
                  writeBackStrategy: GpuWriteBack = None, *, storage_policy=None, threading=None,
                  quadstrat: QuadStrat = None, out: str = "host", dtype=None, rows=None, out_buffer=None, stream=None,
@@ -213,6 +241,10 @@ def assemble_gpu(operator: Operator, test_functions: Space, trial_functions: Spa
     c64 = dtype == np.complex128
     row0, nrows = (0, test_functions.nfun) if rows is None else (int(rows[0]), int(rows[1]))
     ncols = trial_functions.nfun
+    if out not in ("host", "device"):
+        raise ValueError("out must be 'host' or 'device'")
+    buf_ptr = None if out_buffer is None else _out_ptr(out_buffer, dtype, max(1, nrows) * ncols, out == "device",
+                                                           config.device)
     h = get_handle(config.device, config.total_GPU_budget, config.tile_config, config.pinned_ring_bytes,
                    _lib.CFG_PAGEABLE_VIA_RING if config.pageable_via_ring else 0)
     keep = _Keep()
@@ -225,8 +257,7 @@ def assemble_gpu(operator: Operator, test_functions: Space, trial_functions: Spa
             Z = np.empty((nrows, ncols), dtype=dtype, order="F")
             ptr = Z.ctypes.data
         else:
-            Z = out_buffer
-            ptr = Z.data_ptr() if hasattr(Z, "data_ptr") else Z.ctypes.data
+            Z, ptr = out_buffer, buf_ptr
         kind = _lib.OUT_HOST_C64 if c64 else _lib.OUT_HOST_C32
         _lib.check(lib.bgb_assemble(h.ptr, C.byref(cop), C.byref(ct), C.byref(cb), C.byref(cq), prec, C.c_void_p(ptr),
                                     kind, max(1, nrows), row0, nrows, None, C.byref(stats)))
@@ -285,6 +316,10 @@ def _assemble_curve(operator, X, Y, config, quadstrat, out, dtype, rows, out_buf
     c64 = dtype == np.complex128
     row0, nrows = (0, X.nfun) if rows is None else (int(rows[0]), int(rows[1]))
     ncols = Y.nfun
+    if out not in ("host", "device"):
+        raise ValueError("out must be 'host' or 'device'")
+    buf_ptr = None if out_buffer is None else _out_ptr(out_buffer, dtype, max(1, nrows) * ncols, out == "device",
+                                                           config.device)
     h = get_handle(config.device, config.total_GPU_budget, config.tile_config, config.pinned_ring_bytes, 0)
     keep = _Keep()
     cop, ct, cb, cq = c_operator2d(operator), c_curve_space(X, keep), c_curve_space(Y, keep), c_quadstrat2d(quadstrat)
@@ -292,7 +327,7 @@ def _assemble_curve(operator, X, Y, config, quadstrat, out, dtype, rows, out_buf
     lib = _lib.load()
     if out == "host":
         Z = np.empty((nrows, ncols), dtype=dtype, order="F") if out_buffer is None else out_buffer
-        ptr = Z.data_ptr() if hasattr(Z, "data_ptr") else Z.ctypes.data
+        ptr = Z.ctypes.data if out_buffer is None else buf_ptr
         kind = _lib.OUT_HOST_C64 if c64 else _lib.OUT_HOST_C32
         _lib.check(lib.bgb_assemble_curve(h.ptr, C.byref(cop), C.byref(ct), C.byref(cb), C.byref(cq), prec,
                                           C.c_void_p(ptr), kind, max(1, nrows), row0, nrows, None, C.byref(stats)))
