@@ -280,11 +280,14 @@ const TileCfg kTileCfgs[] = {
     {32, 32, 2},    // 14
     {40, 40, 4},    // 15
     {24, 24, 8},    // 16
+    {60, 64, 5},    // 17: mixed, RWG (~50 test triangles x 5 = one round of 256 pairs per chunk)
 };
 // Preference order when the caller does not pin a tile: the first whose shared memory fits.
-const int kPrefMixed[] = {4, 8, 1, 5, 6, 7};
+// RWG: 60 x 64 tiles with 5-triangle chunks (C2 mixed far stage 28.6 ms against 31.1 ms for
+// 64 x 64 x 4, whose ~53 test triangles x 4 leave a sixth of the 256 threads idle in each chunk).
+const int kPrefMixed[] = {17, 4, 8, 1, 5, 6, 7};
 const int kNumPrefMixed = sizeof(kPrefMixed) / sizeof(int);
-const int kPrefFp64[] = {4, 8, 5, 6, 7};
+const int kPrefFp64[] = {17, 4, 8, 5, 6, 7};
 const int kNumPrefFp64 = sizeof(kPrefFp64) / sizeof(int);
 // Lagrange hats have ~6 supports: small function blocks keep the halo and the gather short
 // (measured on the two-plate Helmholtz case: 32 x 32 tiles 6x faster than 64 x 64).
