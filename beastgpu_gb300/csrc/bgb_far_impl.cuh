@@ -884,8 +884,52 @@ __device__ __forceinline__ void tile_body(const FarConst& K, const TilePlan& p, 
   for (int i = tid; i < fm * fn; i += kThreads) s.Zs[i] = P::mk(0.0, 0.0);
   if (tid == 0) *s_nonfar = 0;
   __syncthreads();
-  // Does the tile hold any non-far pair?  Most tiles do not, and skip the per-pair test.
-  for (int i = tid; i < tm; i += kThreads) {
+  // Does the tile hold any non-far pair?  Most tiles do not, and skip the per-pair test.  First a
+  // sphere around each block's triangle spheres (warp 0: test block, warp 1: trial block): blocks
+  // whose spheres are clearly apart hold no pair that passes the per-pair sphere test, so no
+  // non-far pair; only the other tiles scan their test triangles' lists of non-far pairs.
+  __shared__ float4 s_blk[2];
+  if (tid < 64) {
+    const int w = tid >> 5, lane = tid & 31;
+    const float4* __restrict__ bl = w ? s.bndB : s.bndT;
+    const int nb = w ? nbk : tm;
+    float cx = 0.f, cy = 0.f, cz = 0.f;
+    for (int i = lane; i < nb; i += 32) {
+      cx += bl[i].x;
+      cy += bl[i].y;
+      cz += bl[i].z;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      cx += __shfl_xor_sync(0xffffffffu, cx, o);
+      cy += __shfl_xor_sync(0xffffffffu, cy, o);
+      cz += __shfl_xor_sync(0xffffffffu, cz, o);
+    }
+    const float inv = 1.f / (float)max(nb, 1);
+    cx *= inv;
+    cy *= inv;
+    cz *= inv;
+    float r = 0.f;
+    for (int i = lane; i < nb; i += 32) {
+      const float dx = bl[i].x - cx, dy = bl[i].y - cy, dz = bl[i].z - cz;
+      r = fmaxf(r, sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz))) + bl[i].w);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r = fmaxf(r, __shfl_xor_sync(0xffffffffu, r, o));
+    if (lane == 0) s_blk[w] = make_float4(cx, cy, cz, r);
+  }
+  __syncthreads();
+  bool blocks_apart;
+  {
+    const float4 A = s_blk[0], B = s_blk[1];
+    const float dx = A.x - B.x, dy = A.y - B.y, dz = A.z - B.z;
+    // margin over the FP32 rounding of the block spheres (sums of ~64 centres: relative to the
+    // coordinates' size) and of the per-pair test
+    const float mag = fmaxf(fmaxf(fabsf(A.x), fabsf(A.y)), fmaxf(fabsf(A.z), fmaxf(fmaxf(fabsf(B.x), fabsf(B.y)), fabsf(B.z))));
+    const float lim = 1.001f * (A.w + B.w) + 1e-5f * mag + 1e-30f;
+    blocks_apart = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) > lim * lim;  // false for NaN: scan
+  }
+  for (int i = tid; i < (blocks_apart ? 0 : tm); i += kThreads) {
     const int T = s.triT[i];
     for (int64_t e = p.sing_off[T], e1 = p.sing_off[T + 1]; e < e1; ++e) {
       const int sg = p.sing_sigma[e];
