@@ -193,11 +193,18 @@ int make_opparams(const bgb_operator* op, const bgb_space* a, const bgb_space* b
 }
 
 FarConst make_farconst(const OpParams& op, const RuleTable& R, const QuadSel& qs, const bgb_space* test,
-                       const bgb_space* trial) {
+                       const bgb_space* trial, SpaceExtents* ext_t, SpaceExtents* ext_b) {
   FarConst k{};
+  SpaceExtents et{}, eb{};
+  if (test && trial) {
+    et = space_extents(test);
+    eb = same_space(test, trial) ? et : space_extents(trial);
+  }
+  if (ext_t) *ext_t = et;
+  if (ext_b) *ext_b = eb;
   // |k delta| <= k (r_test + r_trial) < k (edge_test + edge_trial): within pi, the point-pair phase
   // phi0 + k delta stays in [-2 pi, 2 pi] and goes to sin / cos without a second reduction
-  k.phase_direct = test && trial && std::fabs(op.gamma[1]) * (max_edge(test) + max_edge(trial)) <= 3.14159;
+  k.phase_direct = test && trial && std::fabs(op.gamma[1]) * (et.max_edge + eb.max_edge) <= 3.14159;
   k.op_kind = op.kind;
   k.qt = R.npoints[qs.far_t];
   k.qb = R.npoints[qs.far_b];
@@ -227,7 +234,7 @@ FarConst make_farconst(const OpParams& op, const RuleTable& R, const QuadSel& qs
   // plain FP64 kernel: series for exp(-i k (R - R0)) when |k (R - R0)| <= k (r_test + r_trial) is small
   k.tay_n = 0;
   if (test && trial && op.gamma[1] != 0.0) {
-    const double xmax = std::fabs(op.gamma[1]) * (max_centroid_radius(test) + max_centroid_radius(trial));
+    const double xmax = std::fabs(op.gamma[1]) * (et.max_centroid_radius + eb.max_centroid_radius);
     if (xmax <= 2.0) {
       double fs = 1.0, fc = 1.0;  // (2j+1)!, (2j)!
       int n = 1;
@@ -340,6 +347,28 @@ double max_edge(const bgb_space* s) {
       m = std::max(m, d);
     }
   return m;
+}
+
+// Longest edge and largest vertex-to-centroid distance of a space, in one pass.
+SpaceExtents space_extents(const bgb_space* s) {
+  double me = 0.0, mc = 0.0;
+  for (int64_t t = 0; t < s->nt; ++t) {
+    const double* v[3];
+    for (int a = 0; a < 3; ++a) v[a] = s->vertices + 3 * (int64_t)s->triangles[3 * t + a];
+    double c[3];
+    for (int k = 0; k < 3; ++k) c[k] = (v[0][k] + v[1][k] + v[2][k]) / 3.0;
+    for (int a = 0; a < 3; ++a) {
+      const double* q = v[(a + 1) % 3];
+      double e2 = 0.0, d2 = 0.0;
+      for (int k = 0; k < 3; ++k) {
+        e2 += (v[a][k] - q[k]) * (v[a][k] - q[k]);
+        d2 += (v[a][k] - c[k]) * (v[a][k] - c[k]);
+      }
+      me = std::max(me, e2);
+      mc = std::max(mc, d2);
+    }
+  }
+  return SpaceExtents{std::sqrt(me), std::sqrt(mc) * (1.0 + 1e-12)};
 }
 
 // Largest distance of a vertex from its triangle's centroid: bounds |x - c| for every rule point x.
@@ -569,7 +598,8 @@ int bgb_create(bgb_handle** out, const bgb_config* cfg) {
   if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess ||
       (e = cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking)) != cudaSuccess ||
       (e = cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking)) != cudaSuccess ||
-      (e = cudaStreamCreateWithFlags(&h->stream_sing, cudaStreamNonBlocking)) != cudaSuccess) {
+      (e = cudaStreamCreateWithFlags(&h->stream_sing, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaStreamCreateWithFlags(&h->stream_up, cudaStreamNonBlocking)) != cudaSuccess) {
     rc = cuda_fail(e, "cudaStreamCreate");
   }
   for (int i = 0; i < 8 && !rc; ++i)
@@ -578,6 +608,8 @@ int bgb_create(bgb_handle** out, const bgb_config* cfg) {
     if ((e = cudaEventCreate(&h->ev2[i])) != cudaSuccess) rc = cuda_fail(e, "cudaEventCreate");
   for (int i = 0; i < 2 && !rc; ++i)
     if ((e = cudaEventCreateWithFlags(&h->ring_ev[i], cudaEventDisableTiming)) != cudaSuccess) rc = cuda_fail(e, "cudaEventCreate");
+  for (int i = 0; i <= bgb_handle::kSlots && !rc; ++i)
+    if ((e = cudaEventCreateWithFlags(&h->ev_up[i], cudaEventDisableTiming)) != cudaSuccess) rc = cuda_fail(e, "cudaEventCreate");
   if (!rc) {
     // the abort flag and, 64 bytes further, the mailbox
     int* p = nullptr;
@@ -606,14 +638,15 @@ int bgb_destroy(bgb_handle* h) {
   if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
   if (h->stream2) cudaStreamSynchronize(h->stream2);
   if (h->stream_sing) cudaStreamSynchronize(h->stream_sing);
+  if (h->stream_up) cudaStreamSynchronize(h->stream_up);
   DevBuf* bufs[] = {&h->verts_t, &h->tris_t, &h->verts_b, &h->tris_b, &h->geo_t, &h->geo_b, &h->bnd_t, &h->bnd_b, &h->bnd_c,
                     &h->rec_t, &h->rec_b, &h->cls_count, &h->cls_off, &h->ent_tau, &h->ent_sigma, &h->ent_cls, &h->ent_mask, &h->geodf_t, &h->geodf_b,
                     &h->sing_L, &h->err, &h->df_tab, &h->tplan_i, &h->tplan_l, &h->tplan_d, &h->tplan_f,
-                    &h->diag_a, &h->diag_b, &h->diag_c, &h->diag_d, &h->grp_tri, &h->grp_cnt, &h->grp_off, &h->grp_perm};
+                    &h->diag_a, &h->diag_b, &h->diag_c, &h->diag_d, &h->grp_tri, &h->grp_cnt, &h->grp_off, &h->grp_perm, &h->cls_hist};
   for (DevBuf* b : bufs) b->release();
   h->curve.release();
   for (int k = 0; k < bgb_handle::kSlots; ++k) {
-    DevBuf* slot_bufs[] = {&h->plan_i[k], &h->plan_l[k], &h->plan_d[k], &h->plan_f[k], &h->far_items[k], &h->far_const[k],
+    DevBuf* slot_bufs[] = {&h->plan_i[k], &h->plan_l[k], &h->plan_d[k], &h->plan_f[k], &h->far_const[k],
                            &h->stage[k]};
     for (DevBuf* b : slot_bufs) b->release();
   }
@@ -622,6 +655,8 @@ int bgb_destroy(bgb_handle* h) {
   for (int i = 0; i < 4 * bgb_handle::kSlots; ++i)
     if (h->ev2[i]) cudaEventDestroy(h->ev2[i]);
   for (cudaEvent_t x : h->grp_ev) cudaEventDestroy(x);
+  for (int i = 0; i <= bgb_handle::kSlots; ++i)
+    if (h->ev_up[i]) cudaEventDestroy(h->ev_up[i]);
   for (int i = 0; i < 2; ++i)
     if (h->ring_ev[i]) cudaEventDestroy(h->ring_ev[i]);
   if (h->ring) cudaFreeHost(h->ring);
@@ -629,6 +664,7 @@ int bgb_destroy(bgb_handle* h) {
   if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
   if (h->stream2) cudaStreamDestroy(h->stream2);
   if (h->stream_sing) cudaStreamDestroy(h->stream_sing);
+  if (h->stream_up) cudaStreamDestroy(h->stream_up);
   if (h->abort_host) cudaFreeHost((void*)h->abort_host);
   delete h;
   return 0;
@@ -817,7 +853,8 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
   }
 
   RuleTable R = make_rules();
-  const FarConst K = make_farconst(opp, R, qsel, test, trial);
+  SpaceExtents ext_t{}, ext_b{};
+  const FarConst K = make_farconst(opp, R, qsel, test, trial, &ext_t, &ext_b);
   const int gen = far_generic_q(K.qt, K.qb);
   const bool same = same_space(test, trial);
   const int64_t ncols = trial->nfun;
@@ -828,12 +865,12 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
   // to the HBM budget with two device staging buffers, and a large output is cut into about
   // 16 blocks (of at least 64 MiB) so that every copy but the last overlaps the far kernel of
   // the next block.
-  size_t freeb = 0, totalb = 0;
-  cudaMemGetInfo(&freeb, &totalb);
-  const int64_t budget = h->cfg.hbm_budget_bytes > 0 ? h->cfg.hbm_budget_bytes : (int64_t)(0.9 * (double)freeb);
   const int64_t per_col = (int64_t)esz * nrows;
   int64_t cols_per_block = ncols;
   if (host_out) {
+    size_t freeb = 0, totalb = 0;
+    if (h->cfg.hbm_budget_bytes <= 0) cudaMemGetInfo(&freeb, &totalb);
+    const int64_t budget = h->cfg.hbm_budget_bytes > 0 ? h->cfg.hbm_budget_bytes : (int64_t)(0.9 * (double)freeb);
     cols_per_block = std::max<int64_t>(1, budget / std::max<int64_t>(1, 4 * per_col));
     const int64_t overlap_cols = std::max<int64_t>((ncols + 15) / 16, ((int64_t)64 << 20) / std::max<int64_t>(1, per_col));
     cols_per_block = std::min(std::min(cols_per_block, overlap_cols), ncols);
@@ -1033,13 +1070,22 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
     launches += trial->nt > 0;
   }
   // 1. classification
+  auto host_ms = [&]() { return std::chrono::duration<double, std::milli>(clk::now() - t_start).count(); };
+  double hm[6] = {host_ms(), 0, 0, 0, 0, 0};  // host marks for BGB_TRACE
   int64_t nsing = 0;
   if ((rc = classify_all(h, test, trial, gt, gb, opp.k2, &nsing))) return rc;
+  hm[1] = host_ms();
   launches += 6;  // 2 bounds, 2 classify passes, scan (+1 singular below)
+  if (stats) {  // entries per class, published to the mailbox (read after the final synchronisation)
+    if ((rc = h->cls_hist.ensure(sizeof(unsigned long long) * 5))) return rc;
+    launch_class_hist(h->ent_cls.as<int8_t>(), nsing, h->cls_hist.as<unsigned long long>(), h->num_sms, h->stream);
+    launch_publish(h->cls_hist.as<int>(), 10, h->mbox_dev, h->stream);
+    launches += nsing > 0 ? 2 : 1;
+  }
   cudaEventRecord(h->ev[1], h->stream);
   // 2. singular / near pairs: FP64 kernel (plain path), double-float kernel (mixed path)
   if ((rc = h->sing_L.ensure(sizeof(double2) * 9 * std::max<int64_t>(1, nsing)))) return rc;
-  const bool use_df = precision == BGB_PREC_MIXED && df_singular_ok(opp, max_edge(test), same ? max_edge(test) : max_edge(trial));
+  const bool use_df = precision == BGB_PREC_MIXED && df_singular_ok(opp, ext_t.max_edge, ext_b.max_edge);
   std::vector<float> df_host;  // uploaded asynchronously: lives until the end of the call
   DfTables M{};
   const GeoDf* dgt = nullptr;
@@ -1123,6 +1169,7 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
   }
   BGB_CUDA(cudaGetLastError());
   cudaEventRecord(h->ev[2], h->stream);
+  hm[2] = host_ms();
   // 3. far-pair records
   const int rst = rec_stride(precision, K.qt, gen), rsb = rec_stride(precision, K.qb, gen);
   const size_t rsz = precision == BGB_PREC_MIXED ? sizeof(float) : sizeof(double);
@@ -1134,6 +1181,7 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
 
   // 4. the host plan (joined here) and the test-side tables, uploaded once
   planner.join();
+  hm[3] = host_ms();
   st.ms_plan = PL.ms;
   if (PL.cfg_id < 0) {
     cudaStreamSynchronize(h->stream);
@@ -1156,9 +1204,12 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
       (rc = h->tplan_d.ensure(sizeof(double) * std::max<size_t>(1, PT.fs_coef.size()))) ||
       (rc = h->tplan_f.ensure(sizeof(float) * std::max<size_t>(1, TF.size()))))
     return rc;
-  if ((rc = upload(h, h->tplan_i, TI, 0)) || (rc = upload(h, h->tplan_l, PT.rows, 0)) ||
-      (rc = upload(h, h->tplan_d, PT.fs_coef, 0)) || (rc = upload(h, h->tplan_f, TF, 0)))
+  // uploads on their own stream: a pageable upload queued behind the singular kernels would hold
+  // the host until they end
+  if ((rc = upload_on(h->stream_up, h->tplan_i, TI)) || (rc = upload_on(h->stream_up, h->tplan_l, PT.rows)) ||
+      (rc = upload_on(h->stream_up, h->tplan_d, PT.fs_coef)) || (rc = upload_on(h->stream_up, h->tplan_f, TF)))
     return rc;
+  BGB_CUDA(cudaEventRecord(h->ev_up[bgb_handle::kSlots], h->stream_up));
   int per_sm = 0;
   if ((rc = far_persistent_occupancy(precision, K.op_kind, gen, smem, &per_sm))) return rc;
   const int ntb = (int)PT.tb_off.size() - 1;
@@ -1187,7 +1238,6 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
     std::vector<int> I;
     std::vector<int64_t> L;
     std::vector<float> F;
-    std::vector<int4> items;
     TilePlan T;
   };
   SlotHost slot_host[NS];
@@ -1207,7 +1257,6 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
     H.I.clear();
     H.L.clear();
     H.F.clear();
-    H.items.clear();
     const size_t o_bb_off = cat_i(H.I, PB.bb_off), o_bb_tris = cat_i(H.I, PB.bb_tris), o_bb_fn = cat_i(H.I, PB.bb_fn_off),
                  o_bb_ch = cat_i(H.I, PB.bb_chunk_off), o_ch_grp = cat_i(H.I, PB.ch_grp_off),
                  o_grp_fn = cat_i(H.I, PB.grp_fn), o_grp_sup = cat_i(H.I, PB.grp_sup_off),
@@ -1219,20 +1268,24 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
     const size_t o_gs_coef = 0;
     pairs_computed += (int64_t)PT.tb_tris.size() * (int64_t)PB.bb_tris.size();
     const int nbb = (int)PB.bb_off.size() - 1;
-    H.items.reserve((size_t)ntb * nbb);  // tiles, row block fastest (neighbouring rows of a column together)
-    for (int bn = 0; bn < nbb; ++bn)
-      for (int bm = 0; bm < ntb; ++bm) H.items.push_back(make_int4(0, bm, bn, 0));
+    // tiles t = bn * ntb + bm (row block fastest: neighbouring rows of a column together); the
+    // kernel derives (bm, bn) from t, no item list
+    const int64_t ntiles = (int64_t)ntb * nbb;
     int rc2;
     if ((rc2 = h->plan_i[slot].ensure(sizeof(int) * std::max<size_t>(1, H.I.size()))) ||
         (rc2 = h->plan_l[slot].ensure(sizeof(int64_t) * std::max<size_t>(1, H.L.size()))) ||
         (rc2 = h->plan_d[slot].ensure(sizeof(double) * std::max<size_t>(1, PB.gs_coef.size()))) ||
         (rc2 = h->plan_f[slot].ensure(sizeof(float) * std::max<size_t>(1, H.F.size()))) ||
-        (rc2 = h->far_items[slot].ensure(sizeof(int4) * std::max<size_t>(1, H.items.size()))) ||
         (rc2 = h->far_const[slot].ensure(sizeof(FarConst) + sizeof(TilePlan) + sizeof(int) * 4)))
       return rc2;
+    if (ntiles > INT32_MAX) {
+      set_error("%lld tiles in one output block", (long long)ntiles);
+      return BGB_ERR_CAPACITY;
+    }
     if (host_out && (rc2 = h->stage[slot].ensure(esz * (size_t)cols_per_block * nrows))) return rc2;
-    if ((rc2 = upload_on(cst, h->plan_i[slot], H.I)) || (rc2 = upload_on(cst, h->plan_l[slot], H.L)) ||
-        (rc2 = upload_on(cst, h->plan_d[slot], PB.gs_coef)) || (rc2 = upload_on(cst, h->plan_f[slot], H.F)))
+    cudaStream_t up = h->stream_up;
+    if ((rc2 = upload_on(up, h->plan_i[slot], H.I)) || (rc2 = upload_on(up, h->plan_l[slot], H.L)) ||
+        (rc2 = upload_on(up, h->plan_d[slot], PB.gs_coef)) || (rc2 = upload_on(up, h->plan_f[slot], H.F)))
       return rc2;
     const int* ti = h->tplan_i.as<int>();
     const int* bi = h->plan_i[slot].as<int>();
@@ -1281,17 +1334,17 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
     FarConst* dK = (FarConst*)h->far_const[slot].p;
     TilePlan* dT = (TilePlan*)((char*)h->far_const[slot].p + sizeof(FarConst));
     int* dctr = (int*)((char*)h->far_const[slot].p + sizeof(FarConst) + sizeof(TilePlan));
-    BGB_CUDA(cudaMemcpyAsync(dK, &K, sizeof(FarConst), cudaMemcpyHostToDevice, cst));
-    BGB_CUDA(cudaMemcpyAsync(dT, &T, sizeof(TilePlan), cudaMemcpyHostToDevice, cst));
-    if (!H.items.empty())
-      BGB_CUDA(cudaMemcpyAsync(h->far_items[slot].p, H.items.data(), sizeof(int4) * H.items.size(),
-                               cudaMemcpyHostToDevice, cst));
-    BGB_CUDA(cudaMemsetAsync(dctr, 0, sizeof(int), cst));
-    const int ctas = (int)std::min<int64_t>((int64_t)H.items.size(), (int64_t)std::max(1, per_sm) * h->num_sms);
+    BGB_CUDA(cudaMemcpyAsync(dK, &K, sizeof(FarConst), cudaMemcpyHostToDevice, up));
+    BGB_CUDA(cudaMemcpyAsync(dT, &T, sizeof(TilePlan), cudaMemcpyHostToDevice, up));
+    BGB_CUDA(cudaMemsetAsync(dctr, 0, sizeof(int), up));
+    BGB_CUDA(cudaEventRecord(h->ev_up[slot], up));
+    BGB_CUDA(cudaStreamWaitEvent(cst, h->ev_up[slot], 0));
+    BGB_CUDA(cudaStreamWaitEvent(cst, h->ev_up[NS], 0));  // test-side tables
+    const int ctas = (int)std::min<int64_t>(ntiles, (int64_t)std::max(1, per_sm) * h->num_sms);
     if (grouped) BGB_CUDA(cudaStreamWaitEvent(cst, h->grp_ev[(size_t)b], 0));  // singular groups 0 .. b
     BGB_CUDA(cudaEventRecord(h->ev2[slot * 4 + 0], cst));
-    if ((rc2 = launch_far_persistent(precision, K.op_kind, gen, dK, dT, (const int4*)h->far_items[slot].p,
-                                     (int)H.items.size(), dctr, smem, std::max(1, ctas), h->abort_dev, cst)))
+    if ((rc2 = launch_far_persistent(precision, K.op_kind, gen, dK, dT, nullptr, (int)ntiles, dctr, smem,
+                                     std::max(1, ctas), h->abort_dev, cst)))
       return rc2;
     ++launches;
     BGB_CUDA(cudaEventRecord(h->ev2[slot * 4 + 1], cst));
@@ -1347,6 +1400,7 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
     BGB_CUDA(cudaEventRecord(h->ev2[slot * 4 + 3], cs));
     return 0;
   };
+  hm[4] = host_ms();
   const auto t_pipe = clk::now();
   // the second compute stream starts after everything enqueued so far (classification, singular
   // pairs, records, test-side tables)
@@ -1356,6 +1410,7 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
     cudaStreamSynchronize(h->stream);
     cudaStreamSynchronize(h->stream2);
     cudaStreamSynchronize(h->stream_sing);
+    cudaStreamSynchronize(h->stream_up);
     cudaStreamSynchronize(h->copy_stream);
     return code;
   };
@@ -1368,6 +1423,7 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
   BGB_CUDA(cudaStreamSynchronize(h->stream));
   BGB_CUDA(cudaStreamSynchronize(h->stream2));
   BGB_CUDA(cudaStreamSynchronize(h->stream_sing));
+  BGB_CUDA(cudaStreamSynchronize(h->stream_up));
   BGB_CUDA(cudaStreamSynchronize(h->copy_stream));
   for (int k = 0; k < NS; ++k) harvest(k);
   const double ms_pipe = std::chrono::duration<double, std::milli>(clk::now() - t_pipe).count();
@@ -1384,6 +1440,9 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
   st.pairs_computed = pairs_computed;
   st.ms_classify = event_ms(h->ev[0], h->ev[1]);
   if (trace)
+    fprintf(stderr, "bgb trace host: upload %.3f classified %.3f singular enqueued %.3f planner joined %.3f tables %.3f ms\n",
+            hm[0], hm[1], hm[2], hm[3], hm[4]);
+  if (trace)
     fprintf(stderr, "bgb trace: classify end %.3f, singular end %.3f, pipeline start %.3f (host) ms\n",
             event_ms(h->ev[0], h->ev[1]), event_ms(h->ev[0], grouped ? h->ev[5] : h->ev[2]),
             std::chrono::duration<double, std::milli>(t_pipe - t_start).count());
@@ -1391,12 +1450,9 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
   st.ms_singular = event_ms(h->ev[1], h->ev[2]) + (grouped ? event_ms(h->ev[4], h->ev[5]) : 0.0);
   st.ms_far = ms_far;
   if (stats) {
-    std::vector<int8_t> cls((size_t)nsing);
-    if (nsing) BGB_CUDA(cudaMemcpy(cls.data(), h->ent_cls.p, nsing, cudaMemcpyDeviceToHost));
-    int64_t cnt[5] = {0, 0, 0, 0, 0};
-    for (int8_t c : cls) cnt[(int)c]++;
-    cnt[0] = st.pairs_total - nsing;
-    for (int c = 0; c < 5; ++c) st.pairs_class[c] = cnt[c];
+    for (int c = 1; c < 5; ++c)
+      st.pairs_class[c] = (int64_t)(((uint64_t)(uint32_t)h->mbox_host[2 * c + 1] << 32) | (uint32_t)h->mbox_host[2 * c]);
+    st.pairs_class[0] = st.pairs_total - nsing;
   }
   st.ms_total = std::chrono::duration<double, std::milli>(clk::now() - t_start).count();
   st.kernel_launches = launches;

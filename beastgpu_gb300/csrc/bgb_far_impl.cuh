@@ -1040,7 +1040,8 @@ __device__ __forceinline__ void tile_body(const FarConst& K, const TilePlan& p, 
 }
 
 // The far kernel: persistent CTAs pull tiles (problem, bm, bn) from a work queue (an atomic
-// counter; no CTA ever waits on another).  A single assembly is a one-problem queue.  Each
+// counter; no CTA ever waits on another): items[t], or without a list the tiles of plans[0] with
+// the row block fastest.  A single assembly is a one-problem queue.  Each
 // problem has its own constants (wave number, alpha, beta) and plan; the tile shape and rules
 // are common to the launch.  The problem's constants and plan are copied to shared memory
 // per tile.
@@ -1059,7 +1060,14 @@ __global__ void __launch_bounds__(kThreads, P::kMinBlocks) k_far_persistent(cons
     __syncthreads();
     const int t = next;
     if (t >= nitems) return;
-    const int4 it = items[t];
+    // an item list (batches), or tile t = bn * n_tblocks + bm of the single plan
+    int4 it;
+    if (items) {
+      it = items[t];
+    } else {
+      const int ntb = plans[0].n_tblocks;
+      it = make_int4(0, t % ntb, t / ntb, 0);
+    }
     for (int i = threadIdx.x; i < (int)(sizeof(FarConst) / 4); i += kThreads)
       ((int*)&sK)[i] = ((const int*)&Ks[it.x])[i];
     for (int i = threadIdx.x; i < (int)(sizeof(TilePlan) / 4); i += kThreads)

@@ -72,8 +72,9 @@ struct bgb_handle {
   bgb::DevBuf verts_t, tris_t, verts_b, tris_b, geo_t, geo_b, bnd_t, bnd_b, bnd_c, rec_t, rec_b;
   bgb::DevBuf cls_count, cls_off, ent_tau, ent_sigma, ent_cls, ent_mask, sing_L, err, geodf_t, geodf_b;
   bgb::DevBuf grp_tri, grp_cnt, grp_off, grp_perm;  // singular entries grouped by output block
+  bgb::DevBuf cls_hist;                             // entries per class (statistics)
   static constexpr int kSlots = 3;  // output-block slots in flight (staging, plan tables, events)
-  bgb::DevBuf plan_i[kSlots], plan_l[kSlots], plan_d[kSlots], plan_f[kSlots], far_items[kSlots], far_const[kSlots], df_tab;
+  bgb::DevBuf plan_i[kSlots], plan_l[kSlots], plan_d[kSlots], plan_f[kSlots], far_const[kSlots], df_tab;
   bgb::DevBuf tplan_i, tplan_l, tplan_d, tplan_f;  // test-side tile tables (shared by all output blocks)
   bgb::DevBuf stage[kSlots];
   bgb::DevBuf diag_a, diag_b, diag_c, diag_d;
@@ -81,6 +82,8 @@ struct bgb_handle {
   cudaEvent_t ev[8] = {};
   cudaEvent_t ev2[4 * kSlots] = {};  // per output-block slot: far start / end, copy start / end
   cudaStream_t stream_sing = nullptr;  // singular groups of a host output in blocks
+  cudaStream_t stream_up = nullptr;    // uploads of the far kernels' tile tables (never behind a kernel)
+  cudaEvent_t ev_up[kSlots + 1] = {};  // per slot: its block's tables uploaded; [kSlots]: test-side tables
   std::vector<cudaEvent_t> grp_ev;     // end of each singular group (grown on demand)
   cudaEvent_t ring_ev[2] = {};
   void* ring = nullptr;      // pinned host staging ring
@@ -121,10 +124,14 @@ int validate_space(const bgb_space* s, const char* name);
 int make_quadsel(const bgb_quadstrat* qs, QuadSel* out);
 int make_opparams(const bgb_operator* op, const bgb_space* a, const bgb_space* b, OpParams* out);
 RuleTable make_rules();
+struct SpaceExtents {
+  double max_edge = 0.0, max_centroid_radius = 0.0;
+};
 // Far-kernel constants; with both spaces given, also decides whether the point-pair phase needs
-// no second reduction (phase_direct).
+// no second reduction (phase_direct), and returns the spaces' extents (ext_t, ext_b if given).
 FarConst make_farconst(const OpParams& op, const RuleTable& R, const QuadSel& qs, const bgb_space* test = nullptr,
-                       const bgb_space* trial = nullptr);
+                       const bgb_space* trial = nullptr, SpaceExtents* ext_t = nullptr,
+                       SpaceExtents* ext_b = nullptr);
 Supports build_supports(const bgb_space* s);
 std::vector<double> function_centres(const bgb_space* s, const Supports& S);
 // Functions [f_begin, f_end) in recursive-bisection order of their centres, in compact runs of `leaf`.
@@ -141,6 +148,7 @@ void plan_trial_side_par(const Supports& S, const std::vector<int>& order, int F
 int planner_threads();
 bool same_space(const bgb_space* a, const bgb_space* b);
 // Largest triangle edge of a space (host), for the argument range of the double-float sincos.
+SpaceExtents space_extents(const bgb_space* s);
 double max_edge(const bgb_space* s);
 double max_centroid_radius(const bgb_space* s);
 // True when the mixed path may integrate singular / near pairs in double-float: no lossy

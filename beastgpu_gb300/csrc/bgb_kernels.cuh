@@ -18,6 +18,8 @@ void launch_classify(bool fill, const float4* tb, const float4* bb, const Geo64*
                      double k2, int* count, const int64_t* offset, int* out_tau, int* out_sigma, int8_t* out_cls,
                      int* err, int num_sms, cudaStream_t st, int16_t* out_mask = nullptr, const float4* cb = nullptr);
 void launch_scan(const int* counts, int n, int64_t* offsets, cudaStream_t st);
+// Entries per class of the non-far list: hist[5] (64-bit counts).
+void launch_class_hist(const int8_t* cls, int64_t n, unsigned long long* hist, int num_sms, cudaStream_t st);
 // Singular entries sorted by group: perm[off[g] .. off[g + 1]) are the entries e with
 // tri_group[sigma[e]] == g (out of range: the last group).  counts: ngroups ints, off: ngroups + 1.
 void launch_group_entries(const int* sigma, int64_t n, const int* tri_group, int ngroups, int* counts, int64_t* off,

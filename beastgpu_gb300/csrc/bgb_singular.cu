@@ -228,6 +228,21 @@ __global__ void k_scan_counts(const int* __restrict__ counts, int n, int64_t* __
   if (threadIdx.x == T - 1) offsets[n] = part[T - 1];
 }
 
+// Entries per class (0..4) of the non-far list, warp-aggregated, into hist[5] (zeroed by the caller).
+__global__ void k_class_hist(const int8_t* __restrict__ cls, int64_t n, unsigned long long* __restrict__ hist) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t b = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) & ~(int64_t)31; b < n;
+       b += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = b + lane;
+    const int c = e < n ? (int)cls[e] : -1;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      const unsigned m = __ballot_sync(0xffffffffu, c == k);
+      if (lane == 0 && m) atomicAdd(&hist[k], (unsigned long long)__popc(m));
+    }
+  }
+}
+
 // Singular entries in groups: entry e belongs to group tri_group[ent_sigma[e]] (clamped to
 // [0, ngroups)).  Count per group (a shared histogram when the groups fit), scan, then place each
 // entry at the next free position of its group.  The order inside a group depends on the atomics;
@@ -970,6 +985,11 @@ void launch_classify(bool fill, const float4* tb, const float4* bb, const Geo64*
 }
 void launch_scan(const int* counts, int n, int64_t* offsets, cudaStream_t st) {
   k_scan_counts<<<1, 1024, 0, st>>>(counts, n, offsets);
+}
+void launch_class_hist(const int8_t* cls, int64_t n, unsigned long long* hist, int num_sms, cudaStream_t st) {
+  cudaMemsetAsync(hist, 0, sizeof(unsigned long long) * 5, st);
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)num_sms * 4));
+  if (n > 0) k_class_hist<<<blocks, 256, 0, st>>>(cls, n, hist);
 }
 void launch_group_entries(const int* sigma, int64_t n, const int* tri_group, int ngroups, int* counts, int64_t* off,
                           int* perm, int num_sms, cudaStream_t st) {
