@@ -1044,7 +1044,8 @@ __device__ __forceinline__ void tile_body(const FarConst& K, const TilePlan& p, 
 // the row block fastest.  A single assembly is a one-problem queue.  Each
 // problem has its own constants (wave number, alpha, beta) and plan; the tile shape and rules
 // are common to the launch.  The problem's constants and plan are copied to shared memory
-// per tile.
+// when a CTA's tile belongs to another problem than its previous one; each CTA claims its next
+// tile when it starts a tile.
 template <class P, int OP, int QT, int QB>
 __global__ void __launch_bounds__(kThreads, P::kMinBlocks) k_far_persistent(const FarConst* __restrict__ Ks,
                                                              const TilePlan* __restrict__ plans,
@@ -1055,9 +1056,10 @@ __global__ void __launch_bounds__(kThreads, P::kMinBlocks) k_far_persistent(cons
   __shared__ int next, nonfar;
   __shared__ FarConst sK;
   __shared__ TilePlan sP;
+  if (threadIdx.x == 0) next = (abort_flag && *abort_flag) ? nitems : atomicAdd(counter, 1);
+  __syncthreads();
+  int cur = -1;  // the problem whose constants and plan are in shared memory (the same in all threads)
   for (;;) {
-    if (threadIdx.x == 0) next = (abort_flag && *abort_flag) ? nitems : atomicAdd(counter, 1);
-    __syncthreads();
     const int t = next;
     if (t >= nitems) return;
     // an item list (batches), or tile t = bn * n_tblocks + bm of the single plan
@@ -1068,12 +1070,19 @@ __global__ void __launch_bounds__(kThreads, P::kMinBlocks) k_far_persistent(cons
       const int ntb = plans[0].n_tblocks;
       it = make_int4(0, t % ntb, t / ntb, 0);
     }
-    for (int i = threadIdx.x; i < (int)(sizeof(FarConst) / 4); i += kThreads)
-      ((int*)&sK)[i] = ((const int*)&Ks[it.x])[i];
-    for (int i = threadIdx.x; i < (int)(sizeof(TilePlan) / 4); i += kThreads)
-      ((int*)&sP)[i] = ((const int*)&plans[it.x])[i];
+    if (it.x != cur) {
+      for (int i = threadIdx.x; i < (int)(sizeof(FarConst) / 4); i += kThreads)
+        ((int*)&sK)[i] = ((const int*)&Ks[it.x])[i];
+      for (int i = threadIdx.x; i < (int)(sizeof(TilePlan) / 4); i += kThreads)
+        ((int*)&sP)[i] = ((const int*)&plans[it.x])[i];
+      cur = it.x;
+    }
     __syncthreads();
+    // claim the next tile now: the atomic completes while this one is computed
+    int claimed = 0;
+    if (threadIdx.x == 0) claimed = (abort_flag && *abort_flag) ? nitems : atomicAdd(counter, 1);
     tile_body<P, OP, QT, QB>(sK, sP, it.y, it.z, smem, &nonfar);
+    if (threadIdx.x == 0) next = claimed;
     __syncthreads();
   }
 }
