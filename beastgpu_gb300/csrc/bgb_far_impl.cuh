@@ -858,12 +858,16 @@ __device__ __forceinline__ void tile_body(const FarConst& K, const TilePlan& p, 
     }
   }
   const bool f32 = sizeof(R) == 4;
+  // local matrices of a chunk: entry (i, j) of pair (ti, si) at Lbuf[(i * 3 + j) * LS + ti * SC + si];
+  // supports are staged as their offsets in it (test: (i * 3) * LS + ti * SC, trial: j * LS + slot)
+  const int LS = p.tmax * SC;
   for (int m = tid; m < fm; m += kThreads) {
     const int a0 = p.fs_off[f0 + m], a1 = p.fs_off[f0 + m + 1];
     const int cnt = min(a1 - a0, MAXS);
     s.fcnt[m] = cnt;
     for (int k = 0; k < cnt; ++k) {
-      s.fcode[m * MAXS + k] = p.fs_code[a0 + k];
+      const int fc = p.fs_code[a0 + k];  // test triangle << 2 | local
+      s.fcode[m * MAXS + k] = (fc & 3) * 3 * LS + (fc >> 2) * SC;
       s.fcoef[m * MAXS + k] = f32 ? (R)p.fs_coef32[a0 + k] : (R)p.fs_coef[a0 + k];
     }
   }
@@ -878,7 +882,8 @@ __device__ __forceinline__ void tile_body(const FarConst& K, const TilePlan& p, 
   if (tid == 0) s.grpOff[gb1 - gb0] = sb1 - sb0;
   for (int i = tid; i <= c1 - c0; i += kThreads) s.chGrp[i] = p.ch_grp_off[c0 + i] - gb0;
   for (int i = tid; i < sb1 - sb0; i += kThreads) {
-    s.gsCode[i] = p.gs_code[sb0 + i];
+    const int code = p.gs_code[sb0 + i];  // trial slot << 2 | local
+    s.gsCode[i] = (code & 3) * LS + (code >> 2);
     s.gsCoef[i] = f32 ? (R)p.gs_coef32[sb0 + i] : (R)p.gs_coef[sb0 + i];
   }
   for (int i = tid; i < fm * fn; i += kThreads) s.Zs[i] = P::mk(0.0, 0.0);
@@ -947,12 +952,14 @@ __device__ __forceinline__ void tile_body(const FarConst& K, const TilePlan& p, 
   }
   // fixed roles of this thread: pair (ti0 + k * tstep, si) of a chunk; gather row m, groups gq + k * gstep
   const int tstep = kThreads / SC, ti0 = tid / SC, si = tid - ti0 * SC;
-  const int FMb = p.FM, gstep = kThreads / FMb, gq = tid / FMb, m = tid - gq * FMb;
+  // gather rows in whole warps (one group stream per warp) when that keeps the groups in flight
+  const int FM32 = (p.FM + 31) & ~31;
+  const int FMb = kThreads / FM32 == kThreads / p.FM ? FM32 : p.FM;
+  const int gstep = kThreads / FMb, gq = tid / FMb, m = tid - gq * FMb;
   const bool gather_on = m < fm && gq < gstep;
   __syncthreads();
   const bool check = *s_nonfar != 0;
 
-  const int LS = p.tmax * SC;
   for (int c = c0; c < c1; ++c) {
     const int sbase = (c - c0) * SC;
     const int scn = min(SC, nbk - sbase);
@@ -999,27 +1006,25 @@ __device__ __forceinline__ void tile_body(const FarConst& K, const TilePlan& p, 
         C acc = s.Zs[n * fm + m];
         const int q0 = s.grpOff[gi], q1 = s.grpOff[gi + 1];
         for (int bsup = q0; bsup < q1; ++bsup) {
-          const int code = s.gsCode[bsup];
-          const int sl = (code >> 2) - sbase, j = code & 3;
+          const int col = s.gsCode[bsup] - sbase;
           const R cb = s.gsCoef[bsup];
           if (MAXS <= 2) {
             {
               const R w = fwA * cb;
-              const C l = s.Lbuf[((fcA & 3) * 3 + j) * LS + (fcA >> 2) * SC + sl];
+              const C l = s.Lbuf[fcA + col];
               acc.x = fma(w, l.x, acc.x);
               acc.y = fma(w, l.y, acc.y);
             }
             if (cnt > 1) {
               const R w = fwB * cb;
-              const C l = s.Lbuf[((fcB & 3) * 3 + j) * LS + (fcB >> 2) * SC + sl];
+              const C l = s.Lbuf[fcB + col];
               acc.x = fma(w, l.x, acc.x);
               acc.y = fma(w, l.y, acc.y);
             }
           } else {
             for (int a = 0; a < cnt; ++a) {
-              const int fc = s.fcode[m * MAXS + a];
               const R w = s.fcoef[m * MAXS + a] * cb;
-              const C l = s.Lbuf[((fc & 3) * 3 + j) * LS + (fc >> 2) * SC + sl];
+              const C l = s.Lbuf[s.fcode[m * MAXS + a] + col];
               acc.x = fma(w, l.x, acc.x);
               acc.y = fma(w, l.y, acc.y);
             }
