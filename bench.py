@@ -53,9 +53,9 @@ UNIT = "pair-interactions/s"
 LEVEL, KWAVE = 5, 2 * np.pi * 4
 ERR_ROWS, ERR_SEED = 1000, 0
 # DRAM bytes (read + write) of one far-kernel launch per triangle pair, from the ncu capture of
-# the level-4 case (0.440 GB for 5120^2 pairs, profiles/kernels_efie_icosphere_l4.md); the
-# traffic is the output written once, so it scales with the pairs.
-FAR_DRAM_BYTES_PER_PAIR = 0.440e9 / (5120 * 5120)
+# the level-4 case (0.462 GB for 5120^2 pairs); the traffic is the output written once, so it
+# scales with the pairs.
+FAR_DRAM_BYTES_PER_PAIR = 0.462e9 / (5120 * 5120)
 
 
 def workload():
@@ -210,8 +210,8 @@ def rows_error(Z_rows, ref):
 
 CURVE_N, CURVE_K, CURVE_ROWS = 16384, 2 * np.pi * 100, 64
 # FP64 flops (2 DFMA + DADD + DMUL thread instructions) per far point pair of the plain hypersingular
-# far kernel, counted by ncu on the 4,096-segment case (profiles/curve_hypersingular_ellipse.md), and
-# its DRAM bytes per segment pair (the 2x2 complex double local matrix written once).
+# far kernel, counted by ncu on the 4,096-segment case, and its DRAM bytes per segment pair (the 2x2
+# complex double local matrix written once).
 CURVE_FP64_FLOPS_PER_POINT_PAIR = 239.5
 CURVE_DRAM_BYTES_PER_PAIR = 1.040e9 / (4096 * 4096)
 # The same for the mixed far kernel: FP32 flops (2 FFMA + FADD + FMUL) per far point pair and DRAM
