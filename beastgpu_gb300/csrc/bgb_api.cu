@@ -972,7 +972,7 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
         probe.gsmax = std::max(probe.gsmax, PL.trial[b].gsmax);
         probe.nmax = std::max(probe.nmax, std::max(1, PL.trial[b].nmax));
       }
-      smem = far_smem_bytes(precision, K.qt, K.qb, probe);
+      smem = far_smem_bytes(precision, K.op_kind, K.qt, K.qb, probe);
       // Occupancy: when the widest test tile pushes shared memory past what the kernel's
       // CTAs per SM allow, cap the triangles per test tile at the largest count that fits.
       int occ = 0;
@@ -982,7 +982,7 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
         for (int t = probe.tmax - 1; t >= std::max(1, PL.test.MAXS); --t) {
           TilePlan q = probe;
           q.tmax = t;
-          const size_t sm = far_smem_bytes(precision, K.qt, K.qb, q);
+          const size_t sm = far_smem_bytes(precision, K.op_kind, K.qt, K.qb, q);
           int o = 0;
           if (far_persistent_occupancy(precision, K.op_kind, gen, sm, &o) == 0 && o >= target_occ) {
             cap = t;
@@ -994,7 +994,7 @@ int bgb_assemble(bgb_handle* h, const bgb_operator* op, const bgb_space* test, c
           plan_test_side_par(St, ord_t, tc.FM, row0, PL.test, nth, cap);
           probe.MAXS = PL.test.MAXS;
           probe.tmax = std::max(1, PL.test.tmax);
-          smem = far_smem_bytes(precision, K.qt, K.qb, probe);
+          smem = far_smem_bytes(precision, K.op_kind, K.qt, K.qb, probe);
         }
       }
       occ = 0;

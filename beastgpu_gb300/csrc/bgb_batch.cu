@@ -145,7 +145,8 @@ int build_plans(bgb_batch* B, const bgb_problem* pr, const std::vector<Supports>
   TilePlan probe{};
   probe.FM = tc.FM; probe.FN = tc.FN; probe.SC = tc.SC; probe.MAXS = MAXS;
   probe.gmax = gmax; probe.gsmax = gsmax; probe.tmax = tmax; probe.nmax = nmax;
-  *smem_out = far_smem_bytes(B->precision, B->rules.npoints[B->qsel.far_t], B->rules.npoints[B->qsel.far_b], probe);
+  *smem_out = far_smem_bytes(B->precision, B->op_kind, B->rules.npoints[B->qsel.far_t], B->rules.npoints[B->qsel.far_b],
+                             probe);
   if (!upload_all) return 0;
   // concatenate
   std::vector<int> I;

@@ -97,10 +97,14 @@ int rec_stride(int precision, int q, int generic) {
   return precision == BGB_PREC_MIXED ? farimpl::off32_size(Q) : 13 + 4 * Q;
 }
 
-size_t far_smem_bytes(int precision, int qt, int qb, const TilePlan& p) {
+size_t far_smem_bytes(int precision, int op_kind, int qt, int qb, const TilePlan& p) {
   const bool gen = far_generic_q(qt, qb);
+  // the layout depends on the operator only through chunk_trial_records (Lagrange or RWG)
+  const bool lag = is_lagrange_op(op_kind);
   if (precision == BGB_PREC_MIXED)
-    return gen ? smem_t<PMixed, 0, BGB_MAXQ, BGB_MAXQ>(p) : smem_t<PMixed, 0, 3, 4>(p);
+    return gen ? (lag ? smem_t<PMixed, BGB_OP_HELMHOLTZ3D_SL, BGB_MAXQ, BGB_MAXQ>(p)
+                      : smem_t<PMixed, BGB_OP_MAXWELL3D_SL, BGB_MAXQ, BGB_MAXQ>(p))
+               : (lag ? smem_t<PMixed, BGB_OP_HELMHOLTZ3D_SL, 3, 4>(p) : smem_t<PMixed, BGB_OP_MAXWELL3D_SL, 3, 4>(p));
   return gen ? smem_t<PFp64, 0, BGB_MAXQ, BGB_MAXQ>(p) : smem_t<PFp64, 0, 3, 4>(p);
 }
 

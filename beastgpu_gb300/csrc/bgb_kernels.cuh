@@ -150,7 +150,7 @@ struct TilePlan {
   const volatile int* abort_flag;
 };
 
-size_t far_smem_bytes(int precision, int qt, int qb, const TilePlan& p);
+size_t far_smem_bytes(int precision, int op_kind, int qt, int qb, const TilePlan& p);
 // CTAs per SM the far kernel is compiled for (__launch_bounds__ minimum blocks).
 int far_target_ctas_per_sm(int precision);
 // Persistent batched launch over a work queue of (problem, bm, bn) items (device arrays).
