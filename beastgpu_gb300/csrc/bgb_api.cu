@@ -288,6 +288,7 @@ const TileCfg kTileCfgs[] = {
     {40, 40, 4},    // 15
     {24, 24, 8},    // 16
     {60, 64, 5},    // 17: mixed, RWG (~50 test triangles x 5 = one round of 256 pairs per chunk)
+    {32, 40, 5},    // 18: Lagrange
 };
 // Preference order when the caller does not pin a tile: the first whose shared memory fits.
 // RWG: 60 x 64 tiles with 5-triangle chunks (C2 mixed far stage 28.6 ms against 31.1 ms for
@@ -300,7 +301,9 @@ const int kPrefFp64[] = {4, 8, 5, 6, 7};
 const int kNumPrefFp64 = sizeof(kPrefFp64) / sizeof(int);
 // Lagrange hats have ~6 supports: small function blocks keep the halo and the gather short
 // (measured on the two-plate Helmholtz case: 32 x 32 tiles 6x faster than 64 x 64).
-const int kPrefLagrange[] = {6, 13, 15, 5, 7};
+// d = 40 cube, mixed: 32 x 40 x 5 330 ms, 40 x 40 x 4 334 ms, 32 x 32 x 4 364 ms (with the FP32
+// Lagrange kernels' per-chunk trial staging).
+const int kPrefLagrange[] = {18, 6, 13, 15, 5, 7};
 const int kNumPrefLagrange = sizeof(kPrefLagrange) / sizeof(int);
 const int kNumTileCfgs = sizeof(kTileCfgs) / sizeof(kTileCfgs[0]);
 
