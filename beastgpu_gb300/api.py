@@ -222,7 +222,8 @@ def assemble_gpu(operator: Operator, test_functions: Space, trial_functions: Spa
     "fp64" and complex64 for "mixed" unless `dtype` says otherwise.  out="device": a torch CUDA
     tensor view of shape (rows, cols) with column-major strides.  rows=(row0, nrows) assembles
     a row window.  out_buffer: a preallocated host (numpy or pinned torch) or device (torch)
-    buffer of the right shape/dtype to write into.
+    buffer of the right shape/dtype to write into; its element type, contiguous size and side
+    (host or device) are checked before any device work (ValueError otherwise).
     """
     config = config or GPUConfiguration()
     if config.amount_of_gpus > 1 and rows is None and out == "host" and out_buffer is None \
