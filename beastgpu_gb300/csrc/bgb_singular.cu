@@ -727,10 +727,12 @@ __device__ inline void finalize(const OpParams& op, const Geo64& A, const Geo64&
     }
 }
 
-// Integral of one non-far pair by a warp; every lane returns the full (reduced) matrix.
-template <int OP>
+// Integral of one non-far pair by a warp; every lane returns the full (reduced) matrix.  NEAR:
+// near pairs only (the other branches are not compiled: fewer registers, more warps per SM).
+template <int OP, bool NEAR = false>
 __device__ void pair_integral64(const OpParams& op, const QuadSel& qs, const RuleTable& rules, int cls,
                                 const Geo64& A, const Geo64& B, double2 L[3][3]) {
+  if (NEAR) cls = BGB_CLASS_NEAR;
   constexpr int NA = NAcc<OP>::N;
   const int lane = threadIdx.x & 31;
   double2 acc[NA];
@@ -822,8 +824,8 @@ __device__ void pair_integral64(const OpParams& op, const QuadSel& qs, const Rul
 // Singular / near pairs, one warp per entry.  BATCH: the operator constants of the test
 // triangle's problem (ops[tri_problem[tau]]) instead of op1.  Single and batched assemblies
 // share this code, so their values are bit-identical.
-template <int OP, bool BATCH>
-__global__ void __launch_bounds__(256) k_singular(OpParams op1, const OpParams* __restrict__ ops,
+template <int OP, bool BATCH, bool NEAR = false>
+__global__ void __launch_bounds__(256, NEAR ? 2 : 1) k_singular(OpParams op1, const OpParams* __restrict__ ops,
                                                   const int* __restrict__ tri_problem,
                                                   const __grid_constant__ QuadSel qs,
                                                   const __grid_constant__ RuleTable rules,
@@ -844,7 +846,7 @@ __global__ void __launch_bounds__(256) k_singular(OpParams op1, const OpParams* 
     const OpParams op = BATCH ? ops[tri_problem[tau]] : op1;
     const Geo64 A = tg[tau], B = bg[ent_sigma[e]];
     double2 L[3][3];
-    pair_integral64<OP>(op, qs, rules, ent_cls[e], A, B, L);
+    pair_integral64<OP, NEAR>(op, qs, rules, ent_cls[e], A, B, L);
     if (lane < 9) {
       double2 v = L[0][0];
 #pragma unroll
@@ -853,7 +855,7 @@ __global__ void __launch_bounds__(256) k_singular(OpParams op1, const OpParams* 
       out[e * 9 + lane] = v;
     }
   };
-  if (near_only) {
+  if (NEAR) {
     // near pairs only (the others come from the double-float kernel): a warp reads the classes of
     // 32 entries at once and integrates the near ones among them
     for (int64_t b = i0 + warp0 * 32; b < i1; b += warps * 32) {
@@ -1020,8 +1022,12 @@ void launch_singular(const OpParams& op, const QuadSel& qs, const RuleTable& rul
   const int64_t cap = (int64_t)num_sms * (perm ? 2 : 32);  // a group: about one wave beside a far kernel
   if (blocks > cap) blocks = cap;
 #define BGB_LAUNCH_SING(OPK)                                                                                   \
-  k_singular<OPK, false><<<(int)blocks, 256, 0, st>>>(op, nullptr, nullptr, qs, rules, tg, bg, et, es, ec, n, out, \
-                                                      abort_flag, near_only ? 1 : 0, perm, range)
+  if (near_only)                                                                                                 \
+    k_singular<OPK, false, true><<<(int)blocks, 256, 0, st>>>(op, nullptr, nullptr, qs, rules, tg, bg, et, es, ec, n, \
+                                                              out, abort_flag, 1, perm, range);                    \
+  else                                                                                                           \
+    k_singular<OPK, false><<<(int)blocks, 256, 0, st>>>(op, nullptr, nullptr, qs, rules, tg, bg, et, es, ec, n, out, \
+                                                        abort_flag, 0, perm, range)
   switch (op.kind) {
     case BGB_OP_HELMHOLTZ3D_SL: BGB_LAUNCH_SING(BGB_OP_HELMHOLTZ3D_SL); break;
     case BGB_OP_MAXWELL3D_SL: BGB_LAUNCH_SING(BGB_OP_MAXWELL3D_SL); break;
@@ -1076,8 +1082,12 @@ void launch_singular_batched(int op_kind, const OpParams* ops, const QuadSel& qs
   int64_t blocks = (n + 7) / 8;
   if (blocks > (int64_t)num_sms * 32) blocks = (int64_t)num_sms * 32;
 #define BGB_LAUNCH_SING(OPK)                                                                                  \
-  k_singular<OPK, true><<<(int)blocks, 256, 0, st>>>(OpParams{}, ops, tri_problem, qs, rules, tg, bg, et, es, ec, n, \
-                                                     out, abort_flag, near_only ? 1 : 0, nullptr, nullptr)
+  if (near_only)                                                                                                \
+    k_singular<OPK, true, true><<<(int)blocks, 256, 0, st>>>(OpParams{}, ops, tri_problem, qs, rules, tg, bg, et, es, \
+                                                             ec, n, out, abort_flag, 1, nullptr, nullptr);          \
+  else                                                                                                          \
+    k_singular<OPK, true><<<(int)blocks, 256, 0, st>>>(OpParams{}, ops, tri_problem, qs, rules, tg, bg, et, es, ec, n, \
+                                                       out, abort_flag, 0, nullptr, nullptr)
   switch (op_kind) {
     case BGB_OP_HELMHOLTZ3D_SL: BGB_LAUNCH_SING(BGB_OP_HELMHOLTZ3D_SL); break;
     case BGB_OP_MAXWELL3D_SL: BGB_LAUNCH_SING(BGB_OP_MAXWELL3D_SL); break;
