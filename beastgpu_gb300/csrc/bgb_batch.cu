@@ -433,8 +433,9 @@ int bgb_batch_create(bgb_handle* h, int32_t n, const bgb_problem* problems, int3
   int smem_max = 0;
   cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
   const bool lagrange = problems[0].test.refspace == BGB_REFSPACE_LAGRANGE_C0D1;
-  const int* prefs = lagrange ? kPrefLagrange : precision == BGB_PREC_MIXED ? kPrefMixed : kPrefFp64;
-  const int nprefs = lagrange ? kNumPrefLagrange : precision == BGB_PREC_MIXED ? kNumPrefMixed : kNumPrefFp64;
+  const bool mixed = precision == BGB_PREC_MIXED;
+  const int* prefs = lagrange ? (mixed ? kPrefLagrange : kPrefLagrangeFp64) : mixed ? kPrefMixed : kPrefFp64;
+  const int nprefs = lagrange ? (mixed ? kNumPrefLagrange : kNumPrefLagrangeFp64) : mixed ? kNumPrefMixed : kNumPrefFp64;
   std::vector<int> cands;
   if (h->cfg.tile_config >= 0) cands.push_back(h->cfg.tile_config);
   else

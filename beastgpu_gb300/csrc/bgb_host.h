@@ -119,6 +119,8 @@ extern const int kPrefFp64[];
 extern const int kNumPrefFp64;
 extern const int kPrefLagrange[];
 extern const int kNumPrefLagrange;
+extern const int kPrefLagrangeFp64[];
+extern const int kNumPrefLagrangeFp64;
 
 int validate_space(const bgb_space* s, const char* name);
 int make_quadsel(const bgb_quadstrat* qs, QuadSel* out);
