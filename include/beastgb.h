@@ -141,7 +141,8 @@ int bgb_destroy(bgb_handle* h);
 
 /* Assemble rows [row0, row0 + nrows) of Z (test functions) against all trial functions.
  * nrows < 0 means all rows.  Output is column-major (Julia layout): element (m, n) at
- * out[(m - row0) + n * ld], ld >= nrows.  Device outputs are written on `stream`
+ * out[(m - row0) + n * ld], ld >= nrows; `out` must hold ld * (trial->nfun - 1) + nrows entries of
+ * the out_kind's type (complex double or complex float; the library cannot check).  Device outputs are written on `stream`
  * (a cudaStream_t, NULL = the handle's stream); host outputs are complete on return.
  * BGB_PREC_MIXED reduces the phase k R exactly for k times the diameter of the two meshes up to
  * 3e5 and returns BGB_ERR_NOT_SUPPORTED beyond (use BGB_PREC_FP64 there).
